@@ -1,0 +1,522 @@
+/*
+ * qgt_oracle.c -- FP64 CPU oracle (TEST INFRASTRUCTURE ONLY; see qgt_oracle.h).
+ *
+ * Plain C11 + OpenMP restatement of the reference algorithms on the QGT hot
+ * path.  Nothing here is shipped in or called by the product library.
+ */
+#include "qgt_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+typedef struct { double re, im; } cd;
+
+static inline cd cmul(cd a, cd b) { cd r = {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; return r; }
+static inline cd cadd(cd a, cd b) { cd r = {a.re + b.re, a.im + b.im}; return r; }
+
+/* ------------------------------------------------------------------------ */
+/* circuit construction                                                      */
+/* ------------------------------------------------------------------------ */
+
+/* learning/quantum_pipeline_impl.c:2499-2526: RY(q) for all q, RZ(q) for all
+ * q, then CNOT(q -> q+1).  The CZ ring variant replaces the ladder by
+ * CZ(q, q+1 mod n). */
+int or_build_ansatz(int n, int layers, int entangler, og_gate_t* gates, int max_gates)
+{
+    if (n < 1 || layers < 0) return -1;
+    int nent = entangler == 0 ? n - 1 : (n >= 3 ? n : n - 1);
+    int need = layers * (2 * n + nent);
+    if (!gates) return need;
+    if (need > max_gates) return -1;
+    int g = 0, p = 0;
+    for (int l = 0; l < layers; l++) {
+        for (int q = 0; q < n; q++) gates[g++] = (og_gate_t){OG_RY, q, -1, p++, 0.0};
+        for (int q = 0; q < n; q++) gates[g++] = (og_gate_t){OG_RZ, q, -1, p++, 0.0};
+        if (entangler == 0) {
+            for (int q = 0; q + 1 < n; q++) gates[g++] = (og_gate_t){OG_CNOT, q, q + 1, -1, 0.0};
+        } else {
+            for (int q = 0; q < nent; q++) gates[g++] = (og_gate_t){OG_CZ, q, (q + 1) % n, -1, 0.0};
+        }
+    }
+    return g;
+}
+
+uint64_t or_splitmix64(uint64_t* s)
+{
+    uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+void or_seed_params(uint64_t seed, int count, double* theta)
+{
+    uint64_t s = seed;
+    for (int i = 0; i < count; i++) {
+        double u = (double)(or_splitmix64(&s) >> 11) * (1.0 / 9007199254740992.0);
+        theta[i] = 2.0 * M_PI * u;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* gate application (hybrid/quantum_classical_algorithms.c:174-318)          */
+/* ------------------------------------------------------------------------ */
+
+static double gate_angle(const og_gate_t* g, const double* theta)
+{
+    return g->param >= 0 ? theta[g->param] : g->angle;
+}
+
+/* 2x2 row-major matrix of a single-qubit gate (a2; quantum_classical_algorithms.c:228-276). */
+static void gate_matrix(int type, double a, cd m[4])
+{
+    double c = cos(a / 2.0), s = sin(a / 2.0), r = 1.0 / sqrt(2.0);
+    switch (type) {
+    case OG_RX: m[0] = (cd){c, 0}; m[1] = (cd){0, -s}; m[2] = (cd){0, -s}; m[3] = (cd){c, 0}; break;
+    case OG_RY: m[0] = (cd){c, 0}; m[1] = (cd){-s, 0}; m[2] = (cd){s, 0}; m[3] = (cd){c, 0}; break;
+    case OG_RZ: m[0] = (cd){c, -s}; m[1] = (cd){0, 0}; m[2] = (cd){0, 0}; m[3] = (cd){c, s}; break;
+    case OG_X: m[0] = (cd){0, 0}; m[1] = (cd){1, 0}; m[2] = (cd){1, 0}; m[3] = (cd){0, 0}; break;
+    case OG_Y: m[0] = (cd){0, 0}; m[1] = (cd){0, -1}; m[2] = (cd){0, 1}; m[3] = (cd){0, 0}; break;
+    case OG_Z: m[0] = (cd){1, 0}; m[1] = (cd){0, 0}; m[2] = (cd){0, 0}; m[3] = (cd){-1, 0}; break;
+    case OG_H: m[0] = (cd){r, 0}; m[1] = (cd){r, 0}; m[2] = (cd){r, 0}; m[3] = (cd){-r, 0}; break;
+    case OG_S: m[0] = (cd){1, 0}; m[1] = (cd){0, 0}; m[2] = (cd){0, 0}; m[3] = (cd){0, 1}; break;
+    case OG_T: m[0] = (cd){1, 0}; m[1] = (cd){0, 0}; m[2] = (cd){0, 0}; m[3] = (cd){r, r}; break;
+    default: m[0] = (cd){1, 0}; m[1] = (cd){0, 0}; m[2] = (cd){0, 0}; m[3] = (cd){1, 0}; break;
+    }
+}
+
+/* (-i/2) G for the generator G of a rotation gate (exact entries). */
+static void generator_matrix(int type, cd m[4])
+{
+    switch (type) {
+    case OG_RX: m[0] = (cd){0, 0}; m[1] = (cd){0, -0.5}; m[2] = (cd){0, -0.5}; m[3] = (cd){0, 0}; break;
+    case OG_RY: m[0] = (cd){0, 0}; m[1] = (cd){-0.5, 0}; m[2] = (cd){0.5, 0}; m[3] = (cd){0, 0}; break;
+    default: /* RZ */ m[0] = (cd){0, -0.5}; m[1] = (cd){0, 0}; m[2] = (cd){0, 0}; m[3] = (cd){0, 0.5}; break;
+    }
+}
+
+static void apply_1q(cd* v, size_t dim, int q, const cd m[4])
+{
+    size_t mask = (size_t)1 << q;
+    for (size_t i = 0; i < dim; i++) {
+        if (i & mask) continue;
+        size_t j = i | mask;
+        cd a0 = v[i], a1 = v[j];
+        v[i] = cadd(cmul(m[0], a0), cmul(m[1], a1));
+        v[j] = cadd(cmul(m[2], a0), cmul(m[3], a1));
+    }
+}
+
+static void apply_gate(cd* v, int n, const og_gate_t* g, const double* theta)
+{
+    size_t dim = (size_t)1 << n;
+    if (g->type == OG_CNOT) {
+        size_t cm = (size_t)1 << g->q0, tm = (size_t)1 << g->q1;
+        for (size_t i = 0; i < dim; i++)
+            if ((i & cm) && !(i & tm)) { cd t = v[i]; v[i] = v[i | tm]; v[i | tm] = t; }
+    } else if (g->type == OG_CZ) {
+        size_t am = (size_t)1 << g->q0, bm = (size_t)1 << g->q1;
+        for (size_t i = 0; i < dim; i++)
+            if ((i & am) && (i & bm)) { v[i].re = -v[i].re; v[i].im = -v[i].im; }
+    } else if (g->type == OG_SWAP) {
+        size_t am = (size_t)1 << g->q0, bm = (size_t)1 << g->q1;
+        for (size_t i = 0; i < dim; i++)
+            if ((i & am) && !(i & bm)) { size_t j = (i & ~am) | bm; cd t = v[i]; v[i] = v[j]; v[j] = t; }
+    } else {
+        cd m[4];
+        gate_matrix(g->type, gate_angle(g, theta), m);
+        apply_1q(v, dim, g->q0, m);
+    }
+}
+
+static int is_rotation(int t) { return t == OG_RX || t == OG_RY || t == OG_RZ; }
+
+int or_simulate(int n, const og_gate_t* gates, int ngates, const double* theta, double* psi)
+{
+    if (n < 1 || n > 30) return -1;
+    size_t dim = (size_t)1 << n;
+    cd* v = (cd*)psi;
+    memset(v, 0, dim * sizeof(cd));
+    v[0].re = 1.0;
+    for (int g = 0; g < ngates; g++) apply_gate(v, n, &gates[g], theta);
+    return 0;
+}
+
+/* Exact derivative states: every live derivative vector is transported with
+ * psi; at a parameterised gate for parameter k the vector (-i/2) G_k psi is
+ * added to row k.  This is the exact form of core/quantum_geometric_gradient.c
+ * compute_higher_order_gradient (a4): (psi(theta+pi/2) - psi(theta-pi/2))/(2 sqrt 2). */
+int or_derivatives(int n, const og_gate_t* gates, int ngates, const double* theta,
+                   int nparams, double* psi, double* D)
+{
+    if (n < 1 || n > 30 || nparams < 0) return -1;
+    size_t dim = (size_t)1 << n;
+    cd* v = (cd*)psi;
+    cd* d = (cd*)D;
+    memset(v, 0, dim * sizeof(cd));
+    v[0].re = 1.0;
+    memset(d, 0, (size_t)nparams * dim * sizeof(cd));
+    char* live = (char*)calloc((size_t)nparams + 1, 1);
+    int* live_list = (int*)malloc(sizeof(int) * ((size_t)nparams + 1));
+    if (!live || !live_list) { free(live); free(live_list); return -1; }
+    int nlive = 0;
+    cd* tmp = (cd*)malloc(dim * sizeof(cd));
+    if (!tmp) { free(live); free(live_list); return -1; }
+    for (int g = 0; g < ngates; g++) {
+        const og_gate_t* gt = &gates[g];
+        apply_gate(v, n, gt, theta);
+        #pragma omp parallel for schedule(dynamic, 1)
+        for (int j = 0; j < nlive; j++) apply_gate(d + (size_t)live_list[j] * dim, n, gt, theta);
+        if (is_rotation(gt->type) && gt->param >= 0) {
+            int k = gt->param;
+            if (k >= nparams) { free(live); free(live_list); free(tmp); return -1; }
+            cd m[4];
+            generator_matrix(gt->type, m);
+            memcpy(tmp, v, dim * sizeof(cd));
+            apply_1q(tmp, dim, gt->q0, m);
+            cd* row = d + (size_t)k * dim;
+            #pragma omp parallel for
+            for (size_t i = 0; i < dim; i++) row[i] = cadd(row[i], tmp[i]);
+            if (!live[k]) { live[k] = 1; live_list[nlive++] = k; }
+        }
+    }
+    free(tmp);
+    free(live);
+    free(live_list);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* QGT contraction (a5)                                                      */
+/* ------------------------------------------------------------------------ */
+
+int or_qgt(size_t dim, int P, const double* psi, const double* D, double* Q)
+{
+    const cd* v = (const cd*)psi;
+    const cd* d = (const cd*)D;
+    cd* q = (cd*)Q;
+    cd* proj = (cd*)malloc(sizeof(cd) * (size_t)(P > 0 ? P : 1));
+    if (!proj) return -1;
+    /* proj_m = <d_m|psi> */
+    #pragma omp parallel for
+    for (int m = 0; m < P; m++) {
+        double re = 0, im = 0;
+        const cd* a = d + (size_t)m * dim;
+        for (size_t k = 0; k < dim; k++) {
+            re += a[k].re * v[k].re + a[k].im * v[k].im;
+            im += a[k].re * v[k].im - a[k].im * v[k].re;
+        }
+        proj[m] = (cd){re, im};
+    }
+    /* Q_mn = <d_m|d_n> - <d_m|psi><psi|d_n>, upper triangle then Hermitian mirror */
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int m = 0; m < P; m++) {
+        const cd* a = d + (size_t)m * dim;
+        for (int nn = m; nn < P; nn++) {
+            const cd* b = d + (size_t)nn * dim;
+            double re = 0, im = 0;
+            for (size_t k = 0; k < dim; k++) {
+                re += a[k].re * b[k].re + a[k].im * b[k].im;
+                im += a[k].re * b[k].im - a[k].im * b[k].re;
+            }
+            cd pn = {proj[nn].re, -proj[nn].im}; /* <psi|d_n> */
+            cd pr = cmul(proj[m], pn);
+            cd val = {re - pr.re, im - pr.im};
+            q[(size_t)m * P + nn] = val;
+            q[(size_t)nn * P + m] = (cd){val.re, -val.im};
+        }
+    }
+    free(proj);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* energy and gradient (a8)                                                  */
+/* ------------------------------------------------------------------------ */
+
+static int tfim_bonds(int n) { return n >= 3 ? n : n - 1; }
+
+void or_tfim_apply(int n, double J, double h, const double* psi, double* out)
+{
+    size_t dim = (size_t)1 << n;
+    const cd* v = (const cd*)psi;
+    cd* o = (cd*)out;
+    int nb = tfim_bonds(n);
+    #pragma omp parallel for
+    for (size_t i = 0; i < dim; i++) {
+        /* diagonal: -J sum Z_a Z_b */
+        double zz = 0;
+        for (int b = 0; b < nb; b++) {
+            int qa = b, qb = (b + 1) % n;
+            int za = (i >> qa) & 1, zb = (i >> qb) & 1;
+            zz += (za ^ zb) ? -1.0 : 1.0;
+        }
+        cd acc = {-J * zz * v[i].re, -J * zz * v[i].im};
+        for (int q = 0; q < n; q++) {
+            cd w = v[i ^ ((size_t)1 << q)];
+            acc.re -= h * w.re;
+            acc.im -= h * w.im;
+        }
+        o[i] = acc;
+    }
+}
+
+double or_tfim_energy(int n, double J, double h, const double* psi)
+{
+    size_t dim = (size_t)1 << n;
+    double* hp = (double*)malloc(2 * dim * sizeof(double));
+    if (!hp) return NAN;
+    or_tfim_apply(n, J, h, psi, hp);
+    double e = 0;
+    for (size_t i = 0; i < dim; i++) e += psi[2 * i] * hp[2 * i] + psi[2 * i + 1] * hp[2 * i + 1];
+    free(hp);
+    return e;
+}
+
+void or_energy_grad(size_t dim, int P, const double* D, const double* Hpsi, double* grad)
+{
+    #pragma omp parallel for
+    for (int k = 0; k < P; k++) {
+        const double* a = D + 2 * (size_t)k * dim;
+        double re = 0;
+        for (size_t i = 0; i < dim; i++) re += a[2 * i] * Hpsi[2 * i] + a[2 * i + 1] * Hpsi[2 * i + 1];
+        grad[k] = 2.0 * re;
+    }
+}
+
+int or_param_shift_grad(int n, const og_gate_t* gates, int ngates, const double* theta,
+                        int P, double J, double h, double* grad)
+{
+    size_t dim = (size_t)1 << n;
+    double* th = (double*)malloc(sizeof(double) * (size_t)(P > 0 ? P : 1));
+    double* psi = (double*)malloc(2 * dim * sizeof(double));
+    if (!th || !psi) { free(th); free(psi); return -1; }
+    memcpy(th, theta, sizeof(double) * (size_t)P);
+    for (int k = 0; k < P; k++) {
+        double o = th[k];
+        th[k] = o + M_PI / 2;
+        or_simulate(n, gates, ngates, th, psi);
+        double ep = or_tfim_energy(n, J, h, psi);
+        th[k] = o - M_PI / 2;
+        or_simulate(n, gates, ngates, th, psi);
+        double em = or_tfim_energy(n, J, h, psi);
+        th[k] = o;
+        grad[k] = (ep - em) / 2.0;
+    }
+    free(th);
+    free(psi);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* natural-gradient solves (a7)                                              */
+/* ------------------------------------------------------------------------ */
+
+int or_cholesky_solve(int P, const double* A, double lambda, const double* b, double* x,
+                      double* lambda_used)
+{
+    double* L = (double*)calloc((size_t)P * P, sizeof(double));
+    double* y = (double*)malloc(sizeof(double) * (size_t)P);
+    if (!L || !y) { free(L); free(y); return -1; }
+    for (int attempt = 0; attempt < 12; attempt++) {
+        int ok = 1;
+        memset(L, 0, sizeof(double) * (size_t)P * P);
+        for (int i = 0; i < P && ok; i++) {
+            for (int j = 0; j <= i; j++) {
+                double s = A[(size_t)i * P + j] + (i == j ? lambda : 0.0);
+                for (int k = 0; k < j; k++) s -= L[(size_t)i * P + k] * L[(size_t)j * P + k];
+                if (i == j) {
+                    if (s <= 0) { ok = 0; break; }
+                    L[(size_t)i * P + i] = sqrt(s);
+                } else {
+                    L[(size_t)i * P + j] = s / L[(size_t)j * P + j];
+                }
+            }
+        }
+        if (!ok) { lambda *= 10.0; continue; }
+        for (int i = 0; i < P; i++) {
+            double s = b[i];
+            for (int k = 0; k < i; k++) s -= L[(size_t)i * P + k] * y[k];
+            y[i] = s / L[(size_t)i * P + i];
+        }
+        for (int i = P - 1; i >= 0; i--) {
+            double s = y[i];
+            for (int k = i + 1; k < P; k++) s -= L[(size_t)k * P + i] * x[k];
+            x[i] = s / L[(size_t)i * P + i];
+        }
+        if (lambda_used) *lambda_used = lambda;
+        free(L);
+        free(y);
+        return 0;
+    }
+    free(L);
+    free(y);
+    return -1;
+}
+
+static double dot(const double* a, const double* b, int n)
+{
+    double s = 0;
+    for (int i = 0; i < n; i++) s += a[i] * b[i];
+    return s;
+}
+
+static void matvec(int P, const double* A, const double* x, double* y)
+{
+    #pragma omp parallel for
+    for (int i = 0; i < P; i++) {
+        double s = 0;
+        for (int j = 0; j < P; j++) s += A[(size_t)i * P + j] * x[j];
+        y[i] = s;
+    }
+}
+
+int or_cg_solve(int P, const double* A, const double* b, double* x, int max_iter, double tol)
+{
+    return or_pcg_solve(P, A, b, x, max_iter, tol, NULL, NULL, 0);
+}
+
+/* Woodbury: (D + U U^T)^{-1} r = D^{-1} r - D^{-1} U (I + U^T D^{-1} U)^{-1} U^T D^{-1} r */
+typedef struct { int P, r; const double* d; const double* U; double* Sinv; double* t; double* w; } wb_t;
+
+static int wb_init(wb_t* w, int P, const double* d, const double* U, int r)
+{
+    w->P = P; w->r = r; w->d = d; w->U = U;
+    w->Sinv = (double*)calloc((size_t)r * r + 1, sizeof(double));
+    w->t = (double*)calloc((size_t)r + 1, sizeof(double));
+    w->w = (double*)calloc((size_t)r + 1, sizeof(double));
+    if (!w->Sinv || !w->t || !w->w) return -1;
+    /* S = I + U^T D^{-1} U, then invert by Gauss-Jordan (SPD, small r) */
+    double* S = (double*)calloc((size_t)r * r + 1, sizeof(double));
+    if (!S) return -1;
+    for (int a = 0; a < r; a++)
+        for (int c = 0; c < r; c++) {
+            double s = (a == c) ? 1.0 : 0.0;
+            for (int i = 0; i < P; i++) s += U[(size_t)i * r + a] * U[(size_t)i * r + c] / d[i];
+            S[a * r + c] = s;
+        }
+    for (int a = 0; a < r; a++) w->Sinv[a * r + a] = 1.0;
+    for (int c = 0; c < r; c++) {
+        double piv = S[c * r + c];
+        for (int j = 0; j < r; j++) { S[c * r + j] /= piv; w->Sinv[c * r + j] /= piv; }
+        for (int a = 0; a < r; a++) {
+            if (a == c) continue;
+            double f = S[a * r + c];
+            for (int j = 0; j < r; j++) { S[a * r + j] -= f * S[c * r + j]; w->Sinv[a * r + j] -= f * w->Sinv[c * r + j]; }
+        }
+    }
+    free(S);
+    return 0;
+}
+
+static void wb_apply(wb_t* w, const double* rin, double* z)
+{
+    int P = w->P, r = w->r;
+    for (int i = 0; i < P; i++) z[i] = rin[i] / w->d[i];
+    if (r == 0) return;
+    for (int a = 0; a < r; a++) {
+        double s = 0;
+        for (int i = 0; i < P; i++) s += w->U[(size_t)i * r + a] * z[i];
+        w->t[a] = s;
+    }
+    for (int a = 0; a < r; a++) {
+        double s = 0;
+        for (int c = 0; c < r; c++) s += w->Sinv[a * r + c] * w->t[c];
+        w->w[a] = s;
+    }
+    for (int i = 0; i < P; i++) {
+        double s = 0;
+        for (int a = 0; a < r; a++) s += w->U[(size_t)i * r + a] * w->w[a];
+        z[i] -= s / w->d[i];
+    }
+}
+
+int or_pcg_solve(int P, const double* A, const double* b, double* x, int max_iter, double tol,
+                 const double* d, const double* U, int r)
+{
+    double* rr = (double*)malloc(sizeof(double) * (size_t)P);
+    double* p = (double*)malloc(sizeof(double) * (size_t)P);
+    double* Ap = (double*)malloc(sizeof(double) * (size_t)P);
+    double* z = (double*)malloc(sizeof(double) * (size_t)P);
+    wb_t w = {0};
+    int pre = d != NULL;
+    if (!rr || !p || !Ap || !z || (pre && wb_init(&w, P, d, U, r) != 0)) {
+        free(rr); free(p); free(Ap); free(z); free(w.Sinv); free(w.t); free(w.w);
+        return -1;
+    }
+    memset(x, 0, sizeof(double) * (size_t)P);
+    memcpy(rr, b, sizeof(double) * (size_t)P);
+    if (pre) wb_apply(&w, rr, z); else memcpy(z, rr, sizeof(double) * (size_t)P);
+    memcpy(p, z, sizeof(double) * (size_t)P);
+    double rz = dot(rr, z, P);
+    int it = 0;
+    if (sqrt(dot(rr, rr, P)) < tol) max_iter = 0;
+    for (it = 0; it < max_iter;) {
+        matvec(P, A, p, Ap);
+        double pAp = dot(p, Ap, P);
+        if (fabs(pAp) < 1e-15) break;
+        double alpha = rz / pAp;
+        for (int i = 0; i < P; i++) { x[i] += alpha * p[i]; rr[i] -= alpha * Ap[i]; }
+        it++;
+        if (sqrt(dot(rr, rr, P)) < tol) break;
+        if (pre) wb_apply(&w, rr, z); else memcpy(z, rr, sizeof(double) * (size_t)P);
+        double rznew = dot(rr, z, P);
+        double beta = rznew / rz;
+        for (int i = 0; i < P; i++) p[i] = z[i] + beta * p[i];
+        rz = rznew;
+    }
+    free(rr); free(p); free(Ap); free(z); free(w.Sinv); free(w.t); free(w.w);
+    return it;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Berry-curvature map over two parameters (a10)                             */
+/* ------------------------------------------------------------------------ */
+
+int or_berry_map(int n, const og_gate_t* gates, int ngates, const double* theta, int P,
+                 int pa, int pb, int grid, double* out)
+{
+    if (pa < 0 || pb < 0 || pa >= P || pb >= P || pa == pb || grid < 1) return -1;
+    size_t dim = (size_t)1 << n;
+    int fail = 0;
+    #pragma omp parallel
+    {
+        /* a private gate list in which only (pa, pb) stay parameters (as 0, 1) */
+        og_gate_t* g2 = (og_gate_t*)malloc(sizeof(og_gate_t) * (size_t)(ngates > 0 ? ngates : 1));
+        double* psi = (double*)malloc(2 * dim * sizeof(double));
+        double* D = (double*)malloc(4 * dim * sizeof(double));
+        double Q[8];
+        if (!g2 || !psi || !D) {
+            #pragma omp atomic write
+            fail = 1;
+        } else {
+            #pragma omp for schedule(dynamic, 1)
+            for (int ij = 0; ij < grid * grid; ij++) {
+                int i = ij / grid, j = ij % grid;
+                double th2[2] = {2.0 * M_PI * i / grid, 2.0 * M_PI * j / grid};
+                for (int g = 0; g < ngates; g++) {
+                    g2[g] = gates[g];
+                    if (gates[g].param >= 0) {
+                        if (gates[g].param == pa) g2[g].param = 0;
+                        else if (gates[g].param == pb) g2[g].param = 1;
+                        else { g2[g].param = -1; g2[g].angle = theta[gates[g].param]; }
+                    }
+                }
+                or_derivatives(n, g2, ngates, th2, 2, psi, D);
+                or_qgt(dim, 2, psi, D, Q);
+                out[ij] = Q[3]; /* Im Q_{ab} */
+            }
+        }
+        free(g2); free(psi); free(D);
+    }
+    return fail ? -1 : 0;
+}

@@ -1,0 +1,111 @@
+"""The FP64 oracle against the golden fixtures made by the reference's own code
+(tests/golden/make_golden.py), plus analytic known answers.  CPU only."""
+import glob
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def test_golden_present():
+    assert len(GOLDEN) >= 8
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_oracle_matches_reference(orc, path):
+    z = np.load(path)
+    n, gates, theta = int(z["n"]), z["gates"], z["theta"]
+    psi, D = orc.derivatives(n, gates, theta)
+    assert rel(psi, z["psi"]) < 1e-13
+    Q = orc.qgt_from_states(psi, D)
+    assert rel(Q, z["Q"]) < 1e-12
+    assert rel(Q.real, z["metric"]) < 1e-12
+    assert rel(-2.0 * Q.imag, z["berry_F"]) < 1e-12 or np.linalg.norm(z["berry_F"]) < 1e-14
+    assert abs(orc.tfim_energy(n, psi) - float(z["energy"])) < 1e-12
+    g = orc.energy_grad(D, orc.tfim_apply(n, psi))
+    assert rel(g, z["grad"]) < 1e-12
+    # parameter-shift restatement agrees with the adjoint form and the reference
+    if len(theta) <= 40:
+        assert rel(orc.param_shift_grad(n, gates, theta), z["grad"]) < 1e-12
+    lam = float(z["lam"])
+    x, used = orc.cholesky_solve(Q.real, g, lam)
+    assert used == lam
+    A = Q.real + lam * np.eye(len(theta))
+    # the reference CG stops at ||r|| < 1e-8: compare within that residual
+    assert np.linalg.norm(A @ z["natgrad_cg"] - g) < 1e-7
+    assert np.linalg.norm(A @ x - g) < 1e-10 * max(1.0, np.linalg.norm(g))
+    # restated CG follows the reference CG
+    xc, it = orc.cg_solve(A, g)
+    assert rel(xc, z["natgrad_cg"]) < 1e-6
+    # float Cholesky inverse of the reference (single precision)
+    inv = z["qfim_inv"].astype(np.float64)
+    assert np.linalg.norm(inv @ A - np.eye(len(theta))) < 5e-2 * max(1.0, np.linalg.cond(A) * 1e-4)
+
+
+def test_single_qubit_known_answers(orc):
+    th, ph = 0.9, 0.4
+    g = O.gates_array([(O.RY, 0, -1, 0, 0.0), (O.RZ, 0, -1, 1, 0.0)])
+    Q = orc.qgt(1, g, np.array([th, ph]))
+    assert abs(Q[0, 0].real - 0.25) < 1e-15
+    assert abs(Q[1, 1].real - math.sin(th) ** 2 / 4) < 1e-15
+    assert abs(Q[0, 1].real) < 1e-15
+    assert abs(Q[0, 1].imag - math.sin(th) / 4) < 1e-15
+
+
+def test_qgt_invariants(orc):
+    g = O.ansatz(6, 3, "cnot")
+    th = O.splitmix64_params(7, O.num_params(g))
+    psi, D = orc.derivatives(6, g, th)
+    Q = orc.qgt_from_states(psi, D)
+    assert np.abs(Q - Q.conj().T).max() < 1e-15
+    assert np.linalg.eigvalsh(Q).min() > -1e-13
+    # global phase invariance
+    ph = np.exp(0.37j)
+    Q2 = orc.qgt_from_states(psi * ph, D * ph)
+    assert np.abs(Q2 - Q).max() < 1e-14
+    # first-layer RY block on |0...0> is I/4
+    assert np.abs(Q[:6, :6].real - 0.25 * np.eye(6)).max() < 1e-14
+
+
+def test_seed_stream_matches_c(orc):
+    a = orc.seed_params(12345, 17)
+    b = O.splitmix64_params(12345, 17)
+    assert np.array_equal(a, b)
+    assert (a >= 0).all() and (a < 2 * math.pi).all()
+
+
+def test_pcg_with_exact_preconditioner(orc):
+    rng = np.random.default_rng(0)
+    P, r = 40, 4
+    U = rng.standard_normal((P, r))
+    d = rng.uniform(0.5, 2.0, P)
+    A = np.diag(d) + U @ U.T
+    b = rng.standard_normal(P)
+    x, it = orc.pcg_solve(A, b, d, U)
+    assert it <= 2
+    assert rel(x, np.linalg.solve(A, b)) < 1e-10
+    x2, it2 = orc.cg_solve(A, b, max_iter=1000, tol=1e-10)
+    assert it2 > it
+
+
+def test_berry_map_matches_full_qgt(orc):
+    g = O.ansatz(3, 2, "cnot")
+    th = O.splitmix64_params(5, O.num_params(g))
+    grid = 4
+    m = orc.berry_map(3, g, th, 0, 3, grid)
+    for i in range(grid):
+        for j in range(grid):
+            t = th.copy()
+            t[0] = 2 * math.pi * i / grid
+            t[3] = 2 * math.pi * j / grid
+            Q = orc.qgt(3, g, t)
+            assert abs(m[i, j] - Q[0, 3].imag) < 1e-14
