@@ -1,0 +1,212 @@
+"""GB300-native quantum geometric tensor engine (Python view of libqgt_gb300.so).
+
+The product is the C ABI in ``include/``: ``libqgt_gb300.so`` (C11 host code +
+sm_103a CUDA kernels).  This module only loads that library with ctypes and
+wraps the plan entry points with numpy; it contains no numerics of its own and
+has no fallback: if the library is missing it raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libqgt_gb300.so")
+
+# gate codes (reference gate_type_t values)
+I, X, Y, Z, H, S, T, RX, RY, RZ, CNOT, CZ, SWAP = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 12, 13
+FP64, MIXED, MIXED_BF16X3 = 0, 1, 2
+HAM_NONE, HAM_TFIM = 0, 1
+
+
+class GateDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("qubits", C.c_int32 * 2), ("param", C.c_int32), ("angle", C.c_double)]
+
+
+class CircuitDesc(C.Structure):
+    _fields_ = [("num_qubits", C.c_int32), ("num_gates", C.c_int32), ("gates", C.POINTER(GateDesc)),
+                ("num_params", C.c_int32)]
+
+
+class PlanOptions(C.Structure):
+    _fields_ = [("precision", C.c_int), ("hamiltonian", C.c_int), ("tfim_J", C.c_double), ("tfim_h", C.c_double),
+                ("lambda_", C.c_double), ("device", C.c_int32), ("use_graph", C.c_int32)]
+
+
+class PlanInfo(C.Structure):
+    _fields_ = [("num_qubits", C.c_int32), ("num_params", C.c_int32), ("num_slots", C.c_int32),
+                ("num_rows", C.c_int32), ("num_passes", C.c_int32), ("num_launches", C.c_int32),
+                ("tile_bits", C.c_int32), ("vector_passes", C.c_int64), ("gate_bytes", C.c_int64),
+                ("gram_flops", C.c_int64), ("device_bytes", C.c_int64)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libqgt_gb300.so (built by __graft_entry__.build()); raise if absent."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libqgt_gb300.so not built ({LIB_PATH}); run __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.qgt_plan_default_options.argtypes = [C.POINTER(PlanOptions)]
+        L.qgt_plan_create.argtypes = [C.POINTER(CircuitDesc), C.POINTER(PlanOptions), C.POINTER(vp)]
+        L.qgt_plan_destroy.argtypes = [vp]
+        L.qgt_plan_get_info.argtypes = [vp, C.POINTER(PlanInfo)]
+        L.qgt_plan_execute_host.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.qgt_plan_execute_device.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.qgt_plan_synchronize.argtypes = [vp]
+        L.qgt_plan_stream.argtypes = [vp]
+        L.qgt_plan_stream.restype = vp
+        L.qgt_plan_get_state.argtypes = [vp, vp]
+        L.qgt_plan_get_row.argtypes = [vp, C.c_int, vp]
+        L.qgt_plan_device_status.argtypes = [vp, vp]
+        L.qgt_cholesky_solve_f64.argtypes = [vp, vp, C.c_double, C.c_int32, vp, vp]
+        L.qgt_last_error.restype = C.c_char_p
+        L.qgt_version.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+class QGTError(RuntimeError):
+    def __init__(self, code, where):
+        super().__init__(f"{where}: error {code}: {lib().qgt_last_error().decode()}")
+        self.code = code
+
+
+def _check(rc, where):
+    if rc != 0:
+        raise QGTError(rc, where)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def circuit_desc(n: int, gates, num_params: int | None = None):
+    """gates: iterable of (type, q0, q1, param, angle) or a structured array with those fields."""
+    arr = (GateDesc * max(1, len(gates)))()
+    maxp = -1
+    for i, g in enumerate(gates):
+        t, q0, q1, p, a = (int(g[0]), int(g[1]), int(g[2]), int(g[3]), float(g[4]))
+        arr[i].type = t
+        arr[i].qubits[0] = q0
+        arr[i].qubits[1] = q1
+        arr[i].param = p
+        arr[i].angle = a
+        maxp = max(maxp, p)
+    P = maxp + 1 if num_params is None else num_params
+    d = CircuitDesc(n, len(gates), C.cast(arr, C.POINTER(GateDesc)), P)
+    d._keep = arr
+    return d
+
+
+def ansatz_gates(n: int, layers: int, entangler: str = "cnot"):
+    """RY layer, RZ layer, then CNOT ladder q->q+1 ("cnot") or CZ ring ("cz")."""
+    g, p = [], 0
+    for _ in range(layers):
+        for q in range(n):
+            g.append((RY, q, -1, p, 0.0)); p += 1
+        for q in range(n):
+            g.append((RZ, q, -1, p, 0.0)); p += 1
+        if entangler == "cnot":
+            g += [(CNOT, q, q + 1, -1, 0.0) for q in range(n - 1)]
+        else:
+            nb = n if n >= 3 else n - 1
+            g += [(CZ, q, (q + 1) % n, -1, 0.0) for q in range(nb)]
+    return g
+
+
+class Plan:
+    """A compiled circuit plan (qgt_plan_t)."""
+
+    def __init__(self, n, gates, num_params=None, precision=MIXED, hamiltonian=HAM_TFIM, J=1.0, h=1.0,
+                 lam=1e-3, device=0, use_graph=True):
+        L = lib()
+        self.desc = circuit_desc(n, gates, num_params)
+        o = PlanOptions()
+        L.qgt_plan_default_options(C.byref(o))
+        o.precision, o.hamiltonian, o.tfim_J, o.tfim_h = precision, hamiltonian, J, h
+        o.lambda_, o.device, o.use_graph = lam, device, int(use_graph)
+        self.opt = o
+        h_ = C.c_void_p()
+        _check(L.qgt_plan_create(C.byref(self.desc), C.byref(o), C.byref(h_)), "qgt_plan_create")
+        self.h = h_
+        self.n, self.P = n, self.desc.num_params
+
+    def info(self) -> PlanInfo:
+        i = PlanInfo()
+        _check(lib().qgt_plan_get_info(self.h, C.byref(i)), "qgt_plan_get_info")
+        return i
+
+    def run(self, theta, want=("Q", "grad", "energy", "natgrad")):
+        P = self.P
+        theta = np.ascontiguousarray(theta, dtype=np.float64)
+        Q = np.zeros((P, P), dtype=np.complex128) if "Q" in want else None
+        g = np.zeros(P) if "grad" in want else None
+        e = np.zeros(1) if "energy" in want else None
+        x = np.zeros(P) if "natgrad" in want else None
+        _check(lib().qgt_plan_execute_host(self.h, _ptr(theta), _ptr(Q), _ptr(g), _ptr(e), _ptr(x)),
+               "qgt_plan_execute_host")
+        return {"Q": Q, "grad": g, "energy": None if e is None else float(e[0]), "natgrad": x}
+
+    def state(self):
+        psi = np.zeros(1 << self.n, dtype=np.complex128)
+        _check(lib().qgt_plan_get_state(self.h, _ptr(psi)), "qgt_plan_get_state")
+        return psi
+
+    def row(self, r):
+        v = np.zeros(1 << self.n, dtype=np.complex128)
+        _check(lib().qgt_plan_get_row(self.h, r, _ptr(v)), "qgt_plan_get_row")
+        return v
+
+    def status(self):
+        lam = np.zeros(1)
+        st = lib().qgt_plan_device_status(self.h, _ptr(lam))
+        return st, float(lam[0])
+
+    def stream(self) -> int:
+        return lib().qgt_plan_stream(self.h) or 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().qgt_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def cholesky_solve(A, b, lam):
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros_like(b)
+    used = np.zeros(1)
+    _check(lib().qgt_cholesky_solve_f64(_ptr(A), _ptr(b), lam, A.shape[0], _ptr(x), _ptr(used)),
+           "qgt_cholesky_solve_f64")
+    return x, float(used[0])
+
+
+def qgt_from_states(psi, D, precision=FP64):
+    """Q from given states on the GPU (qgt_qgt_from_states)."""
+    L = lib()
+    L.qgt_qgt_from_states.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int, C.c_void_p]
+    psi = np.ascontiguousarray(psi, dtype=np.complex128)
+    D = np.ascontiguousarray(D, dtype=np.complex128)
+    P = D.shape[0]
+    Q = np.zeros((P, P), dtype=np.complex128)
+    _check(L.qgt_qgt_from_states(_ptr(psi), _ptr(D), psi.shape[0], P, precision, _ptr(Q)), "qgt_qgt_from_states")
+    return Q

@@ -1,0 +1,441 @@
+// qgt_device.cu -- device context, memory, streams and graphs, and the small
+// FP64 kernels of a step: gate-coefficient preparation, the TFIM H|psi>,
+// the renormalised projector (Gram -> QGT, energy, gradient) and the FP64
+// Cholesky natural-gradient solve.
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <math.h>
+#include <stdio.h>
+
+#include "../qgt_internal.h"
+#include "qgt_gb300.h"
+
+#define QGT_OK 0
+#define QGT_EINVAL (-1)
+#define QGT_ENOMEM (-2)
+#define QGT_EHW (-6)
+#define QGT_ENOTPD (-34)
+
+static int cuda_fail(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return QGT_OK;
+    int code = (e == cudaErrorMemoryAllocation) ? QGT_ENOMEM : QGT_EHW;
+    return qgt_set_error(code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return cuda_fail(e_, what); } while (0)
+
+extern "C" {
+
+int qgt_dev_set_device(int device) { CK(cudaSetDevice(device), "cudaSetDevice"); return QGT_OK; }
+
+int qgt_dev_malloc(void** p, size_t bytes)
+{
+    *p = NULL;
+    if (bytes == 0) return QGT_OK;
+    CK(cudaMalloc(p, bytes), "cudaMalloc");
+    return QGT_OK;
+}
+
+int qgt_dev_free(void* p) { if (p) CK(cudaFree(p), "cudaFree"); return QGT_OK; }
+
+int qgt_dev_memcpy_h2d(void* dst, const void* src, size_t bytes, void* s)
+{
+    if (bytes) CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)s), "cudaMemcpyAsync H2D");
+    return QGT_OK;
+}
+
+int qgt_dev_memcpy_d2h(void* dst, const void* src, size_t bytes, void* s)
+{
+    if (bytes) CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)s), "cudaMemcpyAsync D2H");
+    return QGT_OK;
+}
+
+int qgt_dev_memcpy_d2d(void* dst, const void* src, size_t bytes, void* s)
+{
+    if (bytes) CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)s), "cudaMemcpyAsync D2D");
+    return QGT_OK;
+}
+
+int qgt_dev_memset(void* dst, int v, size_t bytes, void* s)
+{
+    if (bytes) CK(cudaMemsetAsync(dst, v, bytes, (cudaStream_t)s), "cudaMemsetAsync");
+    return QGT_OK;
+}
+
+int qgt_dev_stream_create(void** s)
+{
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    *s = (void*)st;
+    return QGT_OK;
+}
+
+int qgt_dev_stream_destroy(void* s) { if (s) CK(cudaStreamDestroy((cudaStream_t)s), "cudaStreamDestroy"); return QGT_OK; }
+int qgt_dev_stream_sync(void* s) { CK(cudaStreamSynchronize((cudaStream_t)s), "cudaStreamSynchronize"); return QGT_OK; }
+
+int qgt_dev_graph_begin(void* s)
+{
+    CK(cudaStreamBeginCapture((cudaStream_t)s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    return QGT_OK;
+}
+
+int qgt_dev_graph_end(void* s, void** exec)
+{
+    cudaGraph_t g;
+    CK(cudaStreamEndCapture((cudaStream_t)s, &g), "cudaStreamEndCapture");
+    cudaGraphExec_t ge;
+    cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    CK(e, "cudaGraphInstantiate");
+    *exec = (void*)ge;
+    return QGT_OK;
+}
+
+int qgt_dev_graph_launch(void* exec, void* s) { CK(cudaGraphLaunch((cudaGraphExec_t)exec, (cudaStream_t)s), "cudaGraphLaunch"); return QGT_OK; }
+int qgt_dev_graph_destroy(void* exec) { if (exec) CK(cudaGraphExecDestroy((cudaGraphExec_t)exec), "cudaGraphExecDestroy"); return QGT_OK; }
+
+int qgt_dev_host_alloc(void** p, size_t bytes) { CK(cudaMallocHost(p, bytes ? bytes : 1), "cudaMallocHost"); return QGT_OK; }
+int qgt_dev_host_free(void* p) { if (p) CK(cudaFreeHost(p), "cudaFreeHost"); return QGT_OK; }
+
+int qgt_dev_last_error(void) { cudaError_t e = cudaGetLastError(); return cuda_fail(e, "kernel launch"); }
+
+const char* qgt_dev_error_string(void) { return cudaGetErrorString(cudaPeekAtLastError()); }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// gate coefficients (FP64, from theta, on the device)
+// 2x2 row-major matrices of a2: RX = [[c,-is],[-is,c]], RY = [[c,-s],[s,c]],
+// RZ = diag(e^{-ia/2}, e^{ia/2}); fixed gates as in
+// hybrid/quantum_classical_algorithms.c:228-276.
+// ---------------------------------------------------------------------------
+__global__ void prepare_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const double* theta, double* coef)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncoef) return;
+    qgt_dev_coef_desc_t g = d[c];
+    double a = g.param >= 0 ? theta[g.param] : g.angle;
+    double m[8] = {1, 0, 0, 0, 0, 0, 1, 0};
+    double cs, sn;
+    sincos(0.5 * a, &sn, &cs);
+    const double r = 0.70710678118654752440;
+    switch (g.type) {
+    case QGT_GATE_RX: m[0] = cs; m[1] = 0; m[2] = 0; m[3] = -sn; m[4] = 0; m[5] = -sn; m[6] = cs; m[7] = 0; break;
+    case QGT_GATE_RY: m[0] = cs; m[1] = 0; m[2] = -sn; m[3] = 0; m[4] = sn; m[5] = 0; m[6] = cs; m[7] = 0; break;
+    case QGT_GATE_RZ: m[0] = cs; m[1] = -sn; m[2] = 0; m[3] = 0; m[4] = 0; m[5] = 0; m[6] = cs; m[7] = sn; break;
+    case QGT_GATE_X: m[0] = 0; m[2] = 1; m[4] = 1; m[6] = 0; break;
+    case QGT_GATE_Y: m[0] = 0; m[2] = 0; m[3] = -1; m[4] = 0; m[5] = 1; m[6] = 0; break;
+    case QGT_GATE_Z: m[6] = -1; break;
+    case QGT_GATE_H: m[0] = r; m[2] = r; m[4] = r; m[6] = -r; break;
+    case QGT_GATE_S: m[6] = 0; m[7] = 1; break;
+    case QGT_GATE_T: m[6] = r; m[7] = r; break;
+    default: break;
+    }
+    for (int i = 0; i < 8; i++) coef[8 * c + i] = m[i];
+}
+
+// ---------------------------------------------------------------------------
+// TFIM ring: (H psi)_i = -J zz(i) psi_i - h sum_q psi_{i ^ 2^q}, scaled
+// ---------------------------------------------------------------------------
+template <typename T, typename R>
+__global__ void tfim_kernel(const T* __restrict__ psi, T* __restrict__ out, int n, R J, R h, R inv,
+                            void* split, int64_t sld, int64_t pstride, int32_t srow, float sscale, int bf16)
+{
+    int64_t N = (int64_t)1 << n;
+    int nb = n >= 3 ? n : n - 1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        int zz = 0;
+        for (int b = 0; b < nb; b++) {
+            int qa = b, qb = (b + 1) % n;
+            zz += (((i >> qa) ^ (i >> qb)) & 1) ? -1 : 1;
+        }
+        T v = psi[i];
+        R ar = -J * (R)zz * v.x, ai = -J * (R)zz * v.y;
+        for (int q = 0; q < n; q++) {
+            T w = psi[i ^ ((int64_t)1 << q)];
+            ar -= h * w.x;
+            ai -= h * w.y;
+        }
+        T o;
+        o.x = ar * inv;
+        o.y = ai * inv;
+        out[i] = o;
+        if (split) {
+            float xr = (float)o.x * sscale, xi = (float)o.y * sscale;
+            int64_t at = (int64_t)srow * sld + i;
+            if (bf16) {
+                __nv_bfloat16* s = (__nv_bfloat16*)split;
+                __nv_bfloat16 rh = __float2bfloat16_rn(xr), ih = __float2bfloat16_rn(xi);
+                s[at] = rh;
+                s[pstride + at] = __float2bfloat16_rn(xr - __bfloat162float(rh));
+                s[2 * pstride + at] = ih;
+                s[3 * pstride + at] = __float2bfloat16_rn(xi - __bfloat162float(ih));
+            } else {
+                __half* s = (__half*)split;
+                __half rh = __float2half_rn(xr), ih = __float2half_rn(xi);
+                s[at] = rh;
+                s[pstride + at] = __float2half_rn(xr - __half2float(rh));
+                s[2 * pstride + at] = ih;
+                s[3 * pstride + at] = __float2half_rn(xi - __half2float(ih));
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// renormalised projector: s = <psi|psi>, v_p = sum_{a in p} <d_a|psi>,
+// B_pq = sum <d_a|d_b>, Q = B/s - v_p conj(v_q)/s^2.
+// HG_ij = <V_i|V_j>, rows: 0 psi, 1 H psi / hscale, 2 + a slot a.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 hg(const double* HG, int rows, int i, int j)
+{
+    return make_double2(HG[2 * ((int64_t)i * rows + j)], HG[2 * ((int64_t)i * rows + j) + 1]);
+}
+
+__global__ void post_qgt_kernel(qgt_dev_post_args_t a)
+{
+    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int P = a.P;
+    if (idx >= (int64_t)P * P) return;
+    int p = (int)(idx / P), q = (int)(idx % P);
+    double s = a.HG[0];
+    double2 B = make_double2(0, 0), vp = make_double2(0, 0), vq = make_double2(0, 0);
+    for (int x = a.param_ptr[p]; x < a.param_ptr[p + 1]; x++) {
+        int sa = a.param_slots[x];
+        double2 t = hg(a.HG, a.rows, sa + 2, 0);
+        vp.x += t.x; vp.y += t.y;
+        for (int y = a.param_ptr[q]; y < a.param_ptr[q + 1]; y++) {
+            double2 u = hg(a.HG, a.rows, sa + 2, a.param_slots[y] + 2);
+            B.x += u.x; B.y += u.y;
+        }
+    }
+    for (int y = a.param_ptr[q]; y < a.param_ptr[q + 1]; y++) {
+        double2 t = hg(a.HG, a.rows, a.param_slots[y] + 2, 0);
+        vq.x += t.x; vq.y += t.y;
+    }
+    // v_p conj(v_q)
+    double pr = vp.x * vq.x + vp.y * vq.y;
+    double pi = vp.y * vq.x - vp.x * vq.y;
+    double is = 1.0 / s, is2 = is * is;
+    a.Q[2 * idx] = B.x * is - pr * is2;
+    a.Q[2 * idx + 1] = B.y * is - pi * is2;
+}
+
+__global__ void post_grad_kernel(qgt_dev_post_args_t a)
+{
+    double s = a.HG[0];
+    double E = a.hscale * hg(a.HG, a.rows, 0, 1).x / s;
+    if (threadIdx.x == 0 && blockIdx.x == 0 && a.energy) a.energy[0] = E;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.P; p += gridDim.x * blockDim.x) {
+        double g = 0, v = 0;
+        for (int x = a.param_ptr[p]; x < a.param_ptr[p + 1]; x++) {
+            int sa = a.param_slots[x];
+            g += hg(a.HG, a.rows, sa + 2, 1).x;
+            v += hg(a.HG, a.rows, sa + 2, 0).x;
+        }
+        // d/dtheta <psi|H|psi>/<psi|psi> = 2 Re<d psi|H psi>/s - 2 E Re<d psi|psi>/s
+        a.grad[p] = 2.0 * a.hscale * g / s - 2.0 * E * v / s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 Cholesky of (A + lambda I), lambda x10 retries, then two triangular
+// solves (learning/quantum_pipeline_impl.c:1601-1682 restated in double on
+// the GPU).  One CTA; the trailing update of each column is spread over the
+// block.  work: P x P doubles.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) cholesky_kernel(const double* A, int cplx, const double* b, int P,
+                                                        double lambda, double* L, double* x, double* status)
+{
+    __shared__ int fail;
+    __shared__ double red[32];
+    double lam = lambda;
+    for (int attempt = 0; attempt < 12; attempt++) {
+        for (int64_t i = threadIdx.x; i < (int64_t)P * P; i += blockDim.x) {
+            int r = (int)(i / P), c = (int)(i % P);
+            double v = cplx ? A[2 * i] : A[i];
+            L[i] = (r == c) ? v + lam : v;
+        }
+        if (threadIdx.x == 0) fail = 0;
+        __syncthreads();
+        for (int j = 0; j < P; j++) {
+            double d = L[(int64_t)j * P + j];
+            if (d <= 0.0 || !(d == d)) {
+                if (threadIdx.x == 0) fail = 1;
+            }
+            __syncthreads();
+            if (fail) break;
+            double ljj = sqrt(d);
+            for (int i = j + 1 + threadIdx.x; i < P; i += blockDim.x) L[(int64_t)i * P + j] /= ljj;
+            __syncthreads();
+            if (threadIdx.x == 0) L[(int64_t)j * P + j] = ljj;
+            // trailing lower triangle: L[i][k] -= L[i][j] L[k][j], j < k <= i
+            int m = P - j - 1;
+            int64_t cnt = (int64_t)m * (m + 1) / 2;
+            for (int64_t t = threadIdx.x; t < cnt; t += blockDim.x) {
+                // t -> (ii, kk) with 0 <= kk <= ii < m
+                int ii = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+                while ((int64_t)ii * (ii + 1) / 2 > t) ii--;
+                while ((int64_t)(ii + 1) * (ii + 2) / 2 <= t) ii++;
+                int kk = (int)(t - (int64_t)ii * (ii + 1) / 2);
+                int i = j + 1 + ii, k = j + 1 + kk;
+                L[(int64_t)i * P + k] -= L[(int64_t)i * P + j] * L[(int64_t)k * P + j];
+            }
+            __syncthreads();
+        }
+        __syncthreads();
+        if (!fail) {
+            // forward: L y = b (y in x), backward: L^T x = y
+            for (int i = 0; i < P; i++) {
+                double part = 0;
+                for (int k = threadIdx.x; k < i; k += blockDim.x) part += L[(int64_t)i * P + k] * x[k];
+                for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+                if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    double s = 0;
+                    for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w];
+                    x[i] = (b[i] - s) / L[(int64_t)i * P + i];
+                }
+                __syncthreads();
+            }
+            for (int i = P - 1; i >= 0; i--) {
+                double part = 0;
+                for (int k = i + 1 + threadIdx.x; k < P; k += blockDim.x) part += L[(int64_t)k * P + i] * x[k];
+                for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+                if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    double s = 0;
+                    for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w];
+                    x[i] = (x[i] - s) / L[(int64_t)i * P + i];
+                }
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) { status[0] = 0.0; status[1] = lam; }
+            return;
+        }
+        lam *= 10.0;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { status[0] = (double)QGT_ENOTPD; status[1] = lam; }
+}
+
+extern "C" {
+
+int qgt_dev_prepare(const qgt_dev_coef_desc_t* d, int32_t ncoef, const double* theta, double* coef, void* s)
+{
+    if (ncoef <= 0) return QGT_OK;
+    prepare_kernel<<<(ncoef + 127) / 128, 128, 0, (cudaStream_t)s>>>(d, ncoef, theta, coef);
+    return qgt_dev_last_error();
+}
+
+int qgt_dev_tfim(const void* psi, void* out, int32_t n, double J, double h, double inv, int fp64,
+                 void* split, int64_t sld, int64_t pstride, int32_t srow, float sscale, int32_t bf16, void* s)
+{
+    int64_t N = (int64_t)1 << n;
+    int blocks = (int)((N + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (fp64)
+        tfim_kernel<double2, double><<<blocks, 256, 0, (cudaStream_t)s>>>((const double2*)psi, (double2*)out, n, J, h,
+                                                                            inv, NULL, 0, 0, 0, 0.f, 0);
+    else
+        tfim_kernel<float2, float><<<blocks, 256, 0, (cudaStream_t)s>>>((const float2*)psi, (float2*)out, n, (float)J,
+                                                                          (float)h, (float)inv, split, sld, pstride, srow,
+                                                                          sscale, bf16);
+    return qgt_dev_last_error();
+}
+
+int qgt_dev_post(const qgt_dev_post_args_t* a, void* s)
+{
+    int64_t PP = (int64_t)a->P * a->P;
+    post_qgt_kernel<<<(unsigned)((PP + 255) / 256), 256, 0, (cudaStream_t)s>>>(*a);
+    int rc = qgt_dev_last_error();
+    if (rc) return rc;
+    if (a->has_h) {
+        post_grad_kernel<<<(a->P + 255) / 256, 256, 0, (cudaStream_t)s>>>(*a);
+        rc = qgt_dev_last_error();
+    }
+    return rc;
+}
+
+int qgt_dev_cholesky(const double* A, int cplx, const double* b, int32_t P, double lambda, double* work, double* x,
+                     double* status, void* s)
+{
+    if (P <= 0) return qgt_set_error(QGT_EINVAL, "cholesky: P must be positive");
+    cholesky_kernel<<<1, 1024, 0, (cudaStream_t)s>>>(A, cplx, b, P, lambda, work, x, status);
+    return qgt_dev_last_error();
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// host-supplied states -> Gram operands: complex128 rows are rounded to
+// complex64 (the precision a mixed plan evolves in) and split into the four
+// half-precision planes, or kept as complex128 for the FP64 Gram.
+// ---------------------------------------------------------------------------
+__global__ void split_rows_kernel(const double2* __restrict__ X, int rows, int64_t N, void* split, int64_t sld,
+                                  int64_t pstride, int row0, float scale, int bf16)
+{
+    int64_t total = (int64_t)rows * N;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int r = (int)(t / N);
+        int64_t i = t % N;
+        double2 v = X[t];
+        float xr = (float)v.x * scale, xi = (float)v.y * scale;
+        int64_t at = (int64_t)(row0 + r) * sld + i;
+        if (bf16) {
+            __nv_bfloat16* s = (__nv_bfloat16*)split;
+            __nv_bfloat16 rh = __float2bfloat16_rn(xr), ih = __float2bfloat16_rn(xi);
+            s[at] = rh;
+            s[pstride + at] = __float2bfloat16_rn(xr - __bfloat162float(rh));
+            s[2 * pstride + at] = ih;
+            s[3 * pstride + at] = __float2bfloat16_rn(xi - __bfloat162float(ih));
+        } else {
+            __half* s = (__half*)split;
+            __half rh = __float2half_rn(xr), ih = __float2half_rn(xi);
+            s[at] = rh;
+            s[pstride + at] = __float2half_rn(xr - __half2float(rh));
+            s[2 * pstride + at] = ih;
+            s[3 * pstride + at] = __float2half_rn(xi - __half2float(ih));
+        }
+    }
+}
+
+extern "C" int qgt_dev_split_rows(const double* X, int32_t rows, int64_t N, void* split, int64_t sld, int64_t pstride,
+                                  int32_t row0, float scale, int32_t bf16, void* s)
+{
+    int64_t total = (int64_t)rows * N;
+    if (total <= 0) return QGT_OK;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    split_rows_kernel<<<blocks, 256, 0, (cudaStream_t)s>>>((const double2*)X, rows, N, split, sld, pstride, row0, scale,
+                                                           bf16);
+    return qgt_dev_last_error();
+}
+
+// out = sum_k c_k V[row0 + k]  (complex128 rows, real coefficients)
+__global__ void combine_rows_kernel(const double2* __restrict__ V, int64_t N, int row0, const double* __restrict__ c,
+                                    int K, double2* __restrict__ out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        double re = 0, im = 0;
+        for (int k = 0; k < K; k++) {
+            double2 v = V[(int64_t)(row0 + k) * N + i];
+            re += c[k] * v.x;
+            im += c[k] * v.y;
+        }
+        out[i] = make_double2(re, im);
+    }
+}
+
+extern "C" int qgt_dev_combine_rows(const void* V, int64_t N, int32_t row0, const double* c, int32_t K, void* out,
+                                    void* s)
+{
+    int blocks = (int)((N + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    combine_rows_kernel<<<blocks, 256, 0, (cudaStream_t)s>>>((const double2*)V, N, row0, c, K, (double2*)out);
+    return qgt_dev_last_error();
+}

@@ -1,0 +1,161 @@
+/*
+ * qgt_states.c -- QGT from caller-supplied states on the GPU, and the
+ * reference's diffgeo contraction entry points on top of it.
+ *
+ * The reference computes g_ij = Re(<d_i|d_j> - <d_i|psi><psi|d_j>) and
+ * F_ij = -2 Im(...) with a serial triple loop that recomputes both
+ * projections for every (i, j) (src/quantum_geometric/distributed/
+ * differential_geometry.c:2819-2906, 3 P^2 N complex MACs).  Here the states
+ * are copied to HBM once, the Gram of [psi, 0, d_0 .. d_{P-1}] runs on the
+ * GPU (FP64 SIMT, or split-FP16 / split-BF16 tcgen05 from complex64-rounded
+ * states) and the projector is applied in FP64.
+ */
+#include <math.h>
+#include <stdbool.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../qgt_internal.h"
+#include "qgt_gb300.h"
+#include "quantum_geometric/distributed/differential_geometry.h"
+
+#define E_INVAL (-1)
+#define E_NOMEM (-2)
+
+int qgt_qgt_from_states(const double* psi, const double* D, int64_t dim, int32_t P, qgt_precision_t prec, double* Q)
+{
+    if (!psi || (P > 0 && !D) || !Q || dim <= 0 || P < 0) return qgt_set_error(E_INVAL, "qgt_qgt_from_states: bad argument");
+    if (prec < QGT_PRECISION_FP64 || prec > QGT_PRECISION_MIXED_BF16X3)
+        return qgt_set_error(E_INVAL, "qgt_qgt_from_states: unknown precision %d", (int)prec);
+    if (P == 0) return 0;
+    const int rows = P + 2;
+    const int fp64 = prec == QGT_PRECISION_FP64;
+    void* s = NULL;
+    double *X = NULL, *part = NULL, *HG = NULL, *Qd = NULL;
+    void* split = NULL;
+    qgt_tc_gram_t* tc = NULL;
+    int32_t *pptr = NULL, *pslots = NULL, *sparam = NULL;
+    int32_t* hptr = (int32_t*)malloc(sizeof(int32_t) * ((size_t)P + 1));
+    int32_t* hsl = (int32_t*)malloc(sizeof(int32_t) * (size_t)P);
+    if (!hptr || !hsl) { free(hptr); free(hsl); return qgt_set_error(E_NOMEM, "qgt_qgt_from_states: oom"); }
+    for (int i = 0; i <= P; i++) hptr[i] = i;
+    for (int i = 0; i < P; i++) hsl[i] = i;
+    const size_t rowb = (size_t)dim * 16;
+    int rc = qgt_dev_stream_create(&s);
+    if (!rc) rc = qgt_dev_malloc((void**)&X, rowb * rows);
+    if (!rc) rc = qgt_dev_memset(X, 0, rowb * rows, s);
+    if (!rc) rc = qgt_dev_memcpy_h2d(X, psi, rowb, s);
+    if (!rc) rc = qgt_dev_memcpy_h2d((char*)X + 2 * rowb, D, rowb * (size_t)P, s);
+    if (!rc) rc = qgt_dev_malloc((void**)&HG, sizeof(double) * 2 * (size_t)rows * rows);
+    if (!rc) rc = qgt_dev_malloc((void**)&Qd, sizeof(double) * 2 * (size_t)P * P);
+    if (!rc) rc = qgt_dev_malloc((void**)&pptr, sizeof(int32_t) * ((size_t)P + 1));
+    if (!rc) rc = qgt_dev_malloc((void**)&pslots, sizeof(int32_t) * (size_t)P);
+    if (!rc) rc = qgt_dev_malloc((void**)&sparam, sizeof(int32_t) * (size_t)P);
+    if (!rc) rc = qgt_dev_memcpy_h2d(pptr, hptr, sizeof(int32_t) * ((size_t)P + 1), s);
+    if (!rc) rc = qgt_dev_memcpy_h2d(pslots, hsl, sizeof(int32_t) * (size_t)P, s);
+    if (!rc) rc = qgt_dev_memcpy_h2d(sparam, hsl, sizeof(int32_t) * (size_t)P, s);
+    if (!rc && fp64) {
+        int nt = (rows + 31) / 32, ntp = nt * (nt + 1) / 2;
+        int ns = 4 * 152 / ntp;
+        if (ns < 1) ns = 1;
+        if (ns > dim / 16) ns = (int)(dim / 16 > 0 ? dim / 16 : 1);
+        rc = qgt_dev_malloc((void**)&part, sizeof(double) * 2 * 1024 * (size_t)ntp * ns);
+        if (!rc) rc = qgt_dev_gram_f64(X, dim, rows, part, ns, HG, s);
+    } else if (!rc) {
+        /* power-of-two prescale so that max |x| * scale <= 2^14 */
+        double mx = 0;
+        for (int64_t i = 0; i < 2 * dim; i++) mx = fmax(mx, fabs(psi[i]));
+        for (int64_t i = 0; i < 2 * dim * (int64_t)P; i++) mx = fmax(mx, fabs(D[i]));
+        int e = 0;
+        if (mx > 0) { frexp(mx, &e); }
+        float scale = (float)ldexp(1.0, 14 - e);
+        int64_t ld = dim < 32 ? 32 : (dim + 31) / 32 * 32;
+        int rows_pad = (rows + 127) / 128 * 128;
+        size_t sb = (size_t)4 * rows_pad * ld * 2;
+        rc = qgt_dev_malloc(&split, sb);
+        if (!rc) rc = qgt_dev_memset(split, 0, sb, s);
+        if (!rc) rc = qgt_dev_split_rows(X, rows, dim, split, ld, (int64_t)rows_pad * ld, 0, scale,
+                                         prec == QGT_PRECISION_MIXED_BF16X3, s);
+        if (!rc) rc = qgt_dev_tc_gram_create(split, ld, rows, rows_pad, prec == QGT_PRECISION_MIXED_BF16X3, &tc);
+        if (!rc) rc = qgt_dev_tc_gram_run(tc, 1.0 / ((double)scale * scale), HG, s);
+    }
+    if (!rc) {
+        qgt_dev_post_args_t pa;
+        memset(&pa, 0, sizeof pa);
+        pa.HG = HG;
+        pa.rows = rows;
+        pa.P = P;
+        pa.slot_param = sparam;
+        pa.param_ptr = pptr;
+        pa.param_slots = pslots;
+        pa.hscale = 1.0;
+        pa.Q = Qd;
+        rc = qgt_dev_post(&pa, s);
+    }
+    if (!rc) rc = qgt_dev_memcpy_d2h(Q, Qd, sizeof(double) * 2 * (size_t)P * P, s);
+    if (!rc) rc = qgt_dev_stream_sync(s);
+    if (!rc && tc) {
+        int st = qgt_dev_tc_gram_status(tc, s);
+        if (st) rc = qgt_set_error(st, "tensor-core Gram reported device status %d", st);
+    }
+    qgt_dev_tc_gram_destroy(tc);
+    qgt_dev_free(X); qgt_dev_free(part); qgt_dev_free(HG); qgt_dev_free(Qd); qgt_dev_free(split);
+    qgt_dev_free(pptr); qgt_dev_free(pslots); qgt_dev_free(sparam);
+    if (s) qgt_dev_stream_destroy(s);
+    free(hptr);
+    free(hsl);
+    return rc;
+}
+
+/* ---- reference diffgeo entry points ---- */
+
+struct diffgeo_engine {
+    int precision;
+    size_t metric_evaluations, curvature_evaluations;
+};
+
+diffgeo_engine_t* diffgeo_engine_create(void)
+{
+    diffgeo_engine_t* e = (diffgeo_engine_t*)calloc(1, sizeof(diffgeo_engine_t));
+    if (e) e->precision = QGT_PRECISION_FP64;
+    return e;
+}
+
+void diffgeo_engine_destroy(diffgeo_engine_t* e) { free(e); }
+
+static bool diffgeo_q(diffgeo_engine_t* e, const ComplexDouble* state, size_t dim, const ComplexDouble* d, size_t P,
+                      double** Qout)
+{
+    if (!e || !state || !d || dim == 0 || P == 0 || P > 0x7fffffff) return false;
+    double* Q = (double*)malloc(sizeof(double) * 2 * P * P);
+    if (!Q) return false;
+    if (qgt_qgt_from_states((const double*)state, (const double*)d, (int64_t)dim, (int32_t)P,
+                            (qgt_precision_t)e->precision, Q) != 0) {
+        free(Q);
+        return false;
+    }
+    *Qout = Q;
+    return true;
+}
+
+bool diffgeo_compute_fubini_study(diffgeo_engine_t* e, const ComplexDouble* state, size_t dim,
+                                  const ComplexDouble* d, size_t P, double* metric_out)
+{
+    double* Q = NULL;
+    if (!metric_out || !diffgeo_q(e, state, dim, d, P, &Q)) return false;
+    for (size_t i = 0; i < P * P; i++) metric_out[i] = Q[2 * i];
+    free(Q);
+    e->metric_evaluations++;
+    return true;
+}
+
+bool diffgeo_compute_berry_curvature(diffgeo_engine_t* e, const ComplexDouble* state, size_t dim,
+                                     const ComplexDouble* d, size_t P, double* curvature_out)
+{
+    double* Q = NULL;
+    if (!curvature_out || !diffgeo_q(e, state, dim, d, P, &Q)) return false;
+    for (size_t i = 0; i < P * P; i++) curvature_out[i] = -2.0 * Q[2 * i + 1];
+    free(Q);
+    e->curvature_evaluations++;
+    return true;
+}

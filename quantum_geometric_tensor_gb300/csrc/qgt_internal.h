@@ -1,0 +1,174 @@
+/*
+ * qgt_internal.h -- structures shared by the C host (pass compiler, plan
+ * driver, reference API) and the CUDA translation units, and the thin
+ * qgt_dev_* C ABI through which host code reaches the device.
+ *
+ * Data layout in HBM (per plan):
+ *   V       (rows + 1) x N amplitudes, complex128 (FP64 plan) or complex64
+ *           (mixed plan).  Row 0 = psi, row 1 = H psi, row 2 + s = derivative
+ *           slot s; row `rows` is the second psi buffer (psi ping-pongs
+ *           between row 0 and row `rows` across passes, ending in row 0).
+ *   SPLIT   (mixed only) 4 planes {Re hi, Re lo, Im hi, Im lo} x rows_pad x N
+ *           half-precision values, K-major (amplitude index contiguous), the
+ *           operands of the tensor-core Gram.
+ *   PART    split-K partial Gram blocks; HG = (rows x rows) complex FP64 Gram.
+ */
+#ifndef QGT_INTERNAL_H
+#define QGT_INTERNAL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QGT_MAX_QUBITS 30
+#define QGT_TILE_MAX_F32 13   /* 2^13 complex64 = 64 KiB of shared memory */
+#define QGT_TILE_MAX_F64 12   /* 2^12 complex128 = 64 KiB */
+#define QGT_LANE_BITS 5       /* qubits 0..4 are always tile bits: 256 B coalesced segments */
+#define QGT_PASS_THREADS 256
+
+/* ops of a tile pass (one per gate, in pass order) */
+enum {
+    QOP_1Q = 1,     /* dense 2x2 on tile bit lb (coef: m00 m01 m10 m11) */
+    QOP_PHASE = 2,  /* diag(p0, p1) on qubit q (coef: m00 = p0, m11 = p1) */
+    QOP_CZ = 3,     /* -1 on |11> of qubits (q, q2) */
+    QOP_CNOT = 4,   /* X on tile bit lb when qubit q2 (control) is 1 */
+    QOP_SWAP = 5    /* swap tile bits lb and lb2 */
+};
+
+/* generator inserted for a derivative: (-i/2) G after the op */
+enum { QGEN_NONE = 0, QGEN_X = 1, QGEN_Y = 2, QGEN_Z = 3 };
+
+typedef struct {
+    int8_t kind;    /* QOP_* */
+    int8_t lb;      /* tile-local bit of the target / first qubit, -1 if outside the tile */
+    int8_t lb2;     /* tile-local bit of the second qubit (CNOT control, CZ/SWAP second), or -1 */
+    int8_t gen;     /* QGEN_* for parameterised rotations */
+    int8_t q;       /* physical qubit of lb */
+    int8_t q2;      /* physical qubit of lb2 */
+    int16_t pad;
+    int32_t coef;   /* coefficient index, -1 if none */
+    int32_t slot;   /* derivative slot of this gate, -1 if none */
+} qgt_dev_op_t;
+
+/* gate coefficient source: the prepare kernel turns theta into matrices */
+typedef struct {
+    int32_t type;   /* QGT_GATE_* */
+    int32_t param;  /* theta index, -1 = fixed */
+    double angle;
+} qgt_dev_coef_desc_t;
+
+enum {
+    QENT_STORE_V = 1,      /* write the result to V[dst_row] */
+    QENT_STORE_SPLIT = 2,  /* write the result to SPLIT row split_row */
+    QENT_SRC_ZERO = 4      /* source is |0...0> (no read) */
+};
+
+typedef struct {
+    int32_t src_row;
+    int32_t dst_row;
+    int32_t spawn_op;   /* op index (in the pass) after which (-i/2)G is inserted; -1 = transport */
+    int32_t flags;      /* QENT_* */
+    int32_t split_row;
+    int32_t pad;
+} qgt_dev_entry_t;
+
+typedef struct {
+    void* V;                        /* vector buffer (c64 or c128) */
+    int64_t N;                      /* 2^n */
+    const qgt_dev_op_t* ops;        /* device pointer to this pass's ops */
+    int32_t nops;
+    const qgt_dev_entry_t* entries; /* device pointer */
+    int32_t nentries;
+    const double* coef;             /* device coefficient table, 8 doubles per coef */
+    void* split;                    /* SPLIT base (mixed) */
+    int64_t split_ld;               /* row length of a split plane (N rounded up to 32) */
+    int64_t split_plane_stride;     /* elements between planes = rows_pad * split_ld */
+    float split_scale;              /* power of two applied before splitting */
+    int32_t split_bf16;             /* 0: FP16 planes, 1: BF16 planes */
+    int32_t n;
+    int32_t tile_bits;
+    uint32_t tile_mask;             /* physical qubits held in the tile */
+    int8_t local_to_phys[16];
+} qgt_dev_pass_args_t;
+
+/* internal plan helpers used by the reference API layer */
+struct qgt_plan;
+int qgt_plan_combine_slots(struct qgt_plan* p, const double* c, double* out);
+
+/* thread-local last error (host/qgt_error.c): stores the message and returns code */
+int qgt_set_error(int code, const char* fmt, ...);
+void qgt_clear_error(void);
+
+/* ---- device context / memory (qgt_device.cu) ---- */
+int qgt_dev_set_device(int device);
+int qgt_dev_malloc(void** p, size_t bytes);
+int qgt_dev_free(void* p);
+int qgt_dev_memcpy_h2d(void* dst, const void* src, size_t bytes, void* stream);
+int qgt_dev_memcpy_d2h(void* dst, const void* src, size_t bytes, void* stream);
+int qgt_dev_memcpy_d2d(void* dst, const void* src, size_t bytes, void* stream);
+int qgt_dev_memset(void* dst, int value, size_t bytes, void* stream);
+int qgt_dev_stream_create(void** stream);
+int qgt_dev_stream_destroy(void* stream);
+int qgt_dev_stream_sync(void* stream);
+int qgt_dev_graph_begin(void* stream);
+int qgt_dev_graph_end(void* stream, void** exec);
+int qgt_dev_graph_launch(void* exec, void* stream);
+int qgt_dev_graph_destroy(void* exec);
+int qgt_dev_host_alloc(void** p, size_t bytes);   /* pinned */
+int qgt_dev_host_free(void* p);
+int qgt_dev_last_error(void);                     /* cudaGetLastError as qgt_error_t */
+const char* qgt_dev_error_string(void);
+
+/* ---- kernels ---- */
+int qgt_dev_prepare(const qgt_dev_coef_desc_t* descs_dev, int32_t ncoef, const double* theta_dev,
+                    double* coef_dev, void* stream);
+int qgt_dev_pass(const qgt_dev_pass_args_t* args, int fp64, void* stream);
+/* out (row 1 of V, and split row 1 when split != NULL) = H psi / hscale */
+int qgt_dev_tfim(const void* psi, void* out, int32_t n, double J, double h, double inv_hscale,
+                 int fp64, void* split, int64_t split_ld, int64_t split_plane_stride, int32_t split_row,
+                 float split_scale, int32_t split_bf16, void* stream);
+/* complex128 rows X (rows x N) -> split planes rows [row0, row0 + rows) */
+int qgt_dev_split_rows(const double* X, int32_t rows, int64_t N, void* split, int64_t split_ld, int64_t split_plane_stride,
+                       int32_t row0, float scale, int32_t bf16, void* stream);
+/* out = sum_k c[k] V[row0 + k] over complex128 rows (c on the device) */
+int qgt_dev_combine_rows(const void* V, int64_t N, int32_t row0, const double* c, int32_t K, void* out, void* stream);
+/* FP64 Gram of rows [0, rows) of V (complex128): HG = V V^H (HG_ij = <V_i|V_j>) */
+int qgt_dev_gram_f64(const void* V, int64_t N, int32_t rows, double* part, int32_t nsplit,
+                     double* HG, void* stream);
+/* tensor-core Gram on the split operands; HG as above, scaled back by 1/scale^2 */
+typedef struct qgt_tc_gram qgt_tc_gram_t;
+int qgt_dev_tc_gram_create(void* split, int64_t N, int32_t rows, int32_t rows_pad, int32_t bf16,
+                           qgt_tc_gram_t** g);
+int qgt_dev_tc_gram_run(qgt_tc_gram_t* g, double inv_scale2, double* HG, void* stream);
+void qgt_dev_tc_gram_destroy(qgt_tc_gram_t* g);
+/* device error word of the last run (0 ok, QGT_ERROR_TIMEOUT on an expired wait); synchronises */
+int qgt_dev_tc_gram_status(qgt_tc_gram_t* g, void* stream);
+int64_t qgt_dev_tc_gram_scratch_bytes(const qgt_tc_gram_t* g);
+/* HG -> Q, grad, energy (FP64 renormalisation + projector + slot->param sum) */
+typedef struct {
+    const double* HG;
+    int32_t rows;           /* 2 + slots */
+    int32_t P;              /* parameters */
+    const int32_t* slot_param;  /* slot -> param */
+    const int32_t* param_ptr;   /* CSR over params: slots of param p = param_slots[param_ptr[p] .. param_ptr[p+1]) */
+    const int32_t* param_slots;
+    double hscale;          /* H psi row was divided by this */
+    int32_t has_h;
+    double* Q;              /* P x P complex */
+    double* grad;           /* P */
+    double* energy;         /* 1 */
+} qgt_dev_post_args_t;
+int qgt_dev_post(const qgt_dev_post_args_t* a, void* stream);
+/* (Re Q + lambda I) x = b, FP64 Cholesky; A taken as Re of the complex Q when
+ * complex_input, else a real P x P matrix.  status[0] = 0 ok / error code,
+ * status[1] = lambda used (as double bits in the second slot). */
+int qgt_dev_cholesky(const double* A, int complex_input, const double* b, int32_t P,
+                     double lambda, double* work, double* x, double* status, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
