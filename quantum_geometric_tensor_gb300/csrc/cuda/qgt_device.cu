@@ -141,9 +141,11 @@ __global__ void prepare_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const do
 // ---------------------------------------------------------------------------
 template <typename T, typename R>
 __global__ void tfim_kernel(const T* __restrict__ psi, T* __restrict__ out, int n, R J, R h, R inv,
-                            void* split, int64_t sld, int64_t pstride, int32_t srow, float sscale, int bf16)
+                            void* split, int64_t sld, int64_t pstride, int32_t srow, float sscale, int bf16,
+                            uint32_t* rowmax)
 {
     int64_t N = (int64_t)1 << n;
+    float vmax = 0.f;
     int nb = n >= 3 ? n : n - 1;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
         int zz = 0;
@@ -162,6 +164,7 @@ __global__ void tfim_kernel(const T* __restrict__ psi, T* __restrict__ out, int 
         o.x = ar * inv;
         o.y = ai * inv;
         out[i] = o;
+        vmax = fmaxf(vmax, sqrtf((float)(o.x * o.x + o.y * o.y)));
         if (split) {
             float xr = (float)o.x * sscale, xi = (float)o.y * sscale;
             int64_t at = (int64_t)srow * sld + i;
@@ -180,6 +183,17 @@ __global__ void tfim_kernel(const T* __restrict__ psi, T* __restrict__ out, int 
                 s[2 * pstride + at] = ih;
                 s[3 * pstride + at] = __float2half_rn(xi - __half2float(ih));
             }
+        }
+    }
+    if (rowmax) {
+        __shared__ float red[32];
+        for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = vmax;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float m = 0.f;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) m = fmaxf(m, red[w]);
+            atomicMax(rowmax, __float_as_uint(m));
         }
     }
 }
@@ -333,18 +347,19 @@ int qgt_dev_prepare(const qgt_dev_coef_desc_t* d, int32_t ncoef, const double* t
 }
 
 int qgt_dev_tfim(const void* psi, void* out, int32_t n, double J, double h, double inv, int fp64,
-                 void* split, int64_t sld, int64_t pstride, int32_t srow, float sscale, int32_t bf16, void* s)
+                 void* split, int64_t sld, int64_t pstride, int32_t srow, float sscale, int32_t bf16,
+                 uint32_t* rowmax, void* s)
 {
     int64_t N = (int64_t)1 << n;
     int blocks = (int)((N + 255) / 256);
     if (blocks > 152 * 16) blocks = 152 * 16;
     if (fp64)
         tfim_kernel<double2, double><<<blocks, 256, 0, (cudaStream_t)s>>>((const double2*)psi, (double2*)out, n, J, h,
-                                                                            inv, NULL, 0, 0, 0, 0.f, 0);
+                                                                            inv, NULL, 0, 0, 0, 0.f, 0, NULL);
     else
         tfim_kernel<float2, float><<<blocks, 256, 0, (cudaStream_t)s>>>((const float2*)psi, (float2*)out, n, (float)J,
                                                                           (float)h, (float)inv, split, sld, pstride, srow,
-                                                                          sscale, bf16);
+                                                                          sscale, bf16, rowmax);
     return qgt_dev_last_error();
 }
 
@@ -437,5 +452,19 @@ extern "C" int qgt_dev_combine_rows(const void* V, int64_t N, int32_t row0, cons
     int blocks = (int)((N + 255) / 256);
     if (blocks > 152 * 16) blocks = 152 * 16;
     combine_rows_kernel<<<blocks, 256, 0, (cudaStream_t)s>>>((const double2*)V, N, row0, c, K, (double2*)out);
+    return qgt_dev_last_error();
+}
+
+__global__ void c128_to_c64_kernel(const double* __restrict__ X, int64_t count, float* __restrict__ Y)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+        Y[i] = (float)X[i];
+}
+
+extern "C" int qgt_dev_c128_to_c64(const double* X, int64_t count, float* Y, void* s)
+{
+    int blocks = (int)((count + 255) / 256);
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    if (count > 0) c128_to_c64_kernel<<<blocks, 256, 0, (cudaStream_t)s>>>(X, count, Y);
     return qgt_dev_last_error();
 }

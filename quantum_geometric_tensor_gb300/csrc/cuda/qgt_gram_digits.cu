@@ -1,0 +1,515 @@
+// qgt_gram_digits.cu -- the mixed-precision Gram HG_ij = <V_i|V_j> on tcgen05
+// tensor cores with exactly accumulated high digits.
+//
+// Why: the tensor cores' FP32 accumulation truncates, which over long K
+// chains biases every large sum (the diagonal by ~-3e-8 per MMA), so a plain
+// hi/lo split cannot reach 1e-6 relative on 2^20 amplitudes.  Here every
+// complex64 amplitude of row r is written, in units of a per-row power of two
+// u_r (max_k |x_rk| < M u_r, M = 2^mbits), as
+//     x = u_r (D + l),  D = rint(x / u_r) in [-M, M],  |l| <= 1/2,
+// with D exact in FP16 and l rounded to FP16.  The D*D' products are
+// integers and every partial sum of them over a CTA's K range is at most
+// 2^23 (Cauchy-Schwarz; M is chosen per plan from the K range, M = 32 for
+// 4096 amplitudes, up to 1024 for short ranges), so their FP32 tensor
+// accumulation is EXACT.  The D*l', l*D', l*l' terms (a few percent of the
+// total) accumulate in a second TMEM accumulator; their rounding is
+// ~1e-8 relative to the sum.
+//
+// Data path per CTA (tile pair mb <= nb, K range of <= 4096 amplitudes):
+//   TMA: 128 rows x 16 amplitudes of complex64 per row block -> raw smem
+//   4 converter warps: raw -> 4 FP16 planes {Re D, Re l, Im D, Im l}
+//                      in the SWIZZLE_32B K-major UMMA layout
+//   1 thread: 16 tcgen05.mma (M = N = 128, K = 16) per k-step into
+//             TMEM [D*D Re | D*D Im | rest Re | rest Im] (512 columns)
+//   epilogue (the converter warps): TMEM -> FP32 (hh + rest) -> partials
+// A second kernel sums the partials in FP64 and applies u_i u_j.
+//
+// Every mbarrier wait is bounded (globaltimer); on expiry the CTA records an
+// error in *err, stops, drains its own TMA loads and MMAs, frees TMEM.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdlib.h>
+
+#include "../qgt_internal.h"
+
+#define DG_STAGES 3
+#define DG_BK 16                                    // amplitudes per stage (one MMA k-step)
+#define DG_RAW_BYTES (128 * DG_BK * 8)              // 16 KiB: 128 rows x 16 complex64
+#define DG_PLANE_BYTES (128 * DG_BK * 2)            // 4 KiB: 128 rows x 16 fp16
+#define DG_STAGE_BYTES (2 * DG_RAW_BYTES + 8 * DG_PLANE_BYTES)  // 64 KiB
+#define DG_SMEM_BYTES (DG_STAGES * DG_STAGE_BYTES + 1024)
+#define DG_KMAX 4096                                // amplitudes per CTA (exactness bound)
+#define DG_TIMEOUT_NS 4000000000ull
+#define DG_ERR_TIMEOUT (-13)
+#define DG_ERR_INEXACT (-24)
+
+struct qgt_dg_gram {
+    CUtensorMap tmap;
+    const void* V;
+    int64_t N;
+    int rows, nbk, ntp, nsplit;
+    int64_t kchunk;
+    int mbits;                 /* digits D in [-2^mbits, 2^mbits] */
+    const uint32_t* rowmax;
+    float* part;
+    int* err;
+};
+
+static __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+static __device__ __forceinline__ uint64_t gtimer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+static __device__ __forceinline__ void bar_init(uint32_t b, uint32_t c)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(b), "r"(c) : "memory");
+}
+
+static __device__ __forceinline__ void bar_expect_tx(uint32_t b, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+}
+
+static __device__ __forceinline__ void bar_arrive(uint32_t b)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(b) : "memory");
+}
+
+static __device__ __forceinline__ bool bar_wait(uint32_t b, uint32_t parity, uint64_t deadline)
+{
+    for (uint32_t it = 0;; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(b), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((it & 255u) == 255u && gtimer() > deadline) return false;
+    }
+}
+
+static __device__ __forceinline__ void tma_2d(uint32_t dst, const CUtensorMap* m, int c0, int c1, uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"((uint64_t)m), "r"(c0), "r"(c1), "r"(bar)
+        : "memory");
+}
+
+// K-major SWIZZLE_32B operand: rows of 32 B (16 fp16), 8-row groups 256 B apart
+static __device__ __forceinline__ uint64_t desc_sw32(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(256 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)6 << 61;  // SWIZZLE_32B
+    return d;
+}
+
+// kind::f16, D = F32, A = B = F16, K-major, M = N = 128
+static __device__ __forceinline__ uint32_t idesc_f16(int negA)
+{
+    return (1u << 4) | ((uint32_t)negA << 13) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+static __device__ __forceinline__ void umma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(a), "l"(b), "r"(id), "r"(acc)
+        : "memory");
+}
+
+static __device__ __forceinline__ void umma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+static __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+static __device__ __forceinline__ void pair_of(int tp, int nb, int* mb, int* nbo)
+{
+    int i = 0, rem = tp;
+    while (rem >= nb - i) { rem -= nb - i; i++; }
+    *mb = i;
+    *nbo = i + rem;
+}
+
+// unit exponent: rowmax < 2^e, u = 2^(e - mbits), so |x| < 2^mbits u
+static __device__ __forceinline__ int unit_exp(uint32_t bits, int mbits)
+{
+    float m = __uint_as_float(bits);
+    if (!(m > 0.f)) return 0;
+    int e;
+    frexpf(m, &e);  // m = f 2^e, f in [0.5, 1)
+    return e - mbits;
+}
+
+// (A plane, B plane, accumulator, negate A): accumulators 0 = D*D Re, 1 = D*D Im, 2 = rest Re, 3 = rest Im
+__constant__ int8_t dg_terms[16][4] = {
+    {0, 0, 0, 0}, {2, 2, 0, 0}, {0, 2, 1, 0}, {2, 0, 1, 1},
+    {0, 1, 2, 0}, {1, 0, 2, 0}, {1, 1, 2, 0}, {2, 3, 2, 0}, {3, 2, 2, 0}, {3, 3, 2, 0},
+    {0, 3, 3, 0}, {1, 2, 3, 0}, {1, 3, 3, 0}, {2, 1, 3, 1}, {3, 0, 3, 1}, {3, 1, 3, 1}};
+
+__global__ void __launch_bounds__(192, 1)
+    dg_gram_kernel(const __grid_constant__ CUtensorMap tmap, int nbk, int64_t N, int64_t kchunk,
+                   const uint32_t* __restrict__ rowmax, int rows, int mbits, float* __restrict__ part,
+                   int* __restrict__ err)
+{
+    extern __shared__ uint8_t dg_smem[];
+    __shared__ __align__(8) uint64_t full_bar[DG_STAGES];
+    __shared__ __align__(8) uint64_t ready_bar[DG_STAGES];
+    __shared__ __align__(8) uint64_t empty_bar[DG_STAGES];
+    __shared__ __align__(8) uint64_t done_bar;
+    __shared__ uint32_t tmem_sh;
+    __shared__ volatile int abort_sh;
+    __shared__ float inv_u[2][128];
+
+    uint8_t* sb = (uint8_t*)(((uintptr_t)dg_smem + 1023) & ~(uintptr_t)1023);
+    const uint32_t s0 = smem_u32(sb);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int mb, nbo;
+    pair_of(blockIdx.x, nbk, &mb, &nbo);
+    const bool diag = (mb == nbo);
+    const int nblk = diag ? 1 : 2;
+    const int64_t k0 = (int64_t)blockIdx.y * kchunk;
+    int64_t k1 = k0 + kchunk;
+    if (k1 > N) k1 = N;
+    const int nk = (int)((k1 - k0) / DG_BK);
+    const uint64_t deadline = gtimer() + DG_TIMEOUT_NS;
+
+    if (threadIdx.x < 128) {
+        for (int b = 0; b < 2; b++) {
+            int r = (b == 0 ? mb : nbo) * 128 + threadIdx.x;
+            float iu = 0.f;
+            if (r < rows) iu = ldexpf(1.0f, -unit_exp(rowmax[r], mbits));
+            inv_u[b][threadIdx.x] = iu;
+        }
+    }
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < DG_STAGES; s++) {
+            bar_init(smem_u32(&full_bar[s]), 1);
+            bar_init(smem_u32(&ready_bar[s]), 4);
+            bar_init(smem_u32(&empty_bar[s]), 1);
+        }
+        bar_init(smem_u32(&done_bar), 1);
+        abort_sh = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&tmem_sh)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_sh;
+    bool mma_done_commit = false;
+
+    if (warp == 0 && lane == 0) {
+        // ---------- TMA producer: complex64 rows ----------
+        const uint32_t bytes = (uint32_t)nblk * DG_RAW_BYTES;
+        int issued = 0;
+        for (int kt = 0; kt < nk; kt++) {
+            const int s = kt % DG_STAGES;
+            if (kt >= DG_STAGES && !bar_wait(smem_u32(&empty_bar[s]), ((kt / DG_STAGES) & 1) ^ 1, deadline)) {
+                atomicExch(err, DG_ERR_TIMEOUT);
+                abort_sh = 1;
+                break;
+            }
+            if (abort_sh) break;
+            const uint32_t st = s0 + s * DG_STAGE_BYTES;
+            const uint32_t fb = smem_u32(&full_bar[s]);
+            bar_expect_tx(fb, bytes);
+            const int x = (int)(2 * (k0 + (int64_t)kt * DG_BK));  // float index
+            tma_2d(st, &tmap, x, mb * 128, fb);
+            if (!diag) tma_2d(st + DG_RAW_BYTES, &tmap, x, nbo * 128, fb);
+            issued = kt + 1;
+        }
+        for (int u = issued - DG_STAGES; u < issued; u++)
+            if (u >= 0) (void)bar_wait(smem_u32(&full_bar[u % DG_STAGES]), (u / DG_STAGES) & 1, deadline + DG_TIMEOUT_NS);
+    } else if (warp == 1 && lane == 0) {
+        // ---------- MMA issuer ----------
+        const uint32_t idp = idesc_f16(0), idn = idesc_f16(1);
+        for (int kt = 0; kt < nk; kt++) {
+            const int s = kt % DG_STAGES;
+            if (!bar_wait(smem_u32(&ready_bar[s]), (kt / DG_STAGES) & 1, deadline)) {
+                atomicExch(err, DG_ERR_TIMEOUT);
+                abort_sh = 1;
+                break;
+            }
+            if (abort_sh) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t pa = s0 + s * DG_STAGE_BYTES + 2 * DG_RAW_BYTES;
+            const uint32_t pb = diag ? pa : pa + 4 * DG_PLANE_BYTES;
+#pragma unroll
+            for (int t = 0; t < 16; t++) {
+                const int a = dg_terms[t][0], b = dg_terms[t][1], acc = dg_terms[t][2], ng = dg_terms[t][3];
+                const uint32_t first = (kt == 0) && (t == 0 || t == 2 || t == 4 || t == 10);
+                umma(tmem + (uint32_t)acc * 128u, desc_sw32(pa + a * DG_PLANE_BYTES), desc_sw32(pb + b * DG_PLANE_BYTES),
+                     ng ? idn : idp, first ? 0u : 1u);
+            }
+            umma_commit(smem_u32(&empty_bar[s]));
+        }
+        umma_commit(smem_u32(&done_bar));
+        mma_done_commit = true;
+    } else if (warp >= 2) {
+        // ---------- converters: raw complex64 -> {Re D, Re l, Im D, Im l} ----------
+        const int cw = warp - 2;  // rows r = cw, cw + 4, ...
+        for (int kt = 0; kt < nk; kt++) {
+            const int s = kt % DG_STAGES;
+            if (!bar_wait(smem_u32(&full_bar[s]), (kt / DG_STAGES) & 1, deadline)) {
+                atomicExch(err, DG_ERR_TIMEOUT);
+                abort_sh = 1;
+            }
+            if (abort_sh) break;
+            uint8_t* st = sb + s * DG_STAGE_BYTES;
+            const int comp = lane & 1, k = lane >> 1;
+            for (int b = 0; b < nblk; b++) {
+                const float* raw = reinterpret_cast<const float*>(st + b * DG_RAW_BYTES);
+                uint8_t* planes = st + 2 * DG_RAW_BYTES + b * 4 * DG_PLANE_BYTES;
+                for (int r = cw; r < 128; r += 4) {
+                    const float x = raw[r * 32 + lane] * inv_u[b][r];
+                    const float d = rintf(x);
+                    const __half hd = __float2half_rn(d);
+                    const __half hl = __float2half_rn(x - d);
+                    // SWIZZLE_32B: 16-byte chunk (k / 8) xor bit 2 of the row
+                    const int off = r * 32 + ((((k >> 3) ^ (r >> 2)) & 1) << 4) + (k & 7) * 2;
+                    *reinterpret_cast<__half*>(planes + (comp ? 2 : 0) * DG_PLANE_BYTES + off) = hd;
+                    *reinterpret_cast<__half*>(planes + (comp ? 3 : 1) * DG_PLANE_BYTES + off) = hl;
+                }
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) bar_arrive(smem_u32(&ready_bar[s]));
+        }
+        // ---------- epilogue ----------
+        const bool ok = nk > 0 && !abort_sh && bar_wait(smem_u32(&done_bar), 0, deadline);
+        float* out = part + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * (2 * 128 * 128);
+        const int quad = warp & 3;
+        const int row = quad * 32 + lane;
+        if (ok) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            float hh[32], rs[32];
+            const uint32_t lanebase = tmem + ((uint32_t)(quad * 32) << 16);
+            for (int ri = 0; ri < 2; ri++) {
+                for (int c = 0; c < 4; c++) {
+                    tmem_ld32(lanebase + ri * 128 + c * 32, hh);
+                    tmem_ld32(lanebase + 256 + ri * 128 + c * 32, rs);
+                    if (diag && ri == 0 && c == (row >> 5) && hh[row & 31] > 8388608.0f) atomicExch(err, DG_ERR_INEXACT);
+                    float4* o = reinterpret_cast<float4*>(out + ri * 128 * 128 + row * 128 + c * 32);
+#pragma unroll
+                    for (int j = 0; j < 8; j++)
+                        o[j] = make_float4(hh[4 * j] + rs[4 * j], hh[4 * j + 1] + rs[4 * j + 1], hh[4 * j + 2] + rs[4 * j + 2],
+                                           hh[4 * j + 3] + rs[4 * j + 3]);
+                }
+            }
+        } else {
+            if (!(nk > 0) || abort_sh) {
+                if (abort_sh) atomicExch(err, DG_ERR_TIMEOUT);
+            } else {
+                atomicExch(err, DG_ERR_TIMEOUT);
+            }
+            for (int c = 0; c < 128; c++) { out[row * 128 + c] = 0.f; out[128 * 128 + row * 128 + c] = 0.f; }
+        }
+    }
+    if (warp == 1 && lane == 0 && mma_done_commit) (void)bar_wait(smem_u32(&done_bar), 0, deadline + DG_TIMEOUT_NS);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+    }
+}
+
+__global__ void dg_reduce_kernel(const float* __restrict__ part, const uint32_t* __restrict__ rowmax, int rows, int nbk,
+                                 int ntp, int nsplit, int mbits, double2* __restrict__ HG)
+{
+    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)rows * rows) return;
+    int i = (int)(idx / rows), j = (int)(idx % rows);
+    if (i > j) return;
+    int ti = i >> 7, tj = j >> 7;
+    int tp = ti * nbk - ti * (ti - 1) / 2 + (tj - ti);
+    int64_t off = (int64_t)(i & 127) * 128 + (j & 127);
+    double re = 0, im = 0;
+    for (int s = 0; s < nsplit; s++) {
+        const float* b = part + ((int64_t)s * ntp + tp) * (2 * 128 * 128);
+        re += (double)b[off];
+        im += (double)b[128 * 128 + off];
+    }
+    double uu = ldexp(1.0, unit_exp(rowmax[i], mbits) + unit_exp(rowmax[j], mbits));
+    HG[(int64_t)i * rows + j] = make_double2(re * uu, im * uu);
+    HG[(int64_t)j * rows + i] = make_double2(re * uu, -im * uu);
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 dg_encode(void)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = NULL;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void* p = NULL;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+extern "C" int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, const uint32_t* rowmax, qgt_dg_gram_t** out)
+{
+    *out = NULL;
+    if (N % DG_BK || rows < 1 || ((uintptr_t)V & 15))
+        return qgt_set_error(-1, "digit gram: row length %lld must be a multiple of %d", (long long)N, DG_BK);
+    if (2 * N > 0x7fffffffLL) return qgt_set_error(-1, "digit gram: row length too large for TMA coordinates");
+    PFN_cuTensorMapEncodeTiled_v12000 enc = dg_encode();
+    if (!enc) return qgt_set_error(-6, "digit gram: cuTensorMapEncodeTiled unavailable");
+    qgt_dg_gram_t* g = (qgt_dg_gram_t*)calloc(1, sizeof(qgt_dg_gram_t));
+    if (!g) return qgt_set_error(-2, "digit gram: out of host memory");
+    g->V = V;
+    g->N = N;
+    g->rows = rows;
+    g->rowmax = rowmax;
+    int rows_pad = (rows + 127) / 128 * 128;
+    g->nbk = rows_pad / 128;
+    g->ntp = g->nbk * (g->nbk + 1) / 2;
+    /* K per CTA: at most DG_KMAX (exactness), and enough CTAs to fill the GPU */
+    int64_t kc = DG_KMAX;
+    int64_t want = (2 * 152 + g->ntp - 1) / g->ntp;
+    while (kc > 4 * DG_BK && (N + kc - 1) / kc < want) kc /= 2;
+    g->kchunk = kc;
+    g->nsplit = (int)((N + kc - 1) / kc);
+    /* widest digits whose products sum exactly over kc amplitudes:
+     * kc (M^2 + sqrt(2) M + 1/2) <= 2^23 with M = 2^mbits, |D_re|^2 + |D_im|^2 bounded through |x| < M u;
+     * M <= 1024 keeps D exact in FP16 */
+    g->mbits = 10;
+    while (g->mbits > 1) {
+        double M = (double)(1 << g->mbits);
+        if ((double)kc * (M * M + 1.4143 * M + 0.5) <= 8388608.0) break;
+        g->mbits--;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)(2 * N), (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(2 * N * 4)};
+    cuuint32_t box[2] = {2 * DG_BK, 128};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(&g->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)V, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        free(g);
+        return qgt_set_error(-6, "digit gram: cuTensorMapEncodeTiled failed (%d)", (int)r);
+    }
+    size_t pbytes = (size_t)g->nsplit * g->ntp * 2 * 128 * 128 * sizeof(float);
+    cudaError_t e = cudaMalloc((void**)&g->part, pbytes);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&g->err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(g->err, 0, sizeof(int));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(dg_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, DG_SMEM_BYTES);
+    if (e != cudaSuccess) {
+        cudaFree(g->part);
+        cudaFree(g->err);
+        free(g);
+        return qgt_set_error(e == cudaErrorMemoryAllocation ? -2 : -6, "digit gram: %s", cudaGetErrorString(e));
+    }
+    *out = g;
+    return 0;
+}
+
+extern "C" int qgt_dev_dg_gram_run(qgt_dg_gram_t* g, double* HG, void* stream)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    dg_gram_kernel<<<dim3(g->ntp, g->nsplit), 192, DG_SMEM_BYTES, s>>>(g->tmap, g->nbk, g->N, g->kchunk, g->rowmax,
+                                                                       g->rows, g->mbits, g->part, g->err);
+    int rc = qgt_dev_last_error();
+    if (rc) return rc;
+    int64_t cnt = (int64_t)g->rows * g->rows;
+    dg_reduce_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>(g->part, g->rowmax, g->rows, g->nbk, g->ntp, g->nsplit,
+                                                                   g->mbits, (double2*)HG);
+    return qgt_dev_last_error();
+}
+
+extern "C" int qgt_dev_dg_gram_status(qgt_dg_gram_t* g, void* stream)
+{
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, g->err, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return qgt_set_error(-6, "digit gram status: %s", cudaGetErrorString(e));
+    return h;
+}
+
+extern "C" void qgt_dev_dg_gram_destroy(qgt_dg_gram_t* g)
+{
+    if (!g) return;
+    cudaFree(g->part);
+    cudaFree(g->err);
+    free(g);
+}
+
+extern "C" int64_t qgt_dev_dg_gram_scratch_bytes(const qgt_dg_gram_t* g)
+{
+    return g ? (int64_t)g->nsplit * g->ntp * 2 * 128 * 128 * (int64_t)sizeof(float) : 0;
+}
+
+extern "C" void qgt_dev_dg_gram_shape(const qgt_dg_gram_t* g, int* ntp, int* nsplit, int64_t* kchunk)
+{
+    if (ntp) *ntp = g->ntp;
+    if (nsplit) *nsplit = g->nsplit;
+    if (kchunk) *kchunk = g->kchunk;
+}
+
+// ---- row maxima: max_k |x_rk| (complex modulus) of complex64 rows, as float bits ----
+__global__ void rowmax_kernel(const float2* __restrict__ V, int64_t N, int row0, int nrows, uint32_t* __restrict__ out)
+{
+    __shared__ float red[32];
+    const int r = row0 + blockIdx.y;
+    float m = 0.f;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        float2 v = V[(int64_t)r * N + i];
+        m = fmaxf(m, sqrtf(v.x * v.x + v.y * v.y));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) atomicMax(out + r, __float_as_uint(m));
+    }
+}
+
+extern "C" int qgt_dev_rowmax(const void* V, int64_t N, int32_t row0, int32_t nrows, uint32_t* out, void* s)
+{
+    if (nrows <= 0) return 0;
+    int bx = (int)((N + 255) / 256);
+    if (bx > 64) bx = 64;
+    rowmax_kernel<<<dim3(bx, nrows), 256, 0, (cudaStream_t)s>>>((const float2*)V, N, row0, nrows, out);
+    return qgt_dev_last_error();
+}

@@ -197,10 +197,12 @@ __global__ void __launch_bounds__(QGT_PASS_THREADS) pass_kernel(const qgt_dev_pa
         }
     }
     T* dst = reinterpret_cast<T*>(a.V) + (int64_t)e.dst_row * a.N;
+    float vmax = 0.f;
     for (int l = threadIdx.x; l < TS; l += blockDim.x) {
         uint64_t ph = base | scatter_local(l, t, l2p);
         T v = tile[l];
         if (e.flags & QENT_STORE_V) dst[ph] = v;
+        if (e.flags & QENT_ROWMAX) vmax = fmaxf(vmax, sqrtf((float)(v.x * v.x + v.y * v.y)));
         if (e.flags & QENT_STORE_SPLIT) {
             float xr = (float)v.x * a.split_scale, xi = (float)v.y * a.split_scale;
             int64_t at = (int64_t)e.split_row * a.split_ld + (int64_t)ph;
@@ -220,6 +222,18 @@ __global__ void __launch_bounds__(QGT_PASS_THREADS) pass_kernel(const qgt_dev_pa
                 s[2 * ps + at] = ih;
                 s[3 * ps + at] = __float2half_rn(xi - __half2float(ih));
             }
+        }
+    }
+    if (e.flags & QENT_ROWMAX) {
+        // block max -> one atomicMax per CTA (non-negative floats order like their bit patterns)
+        __shared__ float red[QGT_PASS_THREADS / 32];
+        for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = vmax;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float m = 0.f;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) m = fmaxf(m, red[w]);
+            atomicMax(a.rowmax + e.dst_row, __float_as_uint(m));
         }
     }
 }

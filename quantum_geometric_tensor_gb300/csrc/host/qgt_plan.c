@@ -91,7 +91,9 @@ struct qgt_plan {
     double* HG_d;
     double* part_d;
     int part_nsplit;
-    qgt_tc_gram_t* tc;
+    qgt_tc_gram_t* tc;            /* split-BF16 x3 Gram (operands written by the last pass) */
+    qgt_dg_gram_t* dg;            /* integer-digit FP16 Gram (mixed default) */
+    uint32_t* rowmax_d;           /* per-row max |amplitude| (float bits) for the digit Gram */
     double *Q_d, *grad_d, *energy_d, *natgrad_d, *chol_work_d, *status_d;
     int32_t *slot_param_d, *param_ptr_d, *param_slots_d;
     /* pinned host staging */
@@ -291,7 +293,8 @@ static int build_entries(qgt_plan_t* p)
     char* live = (char*)calloc((size_t)p->nslots + 1, 1);
     if (!live) return qgt_set_error(E_NOMEM, "entries: oom");
     const int last = p->npasses - 1;
-    const int split = !p->fp64;
+    const int split = p->opt.precision == QGT_PRECISION_MIXED_BF16X3;
+    const int rmax = p->opt.precision == QGT_PRECISION_MIXED ? QENT_ROWMAX : 0;
     p->vector_passes = 0;
     p->gate_bytes = 0;
     const int64_t ab = p->fp64 ? 16 : 8; /* bytes per amplitude */
@@ -313,7 +316,8 @@ static int build_entries(qgt_plan_t* p)
         e.src_row = psi_src < 0 ? 0 : psi_src;
         e.dst_row = psi_dst;
         e.spawn_op = -1;
-        e.flags = QENT_STORE_V | (psi_src < 0 ? QENT_SRC_ZERO : 0) | ((k == last && split) ? QENT_STORE_SPLIT : 0);
+        e.flags = QENT_STORE_V | (psi_src < 0 ? QENT_SRC_ZERO : 0) | ((k == last && split) ? QENT_STORE_SPLIT : 0) |
+                  (k == last ? rmax : 0);
         e.split_row = 0;
         p->ents_h[ne++] = e;
         p->gate_bytes += ab * p->N * ((psi_src < 0 ? 0 : 1) + 1) + ((k == last && split) ? 8 * p->N : 0);
@@ -324,7 +328,7 @@ static int build_entries(qgt_plan_t* p)
             e.src_row = 2 + s;
             e.dst_row = 2 + s;
             e.spawn_op = -1;
-            e.flags = (k == last && split) ? QENT_STORE_SPLIT : QENT_STORE_V;
+            e.flags = ((k == last && split) ? QENT_STORE_SPLIT : QENT_STORE_V) | (k == last ? rmax : 0);
             e.split_row = 2 + s;
             p->ents_h[ne++] = e;
             p->gate_bytes += ab * p->N + ((k == last && split) ? 8 * p->N : ab * p->N);
@@ -337,7 +341,8 @@ static int build_entries(qgt_plan_t* p)
             e.src_row = psi_src < 0 ? 0 : psi_src;
             e.dst_row = 2 + op->slot;
             e.spawn_op = j;
-            e.flags = (psi_src < 0 ? QENT_SRC_ZERO : 0) | ((k == last && split) ? QENT_STORE_SPLIT : QENT_STORE_V);
+            e.flags = (psi_src < 0 ? QENT_SRC_ZERO : 0) | ((k == last && split) ? QENT_STORE_SPLIT : QENT_STORE_V) |
+                      (k == last ? rmax : 0);
             e.split_row = 2 + op->slot;
             p->ents_h[ne++] = e;
             p->gate_bytes += ab * p->N * (psi_src < 0 ? 0 : 1) + ((k == last && split) ? 8 * p->N : ab * p->N);
@@ -443,7 +448,7 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
         size_t ab = p->fp64 ? 16 : 8;
         DALLOC(p->V, (size_t)(p->rows + 1) * (size_t)p->N * ab);
         if ((rc = qgt_dev_memset(p->V, 0, (size_t)(p->rows + 1) * (size_t)p->N * ab, p->stream)) != 0) goto fail;
-        if (!p->fp64) {
+        if (p->opt.precision == QGT_PRECISION_MIXED_BF16X3) {
             size_t sb = (size_t)4 * p->rows_pad * (size_t)p->split_ld * 2;
             DALLOC(p->split, sb);
             if ((rc = qgt_dev_memset(p->split, 0, sb, p->stream)) != 0) goto fail;
@@ -473,11 +478,14 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
         if (ns > maxs) ns = (int)maxs;
         p->part_nsplit = ns;
         DALLOC(p->part_d, sizeof(double) * 2 * 1024 * (size_t)ntp * ns);
-    } else {
-        if ((rc = qgt_dev_tc_gram_create(p->split, p->split_ld, p->rows, p->rows_pad,
-                                         p->opt.precision == QGT_PRECISION_MIXED_BF16X3, &p->tc)) != 0)
-            goto fail;
+    } else if (p->opt.precision == QGT_PRECISION_MIXED_BF16X3) {
+        if ((rc = qgt_dev_tc_gram_create(p->split, p->split_ld, p->rows, p->rows_pad, 1, &p->tc)) != 0) goto fail;
         p->device_bytes += qgt_dev_tc_gram_scratch_bytes(p->tc);
+    } else {
+        if (p->n < 4) { rc = qgt_set_error(E_INVAL, "mixed precision needs at least 4 qubits (use FP64)"); goto fail; }
+        DALLOC(p->rowmax_d, sizeof(uint32_t) * (size_t)p->rows);
+        if ((rc = qgt_dev_dg_gram_create(p->V, p->N, p->rows, p->rowmax_d, &p->dg)) != 0) goto fail;
+        p->device_bytes += qgt_dev_dg_gram_scratch_bytes(p->dg);
     }
     if ((rc = qgt_dev_memset(p->theta_d, 0, sizeof(double) * (size_t)(p->P + 1), p->stream)) != 0) goto fail;
     if ((rc = qgt_dev_memcpy_h2d(p->ops_d, p->ops_h, sizeof(qgt_dev_op_t) * (size_t)p->nops, p->stream)) != 0) goto fail;
@@ -518,6 +526,8 @@ void qgt_plan_destroy(qgt_plan_t* p)
     if (p->stream) qgt_dev_stream_sync(p->stream);
     qgt_dev_graph_destroy(p->graph);
     qgt_dev_tc_gram_destroy(p->tc);
+    qgt_dev_dg_gram_destroy(p->dg);
+    qgt_dev_free(p->rowmax_d);
     void* dev[] = {p->V, p->split, p->ops_d, p->ents_d, p->coef_desc_d, p->coef_d, p->theta_d, p->HG_d, p->part_d,
                    p->Q_d, p->grad_d, p->energy_d, p->natgrad_d, p->chol_work_d, p->status_d, p->slot_param_d,
                    p->param_ptr_d, p->param_slots_d};
@@ -560,6 +570,7 @@ static int run_step(qgt_plan_t* p)
     int launches = 0;
     if ((rc = qgt_dev_prepare(p->coef_desc_d, p->ncoef, p->theta_d, p->coef_d, p->stream)) != 0) return rc;
     launches += p->ncoef > 0;
+    if (p->dg && (rc = qgt_dev_memset(p->rowmax_d, 0, sizeof(uint32_t) * (size_t)p->rows, p->stream)) != 0) return rc;
     for (int k = 0; k < p->npasses; k++) {
         const spass_t* ps = &p->passes[k];
         qgt_dev_pass_args_t a;
@@ -580,6 +591,7 @@ static int run_step(qgt_plan_t* p)
         a.tile_bits = ps->tile_bits;
         a.tile_mask = ps->tile_mask;
         memcpy(a.local_to_phys, ps->l2p, sizeof a.local_to_phys);
+        a.rowmax = p->rowmax_d;
         if ((rc = qgt_dev_pass(&a, p->fp64, p->stream)) != 0) return rc;
         launches++;
     }
@@ -597,13 +609,15 @@ static int run_step(qgt_plan_t* p)
         size_t ab = p->fp64 ? 16 : 8;
         void* row1 = (char*)p->V + (size_t)p->N * ab;
         if ((rc = qgt_dev_tfim(p->V, row1, p->n, p->opt.tfim_J, p->opt.tfim_h, 1.0 / p->hscale, p->fp64,
-                               p->fp64 ? NULL : p->split, p->split_ld, (int64_t)p->rows_pad * p->split_ld, 1,
-                               p->split_scale, p->opt.precision == QGT_PRECISION_MIXED_BF16X3, p->stream)) != 0)
+                               p->split, p->split_ld, (int64_t)p->rows_pad * p->split_ld, 1, p->split_scale, 1,
+                               p->rowmax_d ? p->rowmax_d + 1 : NULL, p->stream)) != 0)
             return rc;
         launches++;
     }
     if (p->fp64) {
         if ((rc = qgt_dev_gram_f64(p->V, p->N, p->rows, p->part_d, p->part_nsplit, p->HG_d, p->stream)) != 0) return rc;
+    } else if (p->dg) {
+        if ((rc = qgt_dev_dg_gram_run(p->dg, p->HG_d, p->stream)) != 0) return rc;
     } else {
         double s = (double)p->split_scale;
         if ((rc = qgt_dev_tc_gram_run(p->tc, 1.0 / (s * s), p->HG_d, p->stream)) != 0) return rc;
@@ -687,8 +701,8 @@ int qgt_plan_execute_host(qgt_plan_t* p, const double* theta, double* Q, double*
     if (grad) memcpy(grad, p->grad_pin, sizeof(double) * (size_t)p->P);
     if (energy) *energy = p->energy_pin[0];
     if (natgrad) memcpy(natgrad, p->natgrad_pin, sizeof(double) * (size_t)p->P);
-    if (p->tc) {
-        int st = qgt_dev_tc_gram_status(p->tc, p->stream);
+    if (p->tc || p->dg) {
+        int st = p->tc ? qgt_dev_tc_gram_status(p->tc, p->stream) : qgt_dev_dg_gram_status(p->dg, p->stream);
         if (st) return qgt_set_error(st, "tensor-core Gram reported device status %d", st);
     }
     return 0;
@@ -740,6 +754,7 @@ int qgt_plan_device_status(qgt_plan_t* p, double* lambda_used)
     if (lambda_used) *lambda_used = p->status_pin[1];
     int st = (int)p->status_pin[0];
     if (!st && p->tc) st = qgt_dev_tc_gram_status(p->tc, p->stream);
+    if (!st && p->dg) st = qgt_dev_dg_gram_status(p->dg, p->stream);
     return st;
 }
 

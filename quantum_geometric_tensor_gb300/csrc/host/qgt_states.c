@@ -61,6 +61,29 @@ int qgt_qgt_from_states(const double* psi, const double* D, int64_t dim, int32_t
         if (ns > dim / 16) ns = (int)(dim / 16 > 0 ? dim / 16 : 1);
         rc = qgt_dev_malloc((void**)&part, sizeof(double) * 2 * 1024 * (size_t)ntp * ns);
         if (!rc) rc = qgt_dev_gram_f64(X, dim, rows, part, ns, HG, s);
+    } else if (!rc && prec == QGT_PRECISION_MIXED) {
+        /* complex64 rows (row length padded to 16 with zeros), per-row maxima, digit Gram */
+        int64_t ld = (dim + 15) / 16 * 16;
+        float* Y = NULL;
+        uint32_t* rmax = NULL;
+        qgt_dg_gram_t* dg = NULL;
+        rc = qgt_dev_malloc((void**)&Y, sizeof(float) * 2 * (size_t)ld * rows);
+        if (!rc) rc = qgt_dev_memset(Y, 0, sizeof(float) * 2 * (size_t)ld * rows, s);
+        for (int r = 0; !rc && r < rows; r++)
+            rc = qgt_dev_c128_to_c64(X + 2 * (size_t)dim * r, 2 * dim, Y + 2 * (size_t)ld * r, s);
+        if (!rc) rc = qgt_dev_malloc((void**)&rmax, sizeof(uint32_t) * (size_t)rows);
+        if (!rc) rc = qgt_dev_memset(rmax, 0, sizeof(uint32_t) * (size_t)rows, s);
+        if (!rc) rc = qgt_dev_rowmax(Y, ld, 0, rows, rmax, s);
+        if (!rc) rc = qgt_dev_dg_gram_create(Y, ld, rows, rmax, &dg);
+        if (!rc) rc = qgt_dev_dg_gram_run(dg, HG, s);
+        if (!rc) rc = qgt_dev_stream_sync(s);
+        if (!rc) {
+            int st = qgt_dev_dg_gram_status(dg, s);
+            if (st) rc = qgt_set_error(st, "tensor-core Gram reported device status %d", st);
+        }
+        qgt_dev_dg_gram_destroy(dg);
+        qgt_dev_free(Y);
+        qgt_dev_free(rmax);
     } else if (!rc) {
         /* power-of-two prescale so that max |x| * scale <= 2^14 */
         double mx = 0;

@@ -63,7 +63,8 @@ typedef struct {
 enum {
     QENT_STORE_V = 1,      /* write the result to V[dst_row] */
     QENT_STORE_SPLIT = 2,  /* write the result to SPLIT row split_row */
-    QENT_SRC_ZERO = 4      /* source is |0...0> (no read) */
+    QENT_SRC_ZERO = 4,     /* source is |0...0> (no read) */
+    QENT_ROWMAX = 8        /* atomically fold max |x| of the result into rowmax[dst_row] */
 };
 
 typedef struct {
@@ -92,6 +93,7 @@ typedef struct {
     int32_t tile_bits;
     uint32_t tile_mask;             /* physical qubits held in the tile */
     int8_t local_to_phys[16];
+    uint32_t* rowmax;               /* per-row max |amplitude| as float bits (QENT_ROWMAX) */
 } qgt_dev_pass_args_t;
 
 /* internal plan helpers used by the reference API layer */
@@ -129,7 +131,20 @@ int qgt_dev_pass(const qgt_dev_pass_args_t* args, int fp64, void* stream);
 /* out (row 1 of V, and split row 1 when split != NULL) = H psi / hscale */
 int qgt_dev_tfim(const void* psi, void* out, int32_t n, double J, double h, double inv_hscale,
                  int fp64, void* split, int64_t split_ld, int64_t split_plane_stride, int32_t split_row,
-                 float split_scale, int32_t split_bf16, void* stream);
+                 float split_scale, int32_t split_bf16, uint32_t* rowmax_slot, void* stream);
+/* complex128 -> complex64 rows */
+int qgt_dev_c128_to_c64(const double* X, int64_t count, float* Y, void* stream);
+/* rowmax[row0 + r] = max(rowmax, max_k |V[row0 + r][k]|) over complex64 rows (float bits) */
+int qgt_dev_rowmax(const void* V, int64_t N, int32_t row0, int32_t nrows, uint32_t* rowmax, void* stream);
+/* mixed-precision Gram of complex64 rows [0, rows) of V with exactly accumulated
+ * integer high digits (per-row power-of-two units from rowmax); HG as above */
+typedef struct qgt_dg_gram qgt_dg_gram_t;
+int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, const uint32_t* rowmax, qgt_dg_gram_t** g);
+int qgt_dev_dg_gram_run(qgt_dg_gram_t* g, double* HG, void* stream);
+int qgt_dev_dg_gram_status(qgt_dg_gram_t* g, void* stream);
+void qgt_dev_dg_gram_destroy(qgt_dg_gram_t* g);
+int64_t qgt_dev_dg_gram_scratch_bytes(const qgt_dg_gram_t* g);
+void qgt_dev_dg_gram_shape(const qgt_dg_gram_t* g, int* ntp, int* nsplit, int64_t* kchunk);
 /* complex128 rows X (rows x N) -> split planes rows [row0, row0 + rows) */
 int qgt_dev_split_rows(const double* X, int32_t rows, int64_t N, void* split, int64_t split_ld, int64_t split_plane_stride,
                        int32_t row0, float scale, int32_t bf16, void* stream);
