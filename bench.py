@@ -1,0 +1,376 @@
+"""Headline benchmark: QGTs/sec at 20 qubits, P = 320.
+
+Workload (one "step"): one parameter point of the 20-qubit hardware-efficient
+ansatz -- 8 layers of RY(q), RZ(q) on every qubit and a CZ ring (P = 320,
+480 gates), complex64 evolution, split-FP16 integer-digit tcgen05 Gram, FP64
+projector + renormalisation, TFIM ring (J = h = 1) energy gradient and the
+FP64 Cholesky natural-gradient step (Re Q + 1e-3 I) x = grad E.  Parameters
+are seeded uniform in [0, 2pi) (splitmix64); data are synthetic (the
+reference publishes no dataset for this path).  The working set (2.6 GB of
+derivative vectors) is far larger than L2, so no flush is needed between
+steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+The gb300 arm prints one JSON line with value (device-resident theta and
+outputs), e2e (host buffers through qgt_plan_execute_host), roofline of the
+dominant kernel, the FP64 GPU path timed on the same point with the mixed
+path's error against it, clocks sampled during the timed region, and the
+oracle's CPU baseline.  The reference arm times the CPU implementation of the
+path (the FP64 oracle port of the reference algorithms; the reference's own
+tree is not present on the GPU host) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_QUBITS, LAYERS, ENT, LAMBDA, SEED = 20, 8, "cz", 1e-3, 2026
+WORKLOAD = "hea20_L8_czring_P320_tfim_natgrad"
+METRIC = "QGTs/sec @20q,P=320 (mixed vs FP64 GPU, rel err<=1e-6); gate HBM GB/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu, self.rows, self.proc = gpu, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for nm, v in zip(names, r[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+            except Exception:
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws, local):
+    if ws <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return dist
+
+
+def cpu_baseline(threads: int | None = None):
+    """The FP64 oracle on the host cores on a bounded sample of the workload,
+    extrapolated to one full QGT step:
+      derivative generation: all 480 gates on psi + the first S parameters'
+        derivative vectors (the longest-lived ones); cost per vector-gate
+        application x the exact count for all 320 derivatives;
+      contraction: the Gram of S rows x 2^20 amplitudes; cost per pair x P(P+1)/2;
+      energy, gradient and Cholesky solve: measured in full."""
+    from oracle import oracle as O
+    O.build()
+    orc = O.Oracle()
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    g = O.ansatz(N_QUBITS, LAYERS, ENT)
+    P = O.num_params(g)
+    th = O.splitmix64_params(SEED, P)
+    S = 16
+    # keep only the first S parameters as parameters (others fixed) for the sample
+    gs = g.copy()
+    for i in range(len(gs)):
+        if gs[i]["param"] >= S:
+            gs[i]["angle"] = th[gs[i]["param"]]
+            gs[i]["param"] = -1
+    t0 = time.perf_counter()
+    psi, D = orc.derivatives(N_QUBITS, gs, th[:S], S)
+    t_deriv = time.perf_counter() - t0
+    live, a_sample, a_full = 0, 0, 0
+    live_full = 0
+    for gt in g:
+        a_full += 1 + live_full
+        if gt["param"] >= 0:
+            live_full += 1
+    for gt in gs:
+        a_sample += 1 + live
+        if gt["param"] >= 0:
+            live += 1
+    t_deriv_full = t_deriv / a_sample * a_full
+    t0 = time.perf_counter()
+    orc.qgt_from_states(psi, D)
+    t_gram = time.perf_counter() - t0
+    t_gram_full = t_gram / (S * (S + 1) / 2 + S) * (P * (P + 1) / 2 + P)
+    t0 = time.perf_counter()
+    hp = orc.tfim_apply(N_QUBITS, psi)
+    orc.energy_grad(D, hp)
+    A = np.eye(P) * 0.25
+    orc.cholesky_solve(A, np.ones(P), LAMBDA)
+    t_rest = time.perf_counter() - t0
+    total = t_deriv_full + t_gram_full + t_rest
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": 1.0 / total, "unit": "QGTs/sec", "cores": cores, "kind": "port",
+            "sample": (f"20q/8 layers, psi + {S} of {P} derivative states through all 480 gates "
+                       f"({t_deriv:.1f} s) and their {S}x{S} Gram ({t_gram:.1f} s), extrapolated by exact "
+                       f"vector-gate ({a_full}/{a_sample}) and pair counts; {total:.0f} s per QGT"),
+            "seconds_per_qgt": total}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline()
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = statistics.mean(vals)
+    line = {"metric": METRIC, "value": v, "unit": "QGTs/sec", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "qubits": N_QUBITS, "layers": LAYERS, "params": 320,
+                       "entangler": "cz_ring", "hamiltonian": "tfim_ring J=h=1", "lambda": LAMBDA},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "QGTs/sec", "cores": cb["cores"], "kind": cb["kind"],
+                             "sample": cb["sample"]},
+            "e2e": {"value": v, "unit": "QGTs/sec", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, ws, rank, local):
+    import torch
+    import quantum_geometric_tensor_gb300 as Q
+    from oracle import oracle as O
+
+    dist = init_dist(ws, local)
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    gates = Q.ansatz_gates(N_QUBITS, LAYERS, ENT)
+    P = 2 * N_QUBITS * LAYERS
+    theta = O.splitmix64_params(SEED + rank, P)
+    plan = Q.Plan(N_QUBITS, gates, P, precision=Q.MIXED, lam=LAMBDA, device=dev)
+    info = plan.info()
+    th_d = torch.tensor(theta, dtype=torch.float64, device=f"cuda:{dev}")
+    Q_d = torch.zeros((P, P, 2), dtype=torch.float64, device=f"cuda:{dev}")
+    g_d = torch.zeros(P, dtype=torch.float64, device=f"cuda:{dev}")
+    e_d = torch.zeros(1, dtype=torch.float64, device=f"cuda:{dev}")
+    x_d = torch.zeros(P, dtype=torch.float64, device=f"cuda:{dev}")
+    stream = torch.cuda.ExternalStream(plan.stream(), device=f"cuda:{dev}")
+    L = Q.lib()
+    torch.cuda.synchronize()
+
+    def step():
+        rc = L.qgt_plan_execute_device(plan.h, th_d.data_ptr(), Q_d.data_ptr(), g_d.data_ptr(), e_d.data_ptr(),
+                                       x_d.data_ptr())
+        if rc:
+            raise Q.QGTError(rc, "qgt_plan_execute_device")
+
+    for _ in range(args.warmup):
+        step()
+    plan.status()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    st, lam_used = plan.status()
+    if st != 0:
+        raise RuntimeError(f"device status {st} after the timed steps")
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * 1000.0 / ms
+
+    # e2e: host theta in, host Q / grad / energy / natgrad out, through the public C ABI
+    e2e_steps = max(2, min(args.steps, 10))
+    plan.run(theta)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        out = plan.run(theta)
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / e2e_steps
+    if dist:
+        t = torch.tensor([e2e_ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    h2d = P * 8
+    d2h = P * P * 16 + 2 * P * 8 + 8
+
+    if rank != 0:
+        plan.close()
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return 0
+
+    # phase breakdown + roofline of the dominant kernel (device events on the plan's stream)
+    prof = Q.StepProfile()
+    L.qgt_plan_profile_step(plan.h, C_byref(prof))
+    phases = {"passes": prof.passes_ms, "gram": prof.gram_ms, "hamiltonian": prof.hamiltonian_ms,
+              "post": prof.post_ms, "solve": prof.solve_ms, "prepare": prof.prepare_ms}
+    hbm, tfl, peak_src = peaks()
+    gate_gbs = info.gate_bytes / (prof.passes_ms * 1e-3) / 1e9
+    gram_tf = info.gram_flops / (prof.gram_ms * 1e-3) / 1e12
+    dom = max(("passes", "gram"), key=lambda k: phases[k])
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get(dom)
+        except Exception:
+            traffic = None
+    if dom == "passes":
+        roof = {"bound": "hbm", "kernel": "pass_kernel<float> (all tile passes of a step)", "achieved": gate_gbs,
+                "peak": hbm, "unit": "GB/s", "frac": gate_gbs / hbm, "traffic": traffic,
+                "peak_source": peak_src, "algorithmic_bytes": info.gate_bytes, "ms": prof.passes_ms}
+    else:
+        roof = {"bound": "tensor", "kernel": "dg_gram_kernel (+ split-K reduce)", "achieved": gram_tf, "peak": tfl,
+                "unit": "TFLOP/s", "frac": gram_tf / tfl, "traffic": traffic, "peak_source": peak_src,
+                "algorithmic_flops": info.gram_flops, "ms": prof.gram_ms}
+
+    # FP64 GPU path on the same point; mixed error against it
+    fp64 = None
+    try:
+        out_m = plan.run(theta)
+        with Q.Plan(N_QUBITS, gates, P, precision=Q.FP64, lam=LAMBDA, device=dev) as p64:
+            p64.run(theta)
+            t0 = time.perf_counter()
+            r64 = p64.run(theta)
+            t64 = (time.perf_counter() - t0) * 1000.0
+            pr64 = Q.StepProfile()
+            L.qgt_plan_profile_step(p64.h, C_byref(pr64))
+
+        def rel(a, b):
+            return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+        fp64 = {"ms_per_step": pr64.total_ms, "e2e_ms": t64, "value": 1000.0 / pr64.total_ms,
+                "speedup_mixed_vs_fp64": pr64.total_ms / ms,
+                "rel_err": {"metric": rel(out_m["Q"].real, r64["Q"].real), "berry": rel(out_m["Q"].imag, r64["Q"].imag),
+                            "qgt": rel(out_m["Q"], r64["Q"]), "grad": rel(out_m["grad"], r64["grad"]),
+                            "natgrad_step": rel(out_m["natgrad"], r64["natgrad"]),
+                            "energy_abs": abs(out_m["energy"] - r64["energy"])},
+                "phases_ms": {"passes": pr64.passes_ms, "gram": pr64.gram_ms, "solve": pr64.solve_ms}}
+    except Exception as ex:
+        fp64 = {"error": str(ex)[:200]}
+
+    cb = None
+    if ws == 1 and not args.no_cpu:
+        try:
+            cb = cpu_baseline()
+            cb.pop("seconds_per_qgt", None)
+        except Exception as ex:
+            cb = {"error": str(ex)[:200]}
+
+    line = {"metric": METRIC, "value": value, "unit": "QGTs/sec", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64/fp16-digits/f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "qubits": N_QUBITS, "layers": LAYERS, "params": P,
+                       "entangler": "cz_ring", "hamiltonian": "tfim_ring J=h=1", "lambda": LAMBDA,
+                       "precision": "mixed", "parallelism": f"replicas{ws}" if ws > 1 else "single",
+                       "l2": "working set 2.6 GB > L2 (no flush needed)"},
+            "e2e": {"value": ws * 1000.0 / e2e_ms, "unit": "QGTs/sec", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+            "gpu_launches": info.num_launches * args.steps,
+            "roofline": roof,
+            "phases_ms": phases,
+            "gate_hbm_gbs": gate_gbs,
+            "gram_tflops_algorithmic": gram_tf,
+            "plan": {"passes": info.num_passes, "vector_passes": info.vector_passes, "tile_bits": info.tile_bits,
+                     "device_gb": info.device_bytes / 1e9},
+            "fp64_gpu": fp64,
+            "clocks": clk.summary(),
+            "cpu_baseline": cb}
+    print(json.dumps(line), flush=True)
+    plan.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def C_byref(x):
+    import ctypes
+    return ctypes.byref(x)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+    return run_gb300(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

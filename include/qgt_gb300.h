@@ -140,6 +140,21 @@ int qgt_plan_get_row(qgt_plan_t* plan, int row, double* out);
  * (e.g. the Cholesky solve found no positive pivot after its retries). */
 int qgt_plan_device_status(qgt_plan_t* plan, double* lambda_used);
 
+/* Device time of each phase of one step, from CUDA events recorded between
+ * the phases on the plan's stream (the step runs eagerly, not from the graph;
+ * theta already on the device).  The reference's closest facility is the
+ * named-span profiler of src/quantum_geometric/core/quantum_geometric_profiling.c:12-110. */
+typedef struct {
+    double total_ms;
+    double prepare_ms;      /* theta -> gate matrices */
+    double passes_ms;       /* all tile passes (state + derivative evolution) */
+    double hamiltonian_ms;  /* H psi */
+    double gram_ms;         /* Gram contraction + split-K reduction */
+    double post_ms;         /* projector, energy, gradient */
+    double solve_ms;        /* natural-gradient Cholesky solve */
+} qgt_step_profile_t;
+int qgt_plan_profile_step(qgt_plan_t* plan, qgt_step_profile_t* prof);
+
 /* One-shot helpers over a temporary plan (reference-style convenience). */
 int qgt_compute_qgt_f64(const qgt_circuit_desc_t* circuit, const double* theta, double* Q,
                         qgt_precision_t precision);

@@ -72,7 +72,9 @@ bool disable_hardware_acceleration(quantum_geometric_tensor_network_t* qgtn);
 const char* get_quantum_geometric_tensor_network_error(void);
 
 /* Extension (no reference counterpart): precision of the GPU step behind the
- * QGTN queries; 0 = FP64 (default), 1 = mixed FP16x3, 2 = mixed BF16x3. */
+ * QGTN queries; 0 = FP64 (default), 1 = mixed (complex64 evolution, exact
+ * integer-digit FP16 tensor-core Gram), 2 = mixed BF16x3. Networks of fewer
+ * than 4 qubits run FP64 when 1 is selected. */
 bool qgtn_set_precision(quantum_geometric_tensor_network_t* qgtn, int precision);
 
 #ifdef __cplusplus

@@ -42,6 +42,12 @@ class PlanInfo(C.Structure):
                 ("gram_flops", C.c_int64), ("device_bytes", C.c_int64)]
 
 
+class StepProfile(C.Structure):
+    _fields_ = [("total_ms", C.c_double), ("prepare_ms", C.c_double), ("passes_ms", C.c_double),
+                ("hamiltonian_ms", C.c_double), ("gram_ms", C.c_double), ("post_ms", C.c_double),
+                ("solve_ms", C.c_double)]
+
+
 _lib = None
 
 
@@ -66,6 +72,7 @@ def lib() -> C.CDLL:
         L.qgt_plan_get_row.argtypes = [vp, C.c_int, vp]
         L.qgt_plan_device_status.argtypes = [vp, vp]
         L.qgt_cholesky_solve_f64.argtypes = [vp, vp, C.c_double, C.c_int32, vp, vp]
+        L.qgt_plan_profile_step.argtypes = [vp, C.POINTER(StepProfile)]
         L.qgt_last_error.restype = C.c_char_p
         L.qgt_version.restype = C.c_char_p
         _lib = L

@@ -468,3 +468,82 @@ extern "C" int qgt_dev_c128_to_c64(const double* X, int64_t count, float* Y, voi
     if (count > 0) c128_to_c64_kernel<<<blocks, 256, 0, (cudaStream_t)s>>>(X, count, Y);
     return qgt_dev_last_error();
 }
+
+extern "C" {
+int qgt_dev_event_create(void** ev)
+{
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e), "cudaEventCreate");
+    *ev = (void*)e;
+    return QGT_OK;
+}
+int qgt_dev_event_destroy(void* ev) { if (ev) CK(cudaEventDestroy((cudaEvent_t)ev), "cudaEventDestroy"); return QGT_OK; }
+int qgt_dev_event_record(void* ev, void* s) { CK(cudaEventRecord((cudaEvent_t)ev, (cudaStream_t)s), "cudaEventRecord"); return QGT_OK; }
+int qgt_dev_event_elapsed(void* a, void* b, float* ms)
+{
+    CK(cudaEventSynchronize((cudaEvent_t)b), "cudaEventSynchronize");
+    CK(cudaEventElapsedTime(ms, (cudaEvent_t)a, (cudaEvent_t)b), "cudaEventElapsedTime");
+    return QGT_OK;
+}
+}
+
+// ---------------------------------------------------------------------------
+// complex64 gate coefficients with exact rotation angles.
+// Every per-vector scale a gate applies is harmless (each vector of a step
+// carries the product of all gates' scales and Q = B/s - v v^H / s^2 is
+// invariant under it); only the rotation ANGLE of a rounded FP32 matrix is
+// an error, and it is coherent across all vectors.  For RX/RY/RZ the warp
+// searches 512 radii r in [1 - 2^-15, 1 + 2^-15] for the FP32 pair
+// (fl(r cos a/2), fl(r sin a/2)) closest to the exact ray: angle error
+// ~1e-10 instead of ~6e-8.  Diagonal fixed gates get equal-modulus entries.
+// One warp per coefficient; 8 floats per coefficient (2x2 complex, row-major).
+// ---------------------------------------------------------------------------
+__global__ void prepare32_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const double* theta, float* coef)
+{
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= ncoef) return;
+    qgt_dev_coef_desc_t g = d[c];
+    float m[8] = {1.f, 0.f, 0.f, 0.f, 0.f, 0.f, 1.f, 0.f};
+    if (g.type == QGT_GATE_RX || g.type == QGT_GATE_RY || g.type == QGT_GATE_RZ) {
+        double a = g.param >= 0 ? theta[g.param] : g.angle;
+        double s0, c0;
+        sincos(0.5 * a, &s0, &c0);
+        double best = 1e300;
+        float bc = (float)c0, bs = (float)s0;
+        for (int i = 0; i < 16; i++) {
+            int k = lane + 32 * i - 256;
+            double r = 1.0 + (double)k * 5.9604644775390625e-08;  // 2^-24
+            float cf = (float)(r * c0), sf = (float)(r * s0);
+            double e = fabs((double)sf * c0 - (double)cf * s0);
+            if (e < best) { best = e; bc = cf; bs = sf; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            float oc = __shfl_xor_sync(0xffffffffu, bc, o), os = __shfl_xor_sync(0xffffffffu, bs, o);
+            if (ob < best || (ob == best && oc < bc)) { best = ob; bc = oc; bs = os; }
+        }
+        if (g.type == QGT_GATE_RX) { m[0] = bc; m[1] = 0; m[2] = 0; m[3] = -bs; m[4] = 0; m[5] = -bs; m[6] = bc; m[7] = 0; }
+        else if (g.type == QGT_GATE_RY) { m[0] = bc; m[1] = 0; m[2] = -bs; m[3] = 0; m[4] = bs; m[5] = 0; m[6] = bc; m[7] = 0; }
+        else { m[0] = bc; m[1] = -bs; m[2] = 0; m[3] = 0; m[4] = 0; m[5] = 0; m[6] = bc; m[7] = bs; }
+    } else {
+        const float r = 0.70710678118654752440f;
+        switch (g.type) {
+        case QGT_GATE_X: m[0] = 0; m[2] = 1; m[4] = 1; m[6] = 0; break;
+        case QGT_GATE_Y: m[0] = 0; m[3] = -1; m[5] = 1; m[6] = 0; break;
+        case QGT_GATE_Z: m[6] = -1; break;
+        case QGT_GATE_H: m[0] = r; m[2] = r; m[4] = r; m[6] = -r; break;
+        case QGT_GATE_S: m[6] = 0; m[7] = 1; break;
+        case QGT_GATE_T: m[0] = (float)sqrt(2.0 * (double)r * (double)r); m[6] = r; m[7] = r; break;
+        default: break;
+        }
+    }
+    if (lane < 8) coef[8 * c + lane] = m[lane];
+}
+
+extern "C" int qgt_dev_prepare32(const qgt_dev_coef_desc_t* d, int32_t ncoef, const double* theta, float* coef, void* s)
+{
+    if (ncoef <= 0) return QGT_OK;
+    prepare32_kernel<<<(ncoef + 7) / 8, 256, 0, (cudaStream_t)s>>>(d, ncoef, theta, coef);
+    return qgt_dev_last_error();
+}

@@ -7,21 +7,25 @@
 // complex64 amplitude of row r is written, in units of a per-row power of two
 // u_r (max_k |x_rk| < M u_r, M = 2^mbits), as
 //     x = u_r (D + l),  D = rint(x / u_r) in [-M, M],  |l| <= 1/2,
-// with D exact in FP16 and l rounded to FP16.  The D*D' products are
+// with D exact in FP16 and l = l1 + l2 carried by two FP16 values (a single
+// FP16 residual leaves ~1e-6 relative error in Q on real derivative states,
+// where the representation errors of rows with equal magnitudes coincide).  The D*D' products are
 // integers and every partial sum of them over a CTA's K range is at most
 // 2^23 (Cauchy-Schwarz; M is chosen per plan from the K range, M = 32 for
 // 4096 amplitudes, up to 1024 for short ranges), so their FP32 tensor
-// accumulation is EXACT.  The D*l', l*D', l*l' terms (a few percent of the
-// total) accumulate in a second TMEM accumulator; their rounding is
-// ~1e-8 relative to the sum.
+// accumulation is EXACT.  The D*l1', l1*D', l1*l1', D*l2', l2*D' terms (a few
+// percent of the total) accumulate in a second TMEM accumulator; their
+// rounding is ~1e-8 relative to the sum.
 //
 // Data path per CTA (tile pair mb <= nb, K range of <= 4096 amplitudes):
 //   TMA: 128 rows x 16 amplitudes of complex64 per row block -> raw smem
-//   4 converter warps: raw -> 4 FP16 planes {Re D, Re l, Im D, Im l}
-//                      in the SWIZZLE_32B K-major UMMA layout
-//   1 thread: 16 tcgen05.mma (M = N = 128, K = 16) per k-step into
+//   8 converter warps: raw -> 6 FP16 planes {Re D, Re l1, Re l2, Im D, Im l1,
+//                      Im l2} in the SWIZZLE_32B K-major UMMA layout
+//   1 thread: 24 tcgen05.mma (M = N = 128, K = 16) per k-step into
 //             TMEM [D*D Re | D*D Im | rest Re | rest Im] (512 columns)
 //   epilogue (the converter warps): TMEM -> FP32 (hh + rest) -> partials
+// The raw ring (3 stages) and the plane ring (2 stages) are decoupled, so a
+// raw buffer is refilled as soon as it has been converted.
 // A second kernel sums the partials in FP64 and applies u_i u_j.
 //
 // Every mbarrier wait is bounded (globaltimer); on expiry the CTA records an
@@ -35,12 +39,14 @@
 
 #include "../qgt_internal.h"
 
-#define DG_STAGES 3
-#define DG_BK 16                                    // amplitudes per stage (one MMA k-step)
+#define DG_BK 16                                    // amplitudes per k-step (one MMA K)
 #define DG_RAW_BYTES (128 * DG_BK * 8)              // 16 KiB: 128 rows x 16 complex64
 #define DG_PLANE_BYTES (128 * DG_BK * 2)            // 4 KiB: 128 rows x 16 fp16
-#define DG_STAGE_BYTES (2 * DG_RAW_BYTES + 8 * DG_PLANE_BYTES)  // 64 KiB
-#define DG_SMEM_BYTES (DG_STAGES * DG_STAGE_BYTES + 1024)
+#define DG_RAW_STAGES 3                             // raw ring: 3 x 2 blocks x 16 KiB
+#define DG_PL_STAGES 2                              // plane ring: 2 x 2 blocks x 6 planes x 4 KiB
+#define DG_CONV_WARPS 8
+#define DG_THREADS (64 + 32 * DG_CONV_WARPS)
+#define DG_SMEM_BYTES (DG_RAW_STAGES * 2 * DG_RAW_BYTES + DG_PL_STAGES * 12 * DG_PLANE_BYTES + 1024)
 #define DG_KMAX 4096                                // amplitudes per CTA (exactness bound)
 #define DG_TIMEOUT_NS 4000000000ull
 #define DG_ERR_TIMEOUT (-13)
@@ -173,28 +179,34 @@ static __device__ __forceinline__ int unit_exp(uint32_t bits, int mbits)
     return e - mbits;
 }
 
-// (A plane, B plane, accumulator, negate A): accumulators 0 = D*D Re, 1 = D*D Im, 2 = rest Re, 3 = rest Im
-__constant__ int8_t dg_terms[16][4] = {
-    {0, 0, 0, 0}, {2, 2, 0, 0}, {0, 2, 1, 0}, {2, 0, 1, 1},
-    {0, 1, 2, 0}, {1, 0, 2, 0}, {1, 1, 2, 0}, {2, 3, 2, 0}, {3, 2, 2, 0}, {3, 3, 2, 0},
-    {0, 3, 3, 0}, {1, 2, 3, 0}, {1, 3, 3, 0}, {2, 1, 3, 1}, {3, 0, 3, 1}, {3, 1, 3, 1}};
+// 24 terms per k-step: (A plane, B plane, accumulator, negate A).  Planes per
+// row block: 0 Re D, 1 Re l1, 2 Re l2, 3 Im D, 4 Im l1, 5 Im l2.  Accumulator
+// 0 / 1 = exact D*D Re / Im, 2 / 3 = the residual terms Re / Im.
+__constant__ int8_t dg_terms[24][4] = {
+    {0, 0, 0, 0}, {3, 3, 0, 0}, {0, 3, 1, 0}, {3, 0, 1, 1},
+    {0, 1, 2, 0}, {1, 0, 2, 0}, {1, 1, 2, 0}, {0, 2, 2, 0}, {2, 0, 2, 0},
+    {3, 4, 2, 0}, {4, 3, 2, 0}, {4, 4, 2, 0}, {3, 5, 2, 0}, {5, 3, 2, 0},
+    {0, 4, 3, 0}, {1, 3, 3, 0}, {1, 4, 3, 0}, {0, 5, 3, 0}, {2, 3, 3, 0},
+    {3, 1, 3, 1}, {4, 0, 3, 1}, {4, 1, 3, 1}, {3, 2, 3, 1}, {5, 0, 3, 1}};
 
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(DG_THREADS, 1)
     dg_gram_kernel(const __grid_constant__ CUtensorMap tmap, int nbk, int64_t N, int64_t kchunk,
                    const uint32_t* __restrict__ rowmax, int rows, int mbits, float* __restrict__ part,
                    int* __restrict__ err)
 {
     extern __shared__ uint8_t dg_smem[];
-    __shared__ __align__(8) uint64_t full_bar[DG_STAGES];
-    __shared__ __align__(8) uint64_t ready_bar[DG_STAGES];
-    __shared__ __align__(8) uint64_t empty_bar[DG_STAGES];
+    __shared__ __align__(8) uint64_t raw_full[DG_RAW_STAGES];
+    __shared__ __align__(8) uint64_t raw_empty[DG_RAW_STAGES];
+    __shared__ __align__(8) uint64_t pl_full[DG_PL_STAGES];
+    __shared__ __align__(8) uint64_t pl_empty[DG_PL_STAGES];
     __shared__ __align__(8) uint64_t done_bar;
     __shared__ uint32_t tmem_sh;
     __shared__ volatile int abort_sh;
     __shared__ float inv_u[2][128];
 
     uint8_t* sb = (uint8_t*)(((uintptr_t)dg_smem + 1023) & ~(uintptr_t)1023);
-    const uint32_t s0 = smem_u32(sb);
+    uint8_t* raw_base = sb;                                        // DG_RAW_STAGES x 2 blocks x 16 KiB
+    uint8_t* pl_base = sb + DG_RAW_STAGES * 2 * DG_RAW_BYTES;       // DG_PL_STAGES x 2 blocks x 6 planes x 4 KiB
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int mb, nbo;
     pair_of(blockIdx.x, nbk, &mb, &nbo);
@@ -215,10 +227,13 @@ __global__ void __launch_bounds__(192, 1)
         }
     }
     if (threadIdx.x == 0) {
-        for (int s = 0; s < DG_STAGES; s++) {
-            bar_init(smem_u32(&full_bar[s]), 1);
-            bar_init(smem_u32(&ready_bar[s]), 4);
-            bar_init(smem_u32(&empty_bar[s]), 1);
+        for (int s = 0; s < DG_RAW_STAGES; s++) {
+            bar_init(smem_u32(&raw_full[s]), 1);
+            bar_init(smem_u32(&raw_empty[s]), DG_CONV_WARPS);
+        }
+        for (int s = 0; s < DG_PL_STAGES; s++) {
+            bar_init(smem_u32(&pl_full[s]), DG_CONV_WARPS);
+            bar_init(smem_u32(&pl_empty[s]), 1);
         }
         bar_init(smem_u32(&done_bar), 1);
         abort_sh = 0;
@@ -239,106 +254,117 @@ __global__ void __launch_bounds__(192, 1)
         const uint32_t bytes = (uint32_t)nblk * DG_RAW_BYTES;
         int issued = 0;
         for (int kt = 0; kt < nk; kt++) {
-            const int s = kt % DG_STAGES;
-            if (kt >= DG_STAGES && !bar_wait(smem_u32(&empty_bar[s]), ((kt / DG_STAGES) & 1) ^ 1, deadline)) {
+            const int s = kt % DG_RAW_STAGES;
+            if (kt >= DG_RAW_STAGES &&
+                !bar_wait(smem_u32(&raw_empty[s]), ((kt / DG_RAW_STAGES) & 1) ^ 1, deadline)) {
                 atomicExch(err, DG_ERR_TIMEOUT);
                 abort_sh = 1;
                 break;
             }
             if (abort_sh) break;
-            const uint32_t st = s0 + s * DG_STAGE_BYTES;
-            const uint32_t fb = smem_u32(&full_bar[s]);
+            const uint32_t st = smem_u32(raw_base + s * 2 * DG_RAW_BYTES);
+            const uint32_t fb = smem_u32(&raw_full[s]);
             bar_expect_tx(fb, bytes);
             const int x = (int)(2 * (k0 + (int64_t)kt * DG_BK));  // float index
             tma_2d(st, &tmap, x, mb * 128, fb);
             if (!diag) tma_2d(st + DG_RAW_BYTES, &tmap, x, nbo * 128, fb);
             issued = kt + 1;
         }
-        for (int u = issued - DG_STAGES; u < issued; u++)
-            if (u >= 0) (void)bar_wait(smem_u32(&full_bar[u % DG_STAGES]), (u / DG_STAGES) & 1, deadline + DG_TIMEOUT_NS);
+        for (int u = issued - DG_RAW_STAGES; u < issued; u++)
+            if (u >= 0)
+                (void)bar_wait(smem_u32(&raw_full[u % DG_RAW_STAGES]), (u / DG_RAW_STAGES) & 1, deadline + DG_TIMEOUT_NS);
     } else if (warp == 1 && lane == 0) {
         // ---------- MMA issuer ----------
         const uint32_t idp = idesc_f16(0), idn = idesc_f16(1);
         for (int kt = 0; kt < nk; kt++) {
-            const int s = kt % DG_STAGES;
-            if (!bar_wait(smem_u32(&ready_bar[s]), (kt / DG_STAGES) & 1, deadline)) {
+            const int s = kt % DG_PL_STAGES;
+            if (!bar_wait(smem_u32(&pl_full[s]), (kt / DG_PL_STAGES) & 1, deadline)) {
                 atomicExch(err, DG_ERR_TIMEOUT);
                 abort_sh = 1;
                 break;
             }
             if (abort_sh) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t pa = s0 + s * DG_STAGE_BYTES + 2 * DG_RAW_BYTES;
-            const uint32_t pb = diag ? pa : pa + 4 * DG_PLANE_BYTES;
+            const uint32_t pa = smem_u32(pl_base + s * 2 * 6 * DG_PLANE_BYTES);
+            const uint32_t pb = diag ? pa : pa + 6 * DG_PLANE_BYTES;
 #pragma unroll
-            for (int t = 0; t < 16; t++) {
+            for (int t = 0; t < 24; t++) {
                 const int a = dg_terms[t][0], b = dg_terms[t][1], acc = dg_terms[t][2], ng = dg_terms[t][3];
-                const uint32_t first = (kt == 0) && (t == 0 || t == 2 || t == 4 || t == 10);
+                const uint32_t first = (kt == 0) && (t == 0 || t == 2 || t == 4 || t == 14);
                 umma(tmem + (uint32_t)acc * 128u, desc_sw32(pa + a * DG_PLANE_BYTES), desc_sw32(pb + b * DG_PLANE_BYTES),
                      ng ? idn : idp, first ? 0u : 1u);
             }
-            umma_commit(smem_u32(&empty_bar[s]));
+            umma_commit(smem_u32(&pl_empty[s]));
         }
         umma_commit(smem_u32(&done_bar));
         mma_done_commit = true;
     } else if (warp >= 2) {
-        // ---------- converters: raw complex64 -> {Re D, Re l, Im D, Im l} ----------
-        const int cw = warp - 2;  // rows r = cw, cw + 4, ...
+        // ---------- converters: complex64 -> {Re D, Re l1, Re l2, Im D, Im l1, Im l2} ----------
+        const int cw = warp - 2;  // rows r = cw, cw + DG_CONV_WARPS, ...
+        const int comp = lane & 1, k = lane >> 1;
         for (int kt = 0; kt < nk; kt++) {
-            const int s = kt % DG_STAGES;
-            if (!bar_wait(smem_u32(&full_bar[s]), (kt / DG_STAGES) & 1, deadline)) {
+            const int rs = kt % DG_RAW_STAGES, ps = kt % DG_PL_STAGES;
+            bool ok = bar_wait(smem_u32(&raw_full[rs]), (kt / DG_RAW_STAGES) & 1, deadline);
+            if (ok && kt >= DG_PL_STAGES) ok = bar_wait(smem_u32(&pl_empty[ps]), ((kt / DG_PL_STAGES) & 1) ^ 1, deadline);
+            if (!ok) {
                 atomicExch(err, DG_ERR_TIMEOUT);
                 abort_sh = 1;
             }
             if (abort_sh) break;
-            uint8_t* st = sb + s * DG_STAGE_BYTES;
-            const int comp = lane & 1, k = lane >> 1;
+            const uint8_t* rawst = raw_base + rs * 2 * DG_RAW_BYTES;
+            uint8_t* plst = pl_base + ps * 2 * 6 * DG_PLANE_BYTES;
             for (int b = 0; b < nblk; b++) {
-                const float* raw = reinterpret_cast<const float*>(st + b * DG_RAW_BYTES);
-                uint8_t* planes = st + 2 * DG_RAW_BYTES + b * 4 * DG_PLANE_BYTES;
-                for (int r = cw; r < 128; r += 4) {
+                const float* raw = reinterpret_cast<const float*>(rawst + b * DG_RAW_BYTES);
+                uint8_t* planes = plst + b * 6 * DG_PLANE_BYTES;
+                uint8_t* pD = planes + (comp ? 3 : 0) * DG_PLANE_BYTES;
+#pragma unroll 4
+                for (int r = cw; r < 128; r += DG_CONV_WARPS) {
                     const float x = raw[r * 32 + lane] * inv_u[b][r];
                     const float d = rintf(x);
-                    const __half hd = __float2half_rn(d);
-                    const __half hl = __float2half_rn(x - d);
+                    const float l = x - d;
+                    const __half h1 = __float2half_rn(l);
+                    const __half h2 = __float2half_rn(l - __half2float(h1));
                     // SWIZZLE_32B: 16-byte chunk (k / 8) xor bit 2 of the row
                     const int off = r * 32 + ((((k >> 3) ^ (r >> 2)) & 1) << 4) + (k & 7) * 2;
-                    *reinterpret_cast<__half*>(planes + (comp ? 2 : 0) * DG_PLANE_BYTES + off) = hd;
-                    *reinterpret_cast<__half*>(planes + (comp ? 3 : 1) * DG_PLANE_BYTES + off) = hl;
+                    *reinterpret_cast<__half*>(pD + off) = __float2half_rn(d);
+                    *reinterpret_cast<__half*>(pD + DG_PLANE_BYTES + off) = h1;
+                    *reinterpret_cast<__half*>(pD + 2 * DG_PLANE_BYTES + off) = h2;
                 }
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
-            if (lane == 0) bar_arrive(smem_u32(&ready_bar[s]));
+            if (lane == 0) {
+                bar_arrive(smem_u32(&raw_empty[rs]));
+                bar_arrive(smem_u32(&pl_full[ps]));
+            }
         }
-        // ---------- epilogue ----------
+        // ---------- epilogue: warps 2..9; lane quadrant = warp & 3, column half = (warp - 2) / 4 ----------
         const bool ok = nk > 0 && !abort_sh && bar_wait(smem_u32(&done_bar), 0, deadline);
         float* out = part + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * (2 * 128 * 128);
-        const int quad = warp & 3;
+        const int quad = warp & 3, half = (warp - 2) >> 2;
         const int row = quad * 32 + lane;
         if (ok) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            float hh[32], rs[32];
+            float hh[32], rsd[32];
             const uint32_t lanebase = tmem + ((uint32_t)(quad * 32) << 16);
             for (int ri = 0; ri < 2; ri++) {
-                for (int c = 0; c < 4; c++) {
+                for (int c = 2 * half; c < 2 * half + 2; c++) {
                     tmem_ld32(lanebase + ri * 128 + c * 32, hh);
-                    tmem_ld32(lanebase + 256 + ri * 128 + c * 32, rs);
+                    tmem_ld32(lanebase + 256 + ri * 128 + c * 32, rsd);
                     if (diag && ri == 0 && c == (row >> 5) && hh[row & 31] > 8388608.0f) atomicExch(err, DG_ERR_INEXACT);
                     float4* o = reinterpret_cast<float4*>(out + ri * 128 * 128 + row * 128 + c * 32);
 #pragma unroll
                     for (int j = 0; j < 8; j++)
-                        o[j] = make_float4(hh[4 * j] + rs[4 * j], hh[4 * j + 1] + rs[4 * j + 1], hh[4 * j + 2] + rs[4 * j + 2],
-                                           hh[4 * j + 3] + rs[4 * j + 3]);
+                        o[j] = make_float4(hh[4 * j] + rsd[4 * j], hh[4 * j + 1] + rsd[4 * j + 1],
+                                           hh[4 * j + 2] + rsd[4 * j + 2], hh[4 * j + 3] + rsd[4 * j + 3]);
                 }
             }
         } else {
-            if (!(nk > 0) || abort_sh) {
-                if (abort_sh) atomicExch(err, DG_ERR_TIMEOUT);
-            } else {
-                atomicExch(err, DG_ERR_TIMEOUT);
+            atomicExch(err, DG_ERR_TIMEOUT);
+            for (int c = 64 * half; c < 64 * half + 64; c++) {
+                out[row * 128 + c] = 0.f;
+                out[128 * 128 + row * 128 + c] = 0.f;
             }
-            for (int c = 0; c < 128; c++) { out[row * 128 + c] = 0.f; out[128 * 128 + row * 128 + c] = 0.f; }
         }
     }
     if (warp == 1 && lane == 0 && mma_done_commit) (void)bar_wait(smem_u32(&done_bar), 0, deadline + DG_TIMEOUT_NS);
@@ -446,7 +472,7 @@ extern "C" int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, co
 extern "C" int qgt_dev_dg_gram_run(qgt_dg_gram_t* g, double* HG, void* stream)
 {
     cudaStream_t s = (cudaStream_t)stream;
-    dg_gram_kernel<<<dim3(g->ntp, g->nsplit), 192, DG_SMEM_BYTES, s>>>(g->tmap, g->nbk, g->N, g->kchunk, g->rowmax,
+    dg_gram_kernel<<<dim3(g->ntp, g->nsplit), DG_THREADS, DG_SMEM_BYTES, s>>>(g->tmap, g->nbk, g->N, g->kchunk, g->rowmax,
                                                                        g->rows, g->mbits, g->part, g->err);
     int rc = qgt_dev_last_error();
     if (rc) return rc;

@@ -51,6 +51,52 @@ __device__ __forceinline__ int qbit(int l, int lb, int q, uint64_t base)
     return lb >= 0 ? (l >> lb) & 1 : (int)((base >> q) & 1);
 }
 
+// Gate coefficients are FP64 on the device.  In the complex64 path each one
+// is applied as a float-float pair hi + lo (hi = fl(m), lo = fl(m - hi)), so
+// the matrix the kernel applies is the FP64 matrix to ~2^-48: rounding the
+// matrices to FP32 would instead shift every rotation angle by ~6e-8 rad, an
+// error that is coherent across all vectors and shows up directly in Q.
+template <typename R>
+struct coefpair {
+    R h, l;
+};
+
+template <typename R>
+__device__ __forceinline__ coefpair<R> split_coef(double m)
+{
+    coefpair<R> c;
+    c.h = (R)m;
+    c.l = (R)(m - (double)c.h);
+    return c;
+}
+
+// (a + i b) x + (c + i d) y with float-float coefficients (R = float) or plain FP64
+template <typename T, typename R>
+__device__ __forceinline__ T cfma2p(const coefpair<R>* m, T x, T y)
+{
+    T o;
+    o.x = m[0].h * x.x - m[1].h * x.y + m[2].h * y.x - m[3].h * y.y;
+    o.y = m[0].h * x.y + m[1].h * x.x + m[2].h * y.y + m[3].h * y.x;
+    if (sizeof(R) == 4) {
+        o.x += m[0].l * x.x - m[1].l * x.y + m[2].l * y.x - m[3].l * y.y;
+        o.y += m[0].l * x.y + m[1].l * x.x + m[2].l * y.y + m[3].l * y.x;
+    }
+    return o;
+}
+
+template <typename T, typename R>
+__device__ __forceinline__ T cscalep(T x, const coefpair<R>* p)
+{
+    T o;
+    o.x = p[0].h * x.x - p[1].h * x.y;
+    o.y = p[0].h * x.y + p[1].h * x.x;
+    if (sizeof(R) == 4) {
+        o.x += p[0].l * x.x - p[1].l * x.y;
+        o.y += p[0].l * x.y + p[1].l * x.x;
+    }
+    return o;
+}
+
 template <typename R>
 __device__ void apply_op(const qgt_dev_op_t& op, const double* __restrict__ coef, typename vec2t<R>::T* tile, int TS,
                          uint64_t base)
@@ -59,29 +105,30 @@ __device__ void apply_op(const qgt_dev_op_t& op, const double* __restrict__ coef
     const int tid = threadIdx.x, nt = blockDim.x;
     if (op.kind == QOP_1Q) {
         const double* m = coef + 8 * op.coef;
-        R m00r = (R)__ldg(m + 0), m00i = (R)__ldg(m + 1), m01r = (R)__ldg(m + 2), m01i = (R)__ldg(m + 3);
-        R m10r = (R)__ldg(m + 4), m10i = (R)__ldg(m + 5), m11r = (R)__ldg(m + 6), m11i = (R)__ldg(m + 7);
+        coefpair<R> r0[4], r1[4];
+        for (int i = 0; i < 4; i++) { r0[i] = split_coef<R>(__ldg(m + i)); r1[i] = split_coef<R>(__ldg(m + 4 + i)); }
         const int b = op.lb;
         for (int p = tid; p < TS / 2; p += nt) {
             int i0 = ((p >> b) << (b + 1)) | (p & ((1 << b) - 1));
             int i1 = i0 | (1 << b);
             T a0 = tile[i0], a1 = tile[i1];
-            tile[i0] = cfma2<T, R>(m00r, m00i, a0, m01r, m01i, a1);
-            tile[i1] = cfma2<T, R>(m10r, m10i, a0, m11r, m11i, a1);
+            tile[i0] = cfma2p<T, R>(r0, a0, a1);
+            tile[i1] = cfma2p<T, R>(r1, a0, a1);
         }
     } else if (op.kind == QOP_PHASE) {
         const double* m = coef + 8 * op.coef;
-        R p0r = (R)__ldg(m + 0), p0i = (R)__ldg(m + 1), p1r = (R)__ldg(m + 6), p1i = (R)__ldg(m + 7);
+        coefpair<R> p0[2] = {split_coef<R>(__ldg(m + 0)), split_coef<R>(__ldg(m + 1))};
+        coefpair<R> p1[2] = {split_coef<R>(__ldg(m + 6)), split_coef<R>(__ldg(m + 7))};
         if (op.lb >= 0) {
             for (int l = tid; l < TS; l += nt) {
                 int bit = (l >> op.lb) & 1;
-                tile[l] = bit ? cscale<T, R>(tile[l], p1r, p1i) : cscale<T, R>(tile[l], p0r, p0i);
+                tile[l] = cscalep<T, R>(tile[l], bit ? p1 : p0);
             }
         } else {
             int bit = (int)((base >> op.q) & 1);
-            R pr = bit ? p1r : p0r, pi = bit ? p1i : p0i;
-            if (!(pr == (R)1 && pi == (R)0))
-                for (int l = tid; l < TS; l += nt) tile[l] = cscale<T, R>(tile[l], pr, pi);
+            const coefpair<R>* pp = bit ? p1 : p0;
+            if (!(pp[0].h == (R)1 && pp[0].l == (R)0 && pp[1].h == (R)0 && pp[1].l == (R)0))
+                for (int l = tid; l < TS; l += nt) tile[l] = cscalep<T, R>(tile[l], pp);
         }
     } else if (op.kind == QOP_CZ) {
         if (op.lb < 0 && op.lb2 < 0) {

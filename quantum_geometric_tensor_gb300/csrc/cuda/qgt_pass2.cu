@@ -1,0 +1,402 @@
+// qgt_pass2.cu -- register-resident tile passes (the gate-application hot path).
+//
+// A full tile (2^13 complex64 or 2^12 complex128 amplitudes) is held in the
+// registers of one 256-thread CTA: each thread owns NR = 2^RB amplitudes
+// (RB = 5 for complex64, 4 for complex128).  The tile's local bits play three
+// roles:
+//   lane bits  0..4   (always; physical qubits 0..4, so every global access of
+//                      a warp is 32 consecutive amplitudes)
+//   reg bits   RB bits chosen per segment (index into the thread's registers)
+//   warp bits  the remaining 3 bits (the warp index)
+// A pass is compiled on the host into a program of segments.  Within a
+// segment every non-diagonal gate acts on a reg bit (in-register butterfly,
+// statically indexed) or a lane bit (warp shuffle); diagonal gates act on any
+// bit.  Between segments the tile is re-laid out through shared memory
+// (conflict-free: lanes always index consecutive amplitudes).
+//
+// Gate coefficients come from the complex64 table with exact rotation angles
+// (prepare32_kernel).  Derivative slots branch from psi by an exact (-i/2) G
+// inserted after their gate; later passes transport them in place.
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "../qgt_internal.h"
+
+template <typename R> struct v2of;
+template <> struct v2of<float> { typedef float2 T; };
+template <> struct v2of<double> { typedef double2 T; };
+
+// role-encoded bit: 0..4 lane bit, 8 + i reg bit i, 16 + w warp bit w, 32 outside the tile (physical qubit q)
+#define RL_REG 8
+#define RL_WARP 16
+#define RL_OUT 32
+
+template <typename T, typename R>
+struct Cf {
+    R m[8];
+};
+
+template <typename R>
+__device__ __forceinline__ void load_coef(const void* tab, int idx, R* m)
+{
+    const R* t = reinterpret_cast<const R*>(tab) + 8 * idx;
+#pragma unroll
+    for (int i = 0; i < 8; i++) m[i] = __ldg(t + i);
+}
+
+template <typename T, typename R>
+__device__ __forceinline__ T cm(R ar, R ai, T x)
+{
+    T o;
+    o.x = ar * x.x - ai * x.y;
+    o.y = ar * x.y + ai * x.x;
+    return o;
+}
+
+template <typename T, typename R>
+__device__ __forceinline__ T cmad2(const R* m, T x, T y)  // (m0 + i m1) x + (m2 + i m3) y
+{
+    T o;
+    o.x = m[0] * x.x - m[1] * x.y + m[2] * y.x - m[3] * y.y;
+    o.y = m[0] * x.y + m[1] * x.x + m[2] * y.y + m[3] * y.x;
+    return o;
+}
+
+template <typename T, typename R>
+__device__ __forceinline__ T rmad2(R a, T x, R b, T y)  // real a x + b y
+{
+    T o;
+    o.x = a * x.x + b * y.x;
+    o.y = a * x.y + b * y.y;
+    return o;
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_x(T v, int mask);
+template <>
+__device__ __forceinline__ float2 shfl_x<float2>(float2 v, int mask)
+{
+    return make_float2(__shfl_xor_sync(0xffffffffu, v.x, mask), __shfl_xor_sync(0xffffffffu, v.y, mask));
+}
+template <>
+__device__ __forceinline__ double2 shfl_x<double2>(double2 v, int mask)
+{
+    return make_double2(__shfl_xor_sync(0xffffffffu, v.x, mask), __shfl_xor_sync(0xffffffffu, v.y, mask));
+}
+
+// ---- butterflies on a register bit ----
+template <int RI, int NR, typename T, typename R>
+__device__ __forceinline__ void u_reg(T* v, const R* m, bool real)
+{
+#pragma unroll
+    for (int j = 0; j < NR; j++) {
+        if (j & (1 << RI)) continue;
+        const int k = j | (1 << RI);
+        T a0 = v[j], a1 = v[k];
+        if (real) {
+            v[j] = rmad2<T, R>(m[0], a0, m[2], a1);
+            v[k] = rmad2<T, R>(m[4], a0, m[6], a1);
+        } else {
+            v[j] = cmad2<T, R>(m, a0, a1);
+            v[k] = cmad2<T, R>(m + 4, a0, a1);
+        }
+    }
+}
+
+template <int RI, int NR, typename T, typename R>
+__device__ __forceinline__ void phase_reg(T* v, const R* m)
+{
+#pragma unroll
+    for (int j = 0; j < NR; j++) v[j] = (j & (1 << RI)) ? cm<T, R>(m[6], m[7], v[j]) : cm<T, R>(m[0], m[1], v[j]);
+}
+
+// CNOT with reg target RI, control given by a per-register predicate mask (bit j of cmask)
+template <int RI, int NR, typename T>
+__device__ __forceinline__ void cnot_reg(T* v, uint32_t cmask)
+{
+#pragma unroll
+    for (int j = 0; j < NR; j++) {
+        if (j & (1 << RI)) continue;
+        const int k = j | (1 << RI);
+        if ((cmask >> j) & 1u) { T t = v[j]; v[j] = v[k]; v[k] = t; }
+    }
+}
+
+// (-i/2) X or (-i/2) Y on reg bit RI (exact)
+template <int RI, int NR, typename T, typename R>
+__device__ __forceinline__ void gen_reg(T* v, int gen)
+{
+    const R h = (R)0.5;
+#pragma unroll
+    for (int j = 0; j < NR; j++) {
+        if (j & (1 << RI)) continue;
+        const int k = j | (1 << RI);
+        T a0 = v[j], a1 = v[k], o0, o1;
+        if (gen == QGEN_X) { o0.x = h * a1.y; o0.y = -h * a1.x; o1.x = h * a0.y; o1.y = -h * a0.x; }
+        else { o0.x = -h * a1.x; o0.y = -h * a1.y; o1.x = h * a0.x; o1.y = h * a0.y; }
+        v[j] = o0;
+        v[k] = o1;
+    }
+}
+
+#define RB_SWITCH(ri, CALL)                         \
+    switch (ri) {                                   \
+    case 0: CALL(0); break;                         \
+    case 1: CALL(1); break;                         \
+    case 2: CALL(2); break;                         \
+    case 3: CALL(3); break;                         \
+    default: if (RB > 4) { CALL(4 % RB); } break;   \
+    }
+
+// bit value of a non-register role for this thread
+__device__ __forceinline__ int role_bit(int role, int q, int lane, int warp, uint64_t base)
+{
+    if (role < RL_REG) return (lane >> role) & 1;
+    if (role < RL_OUT) return (warp >> (role - RL_WARP)) & 1;
+    return (int)((base >> q) & 1);
+}
+
+// per-register mask of "bit is 1" for any role: reg -> pattern over j; other -> all or nothing
+template <int NR>
+__device__ __forceinline__ uint32_t role_mask(int role, int q, int lane, int warp, uint64_t base)
+{
+    const uint32_t all = (NR == 32) ? 0xffffffffu : ((1u << NR) - 1u);
+    if (role >= RL_REG && role < RL_WARP) {
+        const int ri = role - RL_REG;
+        uint32_t m = 0;
+#pragma unroll
+        for (int j = 0; j < NR; j++) m |= (uint32_t)((j >> ri) & 1) << j;
+        return m;
+    }
+    return role_bit(role, q, lane, warp, base) ? all : 0u;
+}
+
+template <typename R, int RB>
+__global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_t a)
+{
+    typedef typename v2of<R>::T T;
+    constexpr int NR = 1 << RB;
+    extern __shared__ __align__(16) unsigned char p2_smem[];
+    T* tile = reinterpret_cast<T*>(p2_smem);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // the pass program and each op's coefficients, staged once per CTA
+    qgt_dev_op2_t* sops = reinterpret_cast<qgt_dev_op2_t*>(p2_smem + ((size_t)sizeof(T) << (5 + RB + 3)));
+    R* scoef = reinterpret_cast<R*>(sops + a.nops);
+    {
+        const R* ctab = (sizeof(R) == 4) ? reinterpret_cast<const R*>(a.coef32) : reinterpret_cast<const R*>(a.coef);
+        for (int i = threadIdx.x; i < a.nops; i += blockDim.x) sops[i] = a.ops[i];
+        for (int i = threadIdx.x; i < 8 * a.nops; i += blockDim.x) {
+            const int c = a.ops[i >> 3].coef;
+            scoef[i] = c >= 0 ? ctab[8 * c + (i & 7)] : (R)0;
+        }
+        __syncthreads();
+    }
+    const qgt_dev_entry_t e = a.entries[blockIdx.y];
+    uint64_t base = 0;
+    {
+        uint32_t rest = blockIdx.x;
+        for (int q = 0; q < a.n; q++)
+            if (!((a.tile_mask >> q) & 1)) { base |= (uint64_t)(rest & 1u) << q; rest >>= 1; }
+    }
+    // layout of the current segment: local index contributions of reg bits and of this thread
+    int lreg[RB];
+    uint32_t preg[RB];   // n <= 30: physical indices fit in 32 bits
+    int lthr = 0;
+    uint32_t pthr = 0;
+    auto set_layout = [&](int s) {
+        const int8_t* L = a.segs + 16 * s;
+        lthr = lane;
+        pthr = (uint32_t)base | (uint32_t)lane;  // local bits 0..4 are physical qubits 0..4
+#pragma unroll
+        for (int w = 0; w < 3; w++) {
+            const int lb = L[8 + w];
+            if ((warp >> w) & 1) { lthr |= 1 << lb; pthr |= 1u << a.local_to_phys[lb]; }
+        }
+#pragma unroll
+        for (int i = 0; i < RB; i++) { lreg[i] = 1 << L[i]; preg[i] = 1u << a.local_to_phys[L[i]]; }
+    };
+    auto lidx = [&](int j) {
+        int l = lthr;
+#pragma unroll
+        for (int i = 0; i < RB; i++) if ((j >> i) & 1) l |= lreg[i];
+        return l;
+    };
+    auto pidx = [&](int j) {
+        uint32_t p = pthr;
+#pragma unroll
+        for (int i = 0; i < RB; i++) if ((j >> i) & 1) p |= preg[i];
+        return p;
+    };
+
+    T v[NR];
+    set_layout(sops[0].seg);
+    {
+        const T* src = reinterpret_cast<const T*>(a.V) + (int64_t)e.src_row * a.N;
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            const uint32_t ph = pidx(j);
+            if (e.flags & QENT_SRC_ZERO) { v[j].x = (ph == 0) ? (R)1 : (R)0; v[j].y = (R)0; }
+            else v[j] = src[ph];
+        }
+    }
+    for (int pc = 1; pc < a.nops; pc++) {
+        const qgt_dev_op2_t op = sops[pc];
+        R m[8];
+        if (op.kind == Q2_SEG) {
+            // re-layout through shared memory
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < NR; j++) tile[lidx(j)] = v[j];
+            __syncthreads();
+            set_layout(op.seg);
+#pragma unroll
+            for (int j = 0; j < NR; j++) v[j] = tile[lidx(j)];
+            continue;
+        }
+        if (op.kind == Q2_U || op.kind == Q2_UR) {
+#pragma unroll
+            for (int i = 0; i < 8; i++) m[i] = scoef[8 * pc + i];
+            const bool real = op.kind == Q2_UR;
+            if (op.ra >= RL_REG) {
+                const int ri = op.ra - RL_REG;
+#define U_CALL(I) u_reg<I, NR, T, R>(v, m, real)
+                RB_SWITCH(ri, U_CALL)
+#undef U_CALL
+            } else {
+                const int b = op.ra, hi = (lane >> b) & 1;
+#pragma unroll
+                for (int j = 0; j < NR; j++) {
+                    T w = shfl_x<T>(v[j], 1 << b);
+                    if (real) v[j] = hi ? rmad2<T, R>(m[4], w, m[6], v[j]) : rmad2<T, R>(m[0], v[j], m[2], w);
+                    else v[j] = hi ? cmad2<T, R>(m + 4, w, v[j]) : cmad2<T, R>(m, v[j], w);
+                }
+            }
+        } else if (op.kind == Q2_PHASE) {
+#pragma unroll
+            for (int i = 0; i < 8; i++) m[i] = scoef[8 * pc + i];
+            if (op.ra >= RL_REG && op.ra < RL_WARP) {
+                const int ri = op.ra - RL_REG;
+#define P_CALL(I) phase_reg<I, NR, T, R>(v, m)
+                RB_SWITCH(ri, P_CALL)
+#undef P_CALL
+            } else {
+                const int bit = role_bit(op.ra, op.q, lane, warp, base);
+                const R pr = bit ? m[6] : m[0], pi = bit ? m[7] : m[1];
+                if (!(pr == (R)1 && pi == (R)0)) {
+#pragma unroll
+                    for (int j = 0; j < NR; j++) v[j] = cm<T, R>(pr, pi, v[j]);
+                }
+            }
+        } else if (op.kind == Q2_CZ) {
+            const uint32_t mk = role_mask<NR>(op.ra, op.q, lane, warp, base) & role_mask<NR>(op.rb, op.q2, lane, warp, base);
+            if (mk) {
+#pragma unroll
+                for (int j = 0; j < NR; j++)
+                    if ((mk >> j) & 1u) { v[j].x = -v[j].x; v[j].y = -v[j].y; }
+            }
+        } else if (op.kind == Q2_CNOT) {
+            const uint32_t cmask = role_mask<NR>(op.rb, op.q2, lane, warp, base);
+            if (op.ra >= RL_REG) {
+                const int ri = op.ra - RL_REG;
+#define C_CALL(I) cnot_reg<I, NR, T>(v, cmask)
+                RB_SWITCH(ri, C_CALL)
+#undef C_CALL
+            } else {
+                const int b = op.ra;
+#pragma unroll
+                for (int j = 0; j < NR; j++) {
+                    T w = shfl_x<T>(v[j], 1 << b);
+                    if ((cmask >> j) & 1u) v[j] = w;
+                }
+            }
+        }
+        if (pc == e.spawn_op) {
+            if (op.gen == QGEN_Z) {
+                const uint32_t mk = role_mask<NR>(op.ra, op.q, lane, warp, base);
+                const R h = (R)0.5;
+#pragma unroll
+                for (int j = 0; j < NR; j++) {
+                    const R sg = ((mk >> j) & 1u) ? h : -h;  // (-i/2) Z: multiply by i * sg
+                    T o;
+                    o.x = -sg * v[j].y;
+                    o.y = sg * v[j].x;
+                    v[j] = o;
+                }
+            } else if (op.ra >= RL_REG) {
+                const int ri = op.ra - RL_REG;
+                const int gen = op.gen;
+#define G_CALL(I) gen_reg<I, NR, T, R>(v, gen)
+                RB_SWITCH(ri, G_CALL)
+#undef G_CALL
+            } else {
+                const int b = op.ra, hi = (lane >> b) & 1;
+                const R h = (R)0.5;
+#pragma unroll
+                for (int j = 0; j < NR; j++) {
+                    T w = shfl_x<T>(v[j], 1 << b), o;
+                    if (op.gen == QGEN_X) { o.x = h * w.y; o.y = -h * w.x; }   // (-i/2) X: both rows take the partner
+                    else if (hi) { o.x = h * w.x; o.y = h * w.y; }              // (-i/2) Y: row 1 = +a0/2
+                    else { o.x = -h * w.x; o.y = -h * w.y; }                   //           row 0 = -a1/2
+                    v[j] = o;
+                }
+            }
+        }
+    }
+    // store
+    T* dst = reinterpret_cast<T*>(a.V) + (int64_t)e.dst_row * a.N;
+    float vmax = 0.f;
+#pragma unroll
+    for (int j = 0; j < NR; j++) {
+        const uint32_t ph = pidx(j);
+        if (e.flags & QENT_STORE_V) dst[ph] = v[j];
+        if (e.flags & QENT_ROWMAX) vmax = fmaxf(vmax, sqrtf((float)(v[j].x * v[j].x + v[j].y * v[j].y)));
+        if (e.flags & QENT_STORE_SPLIT) {
+            float xr = (float)v[j].x * a.split_scale, xi = (float)v[j].y * a.split_scale;
+            int64_t at = (int64_t)e.split_row * a.split_ld + (int64_t)ph;
+            const int64_t ps = a.split_plane_stride;
+            __nv_bfloat16* s = reinterpret_cast<__nv_bfloat16*>(a.split);
+            __nv_bfloat16 rh = __float2bfloat16_rn(xr), ih = __float2bfloat16_rn(xi);
+            s[at] = rh;
+            s[ps + at] = __float2bfloat16_rn(xr - __bfloat162float(rh));
+            s[2 * ps + at] = ih;
+            s[3 * ps + at] = __float2bfloat16_rn(xi - __bfloat162float(ih));
+        }
+    }
+    if (e.flags & QENT_ROWMAX) {
+        __shared__ float red[8];
+        for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+        if (lane == 0) red[warp] = vmax;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float mx = 0.f;
+            for (int w = 0; w < 8; w++) mx = fmaxf(mx, red[w]);
+            atomicMax(a.rowmax + e.dst_row, __float_as_uint(mx));
+        }
+    }
+}
+
+extern "C" int qgt_dev_pass2(const qgt_dev_pass2_args_t* a, int fp64, void* stream)
+{
+    if (a->nentries <= 0) return 0;
+    const int tb = fp64 ? QGT_TILE_MAX_F64 : QGT_TILE_MAX_F32;
+    if (a->tile_bits != tb) return qgt_set_error(-1, "pass2: tile of %d bits (needs %d)", a->tile_bits, tb);
+    int64_t ntiles = (int64_t)1 << (a->n - a->tile_bits);
+    if (a->nentries > 65535 || ntiles > 0x7fffffff) return qgt_set_error(-1, "pass2: grid too large");
+    dim3 grid((unsigned)ntiles, (unsigned)a->nentries);
+    size_t smem = ((size_t)1 << (tb + (fp64 ? 4 : 3))) +                               /* 64 KiB tile */
+                  (size_t)a->nops * (sizeof(qgt_dev_op2_t) + 8 * (fp64 ? sizeof(double) : sizeof(float)));
+    if (smem > 112 * 1024) return qgt_set_error(-1, "pass2: program of %d ops too large", a->nops);
+    static int attr[2] = {0, 0};
+    cudaError_t e = cudaSuccess;
+    if (!attr[fp64 ? 1 : 0]) {
+        e = fp64 ? cudaFuncSetAttribute(pass2_kernel<double, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 112 * 1024)
+                 : cudaFuncSetAttribute(pass2_kernel<float, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, 112 * 1024);
+        if (e == cudaSuccess) attr[fp64 ? 1 : 0] = 1;
+    }
+    if (e != cudaSuccess) return qgt_set_error(-6, "pass2: %s", cudaGetErrorString(e));
+    if (fp64) pass2_kernel<double, 4><<<grid, 256, smem, (cudaStream_t)stream>>>(*a);
+    else pass2_kernel<float, 5><<<grid, 256, smem, (cudaStream_t)stream>>>(*a);
+    return qgt_dev_last_error();
+}

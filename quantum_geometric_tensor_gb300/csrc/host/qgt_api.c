@@ -429,6 +429,9 @@ static bool ensure_step(const quantum_geometric_tensor_network_t* q, int want64)
     qgt_plan_t** pp = want64 ? &b->plan64 : &b->plan;
     uint64_t* pv = want64 ? &b->plan64_version : &b->plan_version;
     o.precision = want64 ? QGT_PRECISION_FP64 : (qgt_precision_t)b->precision;
+    /* the integer-digit Gram walks amplitudes 16 at a time: registers below
+       4 qubits (fewer than 16 amplitudes) run the FP64 plan instead */
+    if (o.precision == QGT_PRECISION_MIXED && q->num_qubits < 4) o.precision = QGT_PRECISION_FP64;
     if (!*pp || *pv != b->version + 1) {
         qgt_plan_destroy(*pp);
         *pp = NULL;

@@ -39,6 +39,11 @@
 #define E_STATE (-4)
 #define E_HW (-6)
 
+/* role encoding of register-resident programs (see qgt_dev_op2_t) */
+#define RL_REG_ 8
+#define RL_WARP_ 16
+#define RL_OUT_ 32
+
 /* per-qubit action type of a gate, for commutation */
 enum { AT_NONE = 0, AT_Z = 1, AT_X = 2, AT_Y = 3, AT_G = 4 };
 
@@ -56,6 +61,7 @@ typedef struct {
 typedef struct {
     int op_begin, op_count;
     int ent_begin, ent_count;
+    int prog_begin, prog_count;   /* register-resident program (full tiles), 0 = v1 pass */
     int tile_bits;
     uint32_t tile_mask;
     int8_t l2p[16];
@@ -85,6 +91,13 @@ struct qgt_plan {
     void* split;
     qgt_dev_op_t* ops_d;
     qgt_dev_entry_t* ents_d;
+    qgt_dev_op2_t* prog_h;
+    int nprog;
+    int8_t* segs_h;
+    int nsegs;
+    qgt_dev_op2_t* prog_d;
+    int8_t* segs_d;
+    float* coef32_d;
     qgt_dev_coef_desc_t* coef_desc_d;
     double* coef_d;
     double* theta_d;
@@ -104,6 +117,7 @@ struct qgt_plan {
     int64_t vector_passes, gate_bytes;
     int launches;
     int has_run;
+    void* prof_ev[7];             /* phase events of qgt_plan_profile_step (NULL otherwise) */
 };
 
 static int popcount32(uint32_t x) { return __builtin_popcount(x); }
@@ -257,6 +271,7 @@ static int compile_schedule(qgt_plan_t* p)
             op->lb2 = g->q1 >= 0 ? p2l[g->q1] : -1;
             op->coef = g->coef;
             op->slot = g->slot;
+            op->pad = (int16_t)g->type;
             op->gen = QGEN_NONE;
             switch (g->type) {
             case QGT_GATE_RX: op->kind = QOP_1Q; op->gen = g->slot >= 0 ? QGEN_X : 0; break;
@@ -360,6 +375,132 @@ static int build_entries(qgt_plan_t* p)
     return 0;
 }
 
+/* Register-resident programs for passes whose tile has the full width
+ * (13 bits complex64 / 12 bits complex128).  Lanes are local bits 0..4; the
+ * other local bits are split into RB register bits and 3 warp bits per
+ * segment.  A gate whose target is a warp bit opens a new segment whose
+ * register bits are the next distinct targets (looking ahead), so that the
+ * shared-memory re-layouts are few.  SWAP becomes three CNOTs. */
+static int build_programs(qgt_plan_t* p)
+{
+    const int tb = p->fp64 ? QGT_TILE_MAX_F64 : QGT_TILE_MAX_F32;
+    const int RB = p->fp64 ? 4 : 5;
+    int cap = 3 * p->nops + 2 * p->npasses + 16, scap = 2 * p->nops + p->npasses + 16;
+    p->prog_h = (qgt_dev_op2_t*)calloc((size_t)cap, sizeof(qgt_dev_op2_t));
+    p->segs_h = (int8_t*)calloc((size_t)scap * 16, 1);
+    int* remap = (int*)malloc(sizeof(int) * ((size_t)p->nops + 1));
+    if (!p->prog_h || !p->segs_h || !remap) { free(remap); return qgt_set_error(E_NOMEM, "programs: oom"); }
+    p->nprog = 0;
+    p->nsegs = 0;
+    for (int k = 0; k < p->npasses; k++) {
+        spass_t* ps = &p->passes[k];
+        ps->prog_begin = p->nprog;
+        ps->prog_count = 0;
+        if (ps->tile_bits != tb || p->n < tb) continue;
+        const qgt_dev_op_t* ops = p->ops_h + ps->op_begin;
+        const int no = ps->op_count;
+        /* expanded op list: SWAP -> 3 CNOTs (target local bit, control local bit) */
+        int role[32];
+        int regs[8];
+        int nreg = 0;
+        /* first layout: the first RB distinct non-lane targets */
+        #define NEEDBIT(o) (((o)->kind == QOP_1Q || (o)->kind == QOP_CNOT) ? (o)->lb : ((o)->kind == QOP_SWAP ? (o)->lb : -1))
+        int cur_op = 0;
+        int first = 1;
+        while (1) {
+            /* choose the register bits for a segment starting at op cur_op */
+            int chosen[8], nc = 0;
+            for (int j = cur_op; j < no && nc < RB; j++) {
+                int cands[2] = {NEEDBIT(&ops[j]), ops[j].kind == QOP_SWAP ? ops[j].lb2 : -1};
+                for (int c = 0; c < 2; c++) {
+                    int b = cands[c];
+                    if (b < QGT_LANE_BITS || nc >= RB) continue;
+                    int dup = 0;
+                    for (int t = 0; t < nc; t++) dup |= chosen[t] == b;
+                    if (!dup) chosen[nc++] = b;
+                }
+            }
+            /* keep previous register bits to fill up, then the lowest free bits */
+            for (int t = 0; t < nreg && nc < RB; t++) {
+                int dup = 0;
+                for (int u = 0; u < nc; u++) dup |= chosen[u] == regs[t];
+                if (!dup) chosen[nc++] = regs[t];
+            }
+            for (int b = QGT_LANE_BITS; b < tb && nc < RB; b++) {
+                int dup = 0;
+                for (int u = 0; u < nc; u++) dup |= chosen[u] == b;
+                if (!dup) chosen[nc++] = b;
+            }
+            nreg = nc;
+            for (int t = 0; t < nc; t++) regs[t] = chosen[t];
+            if (p->nsegs >= scap || p->nprog + 4 >= cap) { free(remap); return qgt_set_error(E_STATE, "programs: capacity"); }
+            int8_t* L = p->segs_h + 16 * p->nsegs;
+            for (int b = 0; b < 32; b++) role[b] = -1;
+            for (int b = 0; b < QGT_LANE_BITS; b++) role[b] = b;
+            for (int t = 0; t < RB; t++) { L[t] = (int8_t)regs[t]; role[regs[t]] = RL_REG_ + t; }
+            int w = 0;
+            for (int b = QGT_LANE_BITS; b < tb; b++)
+                if (role[b] < 0) { L[8 + w] = (int8_t)b; role[b] = RL_WARP_ + w; w++; }
+            qgt_dev_op2_t* so = &p->prog_h[p->nprog++];
+            memset(so, 0, sizeof *so);
+            so->kind = Q2_SEG;
+            so->seg = (int16_t)p->nsegs++;
+            first = 0;
+            /* emit ops until one needs a warp bit */
+            int j = cur_op;
+            for (; j < no; j++) {
+                const qgt_dev_op_t* o = &ops[j];
+                int need1 = NEEDBIT(o), need2 = o->kind == QOP_SWAP ? o->lb2 : -1;
+                if ((need1 >= 0 && role[need1] >= RL_WARP_) || (need2 >= 0 && role[need2] >= RL_WARP_)) break;
+                if (p->nprog + 3 >= cap) { free(remap); return qgt_set_error(E_STATE, "programs: capacity"); }
+                #define ROLE(lb, q) ((lb) >= 0 ? (uint8_t)role[(lb)] : (uint8_t)RL_OUT_)
+                qgt_dev_op2_t x;
+                memset(&x, 0, sizeof x);
+                x.q = o->q;
+                x.q2 = o->q2;
+                x.coef = o->coef;
+                x.slot = o->slot;
+                x.gen = (uint8_t)o->gen;
+                x.ra = ROLE(o->lb, o->q);
+                x.rb = ROLE(o->lb2, o->q2);
+                switch (o->kind) {
+                case QOP_1Q:
+                    x.kind = (o->pad == QGT_GATE_RY || o->pad == QGT_GATE_H || o->pad == QGT_GATE_X) ? Q2_UR : Q2_U;
+                    break;
+                case QOP_PHASE: x.kind = Q2_PHASE; break;
+                case QOP_CZ: x.kind = Q2_CZ; break;
+                case QOP_CNOT: x.kind = Q2_CNOT; break;
+                case QOP_SWAP: {
+                    /* SWAP(a, b) = CNOT(a->b) CNOT(b->a) CNOT(a->b): target first */
+                    qgt_dev_op2_t c1 = x, c2 = x;
+                    c1.kind = Q2_CNOT; c1.ra = ROLE(o->lb2, o->q2); c1.rb = ROLE(o->lb, o->q); c1.q = o->q2; c1.q2 = o->q;
+                    c2.kind = Q2_CNOT; c2.ra = ROLE(o->lb, o->q); c2.rb = ROLE(o->lb2, o->q2);
+                    c1.gen = 0; c2.gen = 0;
+                    p->prog_h[p->nprog++] = c1;
+                    p->prog_h[p->nprog++] = c2;
+                    x = c1;
+                    break;
+                }
+                default: x.kind = Q2_PHASE; break;
+                }
+                remap[j] = p->nprog;
+                p->prog_h[p->nprog++] = x;
+                #undef ROLE
+            }
+            cur_op = j;
+            if (cur_op >= no) break;
+        }
+        (void)first;
+        #undef NEEDBIT
+        ps->prog_count = p->nprog - ps->prog_begin;
+        /* spawn entries of this pass point into the program */
+        for (int e = ps->ent_begin; e < ps->ent_begin + ps->ent_count; e++)
+            if (p->ents_h[e].spawn_op >= 0) p->ents_h[e].spawn_op = remap[p->ents_h[e].spawn_op] - ps->prog_begin;
+    }
+    free(remap);
+    return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* plan lifecycle                                                            */
 /* ------------------------------------------------------------------------ */
@@ -434,6 +575,7 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
     }
     if ((rc = compile_schedule(p)) != 0) goto fail;
     if ((rc = build_entries(p)) != 0) goto fail;
+    if ((rc = build_programs(p)) != 0) goto fail;
     {
         int nb = p->n >= 3 ? p->n : p->n - 1;
         p->hscale = fabs(p->opt.tfim_J) * nb + fabs(p->opt.tfim_h) * p->n;
@@ -458,6 +600,9 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
     DALLOC(p->ents_d, sizeof(qgt_dev_entry_t) * (size_t)(p->nents + 1));
     DALLOC(p->coef_desc_d, sizeof(qgt_dev_coef_desc_t) * (size_t)(p->ncoef + 1));
     DALLOC(p->coef_d, sizeof(double) * 8 * (size_t)(p->ncoef + 1));
+    DALLOC(p->coef32_d, sizeof(float) * 8 * (size_t)(p->ncoef + 1));
+    DALLOC(p->prog_d, sizeof(qgt_dev_op2_t) * (size_t)(p->nprog + 1));
+    DALLOC(p->segs_d, (size_t)16 * (p->nsegs + 1));
     DALLOC(p->theta_d, sizeof(double) * (size_t)(p->P + 1));
     DALLOC(p->HG_d, sizeof(double) * 2 * (size_t)p->rows * p->rows);
     DALLOC(p->Q_d, sizeof(double) * 2 * (size_t)p->P * p->P);
@@ -490,6 +635,8 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
     if ((rc = qgt_dev_memset(p->theta_d, 0, sizeof(double) * (size_t)(p->P + 1), p->stream)) != 0) goto fail;
     if ((rc = qgt_dev_memcpy_h2d(p->ops_d, p->ops_h, sizeof(qgt_dev_op_t) * (size_t)p->nops, p->stream)) != 0) goto fail;
     if ((rc = qgt_dev_memcpy_h2d(p->ents_d, p->ents_h, sizeof(qgt_dev_entry_t) * (size_t)p->nents, p->stream)) != 0) goto fail;
+    if (p->nprog && (rc = qgt_dev_memcpy_h2d(p->prog_d, p->prog_h, sizeof(qgt_dev_op2_t) * (size_t)p->nprog, p->stream)) != 0) goto fail;
+    if (p->nsegs && (rc = qgt_dev_memcpy_h2d(p->segs_d, p->segs_h, (size_t)16 * p->nsegs, p->stream)) != 0) goto fail;
     if ((rc = qgt_dev_memcpy_h2d(p->coef_desc_d, p->coef_h, sizeof(qgt_dev_coef_desc_t) * (size_t)p->ncoef, p->stream)) != 0) goto fail;
     if ((rc = qgt_dev_memcpy_h2d(p->slot_param_d, p->slot_param_h, sizeof(int32_t) * (size_t)p->nslots, p->stream)) != 0) goto fail;
     if ((rc = qgt_dev_memcpy_h2d(p->param_ptr_d, p->param_ptr_h, sizeof(int32_t) * (size_t)(p->P + 1), p->stream)) != 0) goto fail;
@@ -528,14 +675,14 @@ void qgt_plan_destroy(qgt_plan_t* p)
     qgt_dev_tc_gram_destroy(p->tc);
     qgt_dev_dg_gram_destroy(p->dg);
     qgt_dev_free(p->rowmax_d);
-    void* dev[] = {p->V, p->split, p->ops_d, p->ents_d, p->coef_desc_d, p->coef_d, p->theta_d, p->HG_d, p->part_d,
+    void* dev[] = {p->V, p->split, p->ops_d, p->ents_d, p->prog_d, p->segs_d, p->coef32_d, p->coef_desc_d, p->coef_d, p->theta_d, p->HG_d, p->part_d,
                    p->Q_d, p->grad_d, p->energy_d, p->natgrad_d, p->chol_work_d, p->status_d, p->slot_param_d,
                    p->param_ptr_d, p->param_slots_d};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++) qgt_dev_free(dev[i]);
     void* pin[] = {p->theta_pin, p->Q_pin, p->grad_pin, p->natgrad_pin, p->energy_pin, p->status_pin};
     for (size_t i = 0; i < sizeof pin / sizeof pin[0]; i++) qgt_dev_host_free(pin[i]);
     qgt_dev_stream_destroy(p->stream);
-    free(p->gates); free(p->passes); free(p->ops_h); free(p->ents_h); free(p->coef_h);
+    free(p->gates); free(p->passes); free(p->ops_h); free(p->ents_h); free(p->coef_h); free(p->prog_h); free(p->segs_h);
     free(p->slot_param_h); free(p->param_ptr_h); free(p->param_slots_h);
     free(p);
 }
@@ -564,13 +711,21 @@ int qgt_plan_get_info(const qgt_plan_t* p, qgt_plan_info_t* info)
 /* execution                                                                 */
 /* ------------------------------------------------------------------------ */
 
+#define MARK(i) do { if (p->prof_ev[i] && (rc = qgt_dev_event_record(p->prof_ev[i], p->stream)) != 0) return rc; } while (0)
+
 static int run_step(qgt_plan_t* p)
 {
     int rc;
     int launches = 0;
+    MARK(0);
     if ((rc = qgt_dev_prepare(p->coef_desc_d, p->ncoef, p->theta_d, p->coef_d, p->stream)) != 0) return rc;
     launches += p->ncoef > 0;
+    if (!p->fp64 && p->nprog > 0) {
+        if ((rc = qgt_dev_prepare32(p->coef_desc_d, p->ncoef, p->theta_d, p->coef32_d, p->stream)) != 0) return rc;
+        launches += p->ncoef > 0;
+    }
     if (p->dg && (rc = qgt_dev_memset(p->rowmax_d, 0, sizeof(uint32_t) * (size_t)p->rows, p->stream)) != 0) return rc;
+    MARK(1);
     for (int k = 0; k < p->npasses; k++) {
         const spass_t* ps = &p->passes[k];
         qgt_dev_pass_args_t a;
@@ -592,7 +747,31 @@ static int run_step(qgt_plan_t* p)
         a.tile_mask = ps->tile_mask;
         memcpy(a.local_to_phys, ps->l2p, sizeof a.local_to_phys);
         a.rowmax = p->rowmax_d;
-        if ((rc = qgt_dev_pass(&a, p->fp64, p->stream)) != 0) return rc;
+        if (ps->prog_count > 0) {
+            qgt_dev_pass2_args_t b;
+            memset(&b, 0, sizeof b);
+            b.V = p->V;
+            b.N = p->N;
+            b.ops = p->prog_d + ps->prog_begin;
+            b.nops = ps->prog_count;
+            b.segs = p->segs_d;
+            b.entries = a.entries;
+            b.nentries = a.nentries;
+            b.coef = p->coef_d;
+            b.coef32 = p->coef32_d;
+            b.split = a.split;
+            b.split_ld = a.split_ld;
+            b.split_plane_stride = a.split_plane_stride;
+            b.split_scale = a.split_scale;
+            b.n = a.n;
+            b.tile_bits = a.tile_bits;
+            b.tile_mask = a.tile_mask;
+            memcpy(b.local_to_phys, a.local_to_phys, sizeof b.local_to_phys);
+            b.rowmax = a.rowmax;
+            if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) return rc;
+        } else if ((rc = qgt_dev_pass(&a, p->fp64, p->stream)) != 0) {
+            return rc;
+        }
         launches++;
     }
     if (p->npasses == 0) {
@@ -604,6 +783,7 @@ static int run_step(qgt_plan_t* p)
         if ((rc = qgt_dev_memcpy_h2d(p->V, p->fp64 ? (const void*)one : (const void*)onef, ab, p->stream)) != 0) return rc;
         if (!p->fp64) return qgt_set_error(E_INVAL, "mixed plan needs at least one gate");
     }
+    MARK(2);
     const int has_h = p->opt.hamiltonian == QGT_HAMILTONIAN_TFIM;
     if (has_h) {
         size_t ab = p->fp64 ? 16 : 8;
@@ -614,6 +794,7 @@ static int run_step(qgt_plan_t* p)
             return rc;
         launches++;
     }
+    MARK(3);
     if (p->fp64) {
         if ((rc = qgt_dev_gram_f64(p->V, p->N, p->rows, p->part_d, p->part_nsplit, p->HG_d, p->stream)) != 0) return rc;
     } else if (p->dg) {
@@ -623,6 +804,7 @@ static int run_step(qgt_plan_t* p)
         if ((rc = qgt_dev_tc_gram_run(p->tc, 1.0 / (s * s), p->HG_d, p->stream)) != 0) return rc;
     }
     launches += 2;
+    MARK(4);
     if (p->P > 0) {
         qgt_dev_post_args_t pa;
         memset(&pa, 0, sizeof pa);
@@ -639,14 +821,45 @@ static int run_step(qgt_plan_t* p)
         pa.energy = p->energy_d;
         if ((rc = qgt_dev_post(&pa, p->stream)) != 0) return rc;
         launches += 1 + has_h;
+        MARK(5);
         if (has_h) {
-            if ((rc = qgt_dev_cholesky(p->Q_d, 1, p->grad_d, p->P, p->opt.lambda, p->chol_work_d, p->natgrad_d,
-                                       p->status_d, p->stream)) != 0)
-                return rc;
-            launches++;
+            if (p->P <= 4096) {
+                if ((rc = qgt_dev_cholesky_blocked(p->Q_d, 1, p->grad_d, p->P, p->opt.lambda, p->chol_work_d,
+                                                   p->natgrad_d, p->status_d, p->stream)) != 0)
+                    return rc;
+                launches += qgt_dev_cholesky_launches(p->P);
+            } else {
+                if ((rc = qgt_dev_cholesky(p->Q_d, 1, p->grad_d, p->P, p->opt.lambda, p->chol_work_d, p->natgrad_d,
+                                           p->status_d, p->stream)) != 0)
+                    return rc;
+                launches++;
+            }
         }
     }
+    if (p->P <= 0) MARK(5);
+    MARK(6);
     p->launches = launches;
+    return 0;
+}
+
+int qgt_plan_profile_step(qgt_plan_t* p, qgt_step_profile_t* pr)
+{
+    if (!p || !pr) return qgt_set_error(E_INVAL, "qgt_plan_profile_step: NULL argument");
+    int rc = 0;
+    for (int i = 0; i < 7 && !rc; i++) rc = qgt_dev_event_create(&p->prof_ev[i]);
+    if (!rc) rc = run_step(p);
+    float t[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < 6 && !rc; i++) rc = qgt_dev_event_elapsed(p->prof_ev[i], p->prof_ev[i + 1], &t[i]);
+    for (int i = 0; i < 7; i++) { qgt_dev_event_destroy(p->prof_ev[i]); p->prof_ev[i] = NULL; }
+    if (rc) return rc;
+    p->has_run = 1;
+    pr->prepare_ms = t[0];
+    pr->passes_ms = t[1];
+    pr->hamiltonian_ms = t[2];
+    pr->gram_ms = t[3];
+    pr->post_ms = t[4];
+    pr->solve_ms = t[5];
+    pr->total_ms = t[0] + t[1] + t[2] + t[3] + t[4] + t[5];
     return 0;
 }
 
@@ -692,6 +905,16 @@ int qgt_plan_execute_host(qgt_plan_t* p, const double* theta, double* Q, double*
         if ((rc = qgt_dev_memcpy_h2d(p->theta_d, p->theta_pin, sizeof(double) * (size_t)p->P, p->stream)) != 0) return rc;
     }
     if ((rc = launch_step(p)) != 0) return rc;
+    if (has_h && p->P > 0) {
+        /* the graph's blocked solve has no retries: on a non-positive pivot
+         * rerun the solve with lambda x 10 retries (outside the graph) */
+        if ((rc = qgt_dev_memcpy_d2h(p->status_pin, p->status_d, sizeof(double) * 2, p->stream)) != 0) return rc;
+        if ((rc = qgt_dev_stream_sync(p->stream)) != 0) return rc;
+        if ((int)p->status_pin[0] != 0 &&
+            (rc = qgt_dev_cholesky(p->Q_d, 1, p->grad_d, p->P, p->opt.lambda * 10.0, p->chol_work_d, p->natgrad_d,
+                                   p->status_d, p->stream)) != 0)
+            return rc;
+    }
     if (Q && (rc = qgt_dev_memcpy_d2h(p->Q_pin, p->Q_d, sizeof(double) * 2 * (size_t)p->P * p->P, p->stream)) != 0) return rc;
     if (grad && (rc = qgt_dev_memcpy_d2h(p->grad_pin, p->grad_d, sizeof(double) * (size_t)p->P, p->stream)) != 0) return rc;
     if (energy && (rc = qgt_dev_memcpy_d2h(p->energy_pin, p->energy_d, sizeof(double), p->stream)) != 0) return rc;
@@ -739,9 +962,19 @@ int qgt_plan_get_state(qgt_plan_t* p, double* psi)
 int qgt_plan_get_row(qgt_plan_t* p, int row, double* out)
 {
     if (!p || !out || row < 0 || row >= p->rows) return qgt_set_error(E_INVAL, "qgt_plan_get_row: bad argument");
-    if (!p->fp64) return qgt_set_error(E_STATE, "qgt_plan_get_row: derivative rows are kept only by FP64 plans");
-    int rc = qgt_dev_memcpy_d2h(out, (char*)p->V + (size_t)row * p->N * 16, sizeof(double) * 2 * (size_t)p->N, p->stream);
+    if (!p->has_run) return qgt_set_error(E_STATE, "qgt_plan_get_row: no step has run");
+    if (p->fp64) {
+        int rc = qgt_dev_memcpy_d2h(out, (char*)p->V + (size_t)row * p->N * 16, sizeof(double) * 2 * (size_t)p->N, p->stream);
+        if (!rc) rc = qgt_dev_stream_sync(p->stream);
+        return rc;
+    }
+    if (p->opt.precision != QGT_PRECISION_MIXED) return qgt_set_error(E_STATE, "qgt_plan_get_row: not kept by BF16x3 plans");
+    float* tmp = (float*)malloc(sizeof(float) * 2 * (size_t)p->N);
+    if (!tmp) return qgt_set_error(E_NOMEM, "qgt_plan_get_row: oom");
+    int rc = qgt_dev_memcpy_d2h(tmp, (char*)p->V + (size_t)row * p->N * 8, sizeof(float) * 2 * (size_t)p->N, p->stream);
     if (!rc) rc = qgt_dev_stream_sync(p->stream);
+    if (!rc) for (int64_t i = 0; i < 2 * p->N; i++) out[i] = tmp[i];
+    free(tmp);
     return rc;
 }
 

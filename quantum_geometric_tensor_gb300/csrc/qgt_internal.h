@@ -96,6 +96,45 @@ typedef struct {
     uint32_t* rowmax;               /* per-row max |amplitude| as float bits (QENT_ROWMAX) */
 } qgt_dev_pass_args_t;
 
+/* ---- register-resident passes (qgt_pass2.cu) ----
+ * A pass program is a list of ops; Q2_SEG ops switch the layout (which local
+ * bits are register bits / warp bits) through shared memory.  Bits are
+ * role-encoded: 0..4 lane bit, 8 + i register bit i, 16 + w warp bit w,
+ * 32 outside the tile (physical qubit in q / q2). */
+enum { Q2_SEG = 1, Q2_U = 2, Q2_UR = 3, Q2_PHASE = 4, Q2_CZ = 5, Q2_CNOT = 6 };
+typedef struct {
+    uint8_t kind;
+    uint8_t ra;     /* target / first bit (role-encoded) */
+    uint8_t rb;     /* control / second bit (role-encoded) */
+    uint8_t gen;    /* QGEN_* inserted after this op for a spawn entry */
+    int8_t q, q2;   /* physical qubits of ra / rb */
+    int16_t seg;    /* Q2_SEG: layout index */
+    int32_t coef;
+    int32_t slot;
+} qgt_dev_op2_t;
+
+typedef struct {
+    void* V;
+    int64_t N;
+    const qgt_dev_op2_t* ops;       /* program; ops[0] is the initial Q2_SEG */
+    int32_t nops;
+    const int8_t* segs;             /* 16 per layout: [0, RB) register local bits, [8, 11) warp local bits */
+    const qgt_dev_entry_t* entries; /* spawn_op = program index */
+    int32_t nentries;
+    const double* coef;             /* FP64 coefficients (complex128 path) */
+    const float* coef32;            /* complex64 coefficients with exact angles */
+    void* split;
+    int64_t split_ld, split_plane_stride;
+    float split_scale;
+    int32_t n, tile_bits;
+    uint32_t tile_mask;
+    int8_t local_to_phys[16];
+    uint32_t* rowmax;
+} qgt_dev_pass2_args_t;
+int qgt_dev_pass2(const qgt_dev_pass2_args_t* args, int fp64, void* stream);
+int qgt_dev_prepare32(const qgt_dev_coef_desc_t* descs_dev, int32_t ncoef, const double* theta_dev,
+                      float* coef32_dev, void* stream);
+
 /* internal plan helpers used by the reference API layer */
 struct qgt_plan;
 int qgt_plan_combine_slots(struct qgt_plan* p, const double* c, double* out);
@@ -123,6 +162,11 @@ int qgt_dev_host_alloc(void** p, size_t bytes);   /* pinned */
 int qgt_dev_host_free(void* p);
 int qgt_dev_last_error(void);                     /* cudaGetLastError as qgt_error_t */
 const char* qgt_dev_error_string(void);
+
+int qgt_dev_event_create(void** ev);
+int qgt_dev_event_destroy(void* ev);
+int qgt_dev_event_record(void* ev, void* stream);
+int qgt_dev_event_elapsed(void* start, void* end, float* ms);
 
 /* ---- kernels ---- */
 int qgt_dev_prepare(const qgt_dev_coef_desc_t* descs_dev, int32_t ncoef, const double* theta_dev,
@@ -182,6 +226,11 @@ int qgt_dev_post(const qgt_dev_post_args_t* a, void* stream);
  * status[1] = lambda used (as double bits in the second slot). */
 int qgt_dev_cholesky(const double* A, int complex_input, const double* b, int32_t P,
                      double lambda, double* work, double* x, double* status, void* stream);
+/* the same solve, blocked over many CTAs, without retries (status[0] =
+ * QGT_ERROR_NOT_POSITIVE_DEFINITE on a non-positive pivot); P <= 4096 */
+int qgt_dev_cholesky_blocked(const double* A, int complex_input, const double* b, int32_t P,
+                             double lambda, double* work, double* x, double* status, void* stream);
+int qgt_dev_cholesky_launches(int32_t P);
 
 #ifdef __cplusplus
 }

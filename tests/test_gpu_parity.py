@@ -100,7 +100,8 @@ def test_cholesky_retry_and_solve(Q):
     x, used = Q.cholesky_solve(A, b, 1e-3)
     assert used == 1e-3
     assert rel((A + 1e-3 * np.eye(40)) @ x, b) < 1e-10
-    # indefinite matrix: lambda grows x10 until positive
+    # indefinite matrix: lambda grows x10 until positive (-0.05 + 0.1 > 0)
     B = np.diag(np.r_[np.ones(39), -0.05])
     x, used = Q.cholesky_solve(B, np.ones(40), 1e-3)
-    assert used == pytest.approx(1.0)
+    assert used == pytest.approx(0.1)
+    assert rel((B + used * np.eye(40)) @ x, np.ones(40)) < 1e-12
