@@ -176,6 +176,18 @@ int qgt_qgt_from_states(const double* psi, const double* D, int64_t dim, int32_t
 int qgt_cholesky_solve_f64(const double* A, const double* g, double lambda, int32_t P,
                            double* x, double* lambda_used);
 
+/* The same solve with no device allocation (no counterpart in the reference):
+ * every device buffer comes from one static array sized for P up to
+ * QGT_NOALLOC_SOLVE_MAX_P; larger P is rejected with an error.  For callers
+ * whose device memory belongs to another allocator, or that cannot take
+ * cudaFree's device-wide synchronisation in a loop.  The first call on each
+ * device (that device current) looks up the array's address; make it before
+ * any stream capture begins there.  Calls overlapping in time on one device
+ * share the array and race: serialise them. */
+#define QGT_NOALLOC_SOLVE_MAX_P 512
+int qgt_cholesky_solve_f64_noalloc(const double* A, const double* g, double lambda, int32_t P,
+                                   double* x, double* lambda_used);
+
 /* Thread-local text of the last error. */
 const char* qgt_last_error(void);
 /* Library version string. */
