@@ -203,10 +203,12 @@ def run_gb300(args, ws, rank, local):
     dist = init_dist(ws, local)
     dev = local if ws > 1 else 0
     torch.cuda.set_device(dev)
-    gates = Q.ansatz_gates(N_QUBITS, LAYERS, ENT)
-    P = 2 * N_QUBITS * LAYERS
+    nq, nl = args.qubits, args.layers
+    workload = WORKLOAD if (nq, nl) == (N_QUBITS, LAYERS) else f"hea{nq}_L{nl}_czring_P{2 * nq * nl}_tfim_natgrad"
+    gates = Q.ansatz_gates(nq, nl, ENT)
+    P = 2 * nq * nl
     theta = O.splitmix64_params(SEED + rank, P)
-    plan = Q.Plan(N_QUBITS, gates, P, precision=Q.MIXED, lam=LAMBDA, device=dev)
+    plan = Q.Plan(nq, gates, P, precision=Q.MIXED, lam=LAMBDA, device=dev)
     info = plan.info()
     th_d = torch.tensor(theta, dtype=torch.float64, device=f"cuda:{dev}")
     Q_d = torch.zeros((P, P, 2), dtype=torch.float64, device=f"cuda:{dev}")
@@ -296,8 +298,10 @@ def run_gb300(args, ws, rank, local):
     # FP64 GPU path on the same point; mixed error against it
     fp64 = None
     try:
+        if args.no_fp64:
+            raise RuntimeError("skipped (--no-fp64)")
         out_m = plan.run(theta)
-        with Q.Plan(N_QUBITS, gates, P, precision=Q.FP64, lam=LAMBDA, device=dev) as p64:
+        with Q.Plan(nq, gates, P, precision=Q.FP64, lam=LAMBDA, device=dev) as p64:
             p64.run(theta)
             t0 = time.perf_counter()
             r64 = p64.run(theta)
@@ -319,7 +323,7 @@ def run_gb300(args, ws, rank, local):
         fp64 = {"error": str(ex)[:200]}
 
     cb = None
-    if ws == 1 and not args.no_cpu:
+    if ws == 1 and not args.no_cpu and (nq, nl) == (N_QUBITS, LAYERS):
         try:
             cb = cpu_baseline()
             cb.pop("seconds_per_qgt", None)
@@ -329,10 +333,10 @@ def run_gb300(args, ws, rank, local):
     line = {"metric": METRIC, "value": value, "unit": "QGTs/sec", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64/fp16-digits/f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "qubits": N_QUBITS, "layers": LAYERS, "params": P,
+            "config": {"workload": workload, "qubits": nq, "layers": nl, "params": P,
                        "entangler": "cz_ring", "hamiltonian": "tfim_ring J=h=1", "lambda": LAMBDA,
                        "precision": "mixed", "parallelism": f"replicas{ws}" if ws > 1 else "single",
-                       "l2": "working set 2.6 GB > L2 (no flush needed)"},
+                       "l2": f"working set {info.device_bytes / 1e9:.1f} GB > L2 (no flush needed)"},
             "e2e": {"value": ws * 1000.0 / e2e_ms, "unit": "QGTs/sec", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
             "gpu_launches": info.num_launches * args.steps,
@@ -365,6 +369,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison")
+    ap.add_argument("--qubits", type=int, default=N_QUBITS, help="smaller register for profiling captures")
+    ap.add_argument("--layers", type=int, default=LAYERS)
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":

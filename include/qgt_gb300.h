@@ -85,6 +85,14 @@ typedef struct {
     double lambda;      /* Tikhonov lambda of the natural-gradient step (Re Q + lambda I) x = grad E */
     int32_t device;     /* CUDA device ordinal */
     int32_t use_graph;  /* capture the whole step in one CUDA graph (default 1) */
+    /* parameter points evaluated per step (default 1): theta is batch x
+     * num_params, every output one block per point; all points share one
+     * launch per kernel (the point is a grid dimension) */
+    int32_t batch;
+    /* parameters [0, num_deriv_params) get derivative states and the outputs
+     * are num_deriv_params wide (Q: Pd x Pd, grad / natgrad: Pd); the others
+     * only set gate angles.  0 = all num_params. */
+    int32_t num_deriv_params;
 } qgt_plan_options_t;
 
 typedef struct qgt_plan qgt_plan_t;
@@ -97,6 +105,7 @@ typedef struct {
     int64_t gate_bytes;                                    /* algorithmic HBM bytes of the gate passes per step */
     int64_t gram_flops;                                    /* 4 P (P+1) N: algorithmic Gram flops per step */
     int64_t device_bytes;                                  /* device memory held by the plan */
+    int32_t batch, num_deriv_params;                       /* points per step; output width Pd */
 } qgt_plan_info_t;
 
 /* Default options: MIXED, TFIM J = h = 1, lambda = 1e-3, device 0, graph on. */
@@ -117,7 +126,8 @@ int qgt_plan_get_info(const qgt_plan_t* plan, qgt_plan_info_t* info);
  *   grad    P      dE/dtheta (NULL allowed; needs a Hamiltonian)
  *   energy  1      <psi|H|psi>
  *   natgrad P      (Re Q + lambda I)^{-1} grad
- * Any output may be NULL. */
+ * Any output may be NULL.  With batch B and Pd derivative parameters theta is
+ * B x num_params and the outputs B x Pd x Pd, B x Pd, B, B x Pd. */
 int qgt_plan_execute_host(qgt_plan_t* plan, const double* theta, double* Q, double* grad,
                           double* energy, double* natgrad);
 
@@ -154,6 +164,126 @@ typedef struct {
     double solve_ms;        /* natural-gradient Cholesky solve */
 } qgt_step_profile_t;
 int qgt_plan_profile_step(qgt_plan_t* plan, qgt_step_profile_t* prof);
+
+/* ---- ragged batches ------------------------------------------------------
+ * Many circuits (any mix of qubit counts, depths and parameters) evaluated
+ * by ONE CUDA-graph launch.  Circuits with the same structure share one
+ * batched plan (the parameter point is a grid dimension of every kernel);
+ * optionally each circuit also gets a G x G Berry-curvature map
+ * Omega_ab(theta_a, theta_b) = Im Q_ab over two of its parameters on the
+ * lattice theta = 2 pi k / G, k = 0 .. G-1, the other parameters at the
+ * circuit's theta.  The reference has no batch interface: it evaluates each
+ * circuit through geometric_compute_full_qgt
+ * (src/quantum_geometric/core/quantum_geometric_curvature.c:289-320) and the
+ * pointwise curvature of quantum_geometric_curvature.c:181-198. */
+typedef struct qgt_batch qgt_batch_t;
+
+typedef struct {
+    qgt_precision_t precision;  /* QGT_PRECISION_FP64 or QGT_PRECISION_MIXED */
+    int32_t berry_grid;         /* G (0 = no maps; default 32) */
+    int32_t device;
+    int32_t streams;            /* concurrent branches inside the graph (default 4, max 16) */
+} qgt_batch_options_t;
+
+typedef struct {
+    int32_t num_circuits, num_groups, num_berry_plans;
+    int32_t graph_kernels;      /* kernels and copies per batch launch */
+    int64_t device_bytes;
+} qgt_batch_info_t;
+
+void qgt_batch_default_options(qgt_batch_options_t* opt);
+/* berry_params: 2 per circuit (a, b), required when berry_grid > 0. */
+int qgt_batch_create(const qgt_circuit_desc_t* circuits, int32_t count, const int32_t* berry_params,
+                     const qgt_batch_options_t* opt, qgt_batch_t** batch);
+/* theta: the circuits' parameter vectors back to back (num_params each);
+ * Q: their P x P complex QGTs back to back (NULL allowed); berry: count x G x G
+ * doubles, map[i][j] at (theta_a, theta_b) = (2 pi i / G, 2 pi j / G) (NULL allowed). */
+int qgt_batch_execute_host(qgt_batch_t* batch, const double* theta, double* Q, double* berry);
+int qgt_batch_get_info(const qgt_batch_t* batch, qgt_batch_info_t* info);
+void qgt_batch_destroy(qgt_batch_t* batch);
+
+/* ---- learned metric preconditioner -------------------------------------
+ * No reference counterpart.  A 3-layer MLP (hidden width W, BF16 weights,
+ * FP32 accumulation) maps theta (P) to M = diag(d) + U U^T (U: P x r)
+ * approximating Re Q + lambda I; trained on the GPU by hand-written forward,
+ * backward and Adam kernels on exact metrics that theta-batched plans
+ * generate; used as the preconditioner of a GPU PCG natural-gradient solve.
+ * The exact-metric Cholesky step stays the reference solve
+ * (src/quantum_geometric/learning/quantum_pipeline_impl.c:1601-1682); the
+ * unpreconditioned CG it is compared with is
+ * src/quantum_geometric/hybrid/classical_optimization_engine.c:543-611. */
+typedef struct qgt_precond qgt_precond_t;
+
+typedef struct {
+    int32_t num_params;  /* P (1 .. 1024) */
+    int32_t width;       /* hidden width (default 512) */
+    int32_t rank;        /* r of U (default 16, max 32) */
+    double lambda;       /* target Re Q + lambda I; d >= lambda (default 1e-3) */
+    double u_scale;      /* U = u_scale x raw outputs (default 0.1) */
+    uint64_t seed;       /* weight initialisation */
+    int32_t device;
+} qgt_precond_config_t;
+
+typedef struct {
+    int32_t epochs;      /* default 30 */
+    int32_t batch;       /* default 256 (full batches only) */
+    double lr;           /* Adam learning rate (default 1e-3) */
+    double weight_decay; /* default 0 */
+    uint64_t seed;       /* shuffling */
+} qgt_precond_train_options_t;
+
+void qgt_precond_default_config(qgt_precond_config_t* cfg);
+void qgt_precond_default_train_options(qgt_precond_train_options_t* opt);
+int qgt_precond_create(const qgt_precond_config_t* cfg, qgt_precond_t** pc);
+void qgt_precond_destroy(qgt_precond_t* pc);
+/* weights as FP32 masters: W1 (W x 2P), b1 (W), W2 (W x W), b2 (W),
+ * W3 (O x W), b3 (O), O = P + P r; the products use their BF16 rounding.
+ * Input features are [cos theta, sin theta]; d = softplus(o[0:P]) + lambda,
+ * U = u_scale o[P:] (row-major P x r). */
+int64_t qgt_precond_num_weights(const qgt_precond_t* pc);
+int qgt_precond_get_weights(const qgt_precond_t* pc, float* w);
+int qgt_precond_set_weights(qgt_precond_t* pc, const float* w);
+/* exact metrics Re Q of S parameter points (theta S x P) on the GPU: metric S x P x P */
+int qgt_metric_dataset(const qgt_circuit_desc_t* circuit, const double* theta, int32_t S,
+                       qgt_precision_t precision, int32_t device, double* metric);
+/* train on host pairs (theta S x P, metric S x P x P); loss_history: epochs (NULL allowed) */
+int qgt_precond_train(qgt_precond_t* pc, const double* theta, const double* metric, int32_t S,
+                      const qgt_precond_train_options_t* opt, double* loss_history);
+/* train on the exact metrics of a circuit at S parameter points, generated on the GPU */
+int qgt_precond_train_circuit(qgt_precond_t* pc, const qgt_circuit_desc_t* circuit, const double* theta,
+                              int32_t S, qgt_precision_t precision, const qgt_precond_train_options_t* opt,
+                              double* loss_history);
+/* mean loss ||M - T||_F^2 / ||T||_F^2 over S samples and its gradient (num_weights floats), no update */
+int qgt_precond_loss_grad(qgt_precond_t* pc, const double* theta, const double* metric, int32_t S,
+                          double* loss, float* grad);
+/* d (S x P) and U (S x P x r) for S parameter points */
+int qgt_precond_predict(qgt_precond_t* pc, const double* theta, int32_t S, double* d, double* U);
+
+/* PCG on the GPU: (A + lambda I) x = b, A real P x P (host buffers);
+ * M = diag(d) + U U^T by Woodbury (d NULL: identity; r = 0: diagonal only).
+ * Stops at ||r|| <= tol ||b|| or max_iter; iters / resid: what it reached. */
+int qgt_pcg_solve_f64(const double* A, const double* b, double lambda, int32_t P, const double* d,
+                      const double* U, int32_t r, double tol, int32_t max_iter, double* x,
+                      int32_t* iters, double* resid);
+
+/* Natural-gradient VQE on the TFIM ring: theta <- theta - eta x per step, x
+ * from the exact Cholesky step, from CG, or from PCG with the learned
+ * preconditioner; the whole loop is enqueued on the device (one graph
+ * launch, one solve and one update per step).  Reference loop:
+ * src/quantum_geometric/hybrid/quantum_classical_algorithms.c:854-886. */
+enum { QGT_VQE_SOLVER_CHOLESKY = 0, QGT_VQE_SOLVER_CG = 1, QGT_VQE_SOLVER_PCG_LEARNED = 2 };
+typedef struct {
+    int32_t steps;        /* default 500 */
+    double eta;           /* default 0.05 */
+    double pcg_tol;       /* relative residual (default 1e-10) */
+    int32_t pcg_max_iter; /* default 1000 */
+    int32_t solver;       /* QGT_VQE_SOLVER_* (default Cholesky) */
+} qgt_vqe_options_t;
+void qgt_vqe_default_options(qgt_vqe_options_t* opt);
+/* energies: steps values E(theta_t) before each update; pcg_iters: steps (NULL allowed) */
+int qgt_vqe_run(const qgt_circuit_desc_t* circuit, const qgt_plan_options_t* plan_opt, qgt_precond_t* pc,
+                const qgt_vqe_options_t* opt, const double* theta0, double* energies, int32_t* pcg_iters,
+                double* theta_out);
 
 /* One-shot helpers over a temporary plan (reference-style convenience). */
 int qgt_compute_qgt_f64(const qgt_circuit_desc_t* circuit, const double* theta, double* Q,

@@ -32,14 +32,25 @@ class CircuitDesc(C.Structure):
 
 class PlanOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("hamiltonian", C.c_int), ("tfim_J", C.c_double), ("tfim_h", C.c_double),
-                ("lambda_", C.c_double), ("device", C.c_int32), ("use_graph", C.c_int32)]
+                ("lambda_", C.c_double), ("device", C.c_int32), ("use_graph", C.c_int32), ("batch", C.c_int32),
+                ("num_deriv_params", C.c_int32)]
 
 
 class PlanInfo(C.Structure):
     _fields_ = [("num_qubits", C.c_int32), ("num_params", C.c_int32), ("num_slots", C.c_int32),
                 ("num_rows", C.c_int32), ("num_passes", C.c_int32), ("num_launches", C.c_int32),
                 ("tile_bits", C.c_int32), ("vector_passes", C.c_int64), ("gate_bytes", C.c_int64),
-                ("gram_flops", C.c_int64), ("device_bytes", C.c_int64)]
+                ("gram_flops", C.c_int64), ("device_bytes", C.c_int64), ("batch", C.c_int32),
+                ("num_deriv_params", C.c_int32)]
+
+
+class BatchOptions(C.Structure):
+    _fields_ = [("precision", C.c_int), ("berry_grid", C.c_int32), ("device", C.c_int32), ("streams", C.c_int32)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("num_circuits", C.c_int32), ("num_groups", C.c_int32), ("num_berry_plans", C.c_int32),
+                ("graph_kernels", C.c_int32), ("device_bytes", C.c_int64)]
 
 
 class StepProfile(C.Structure):
@@ -73,6 +84,11 @@ def lib() -> C.CDLL:
         L.qgt_plan_device_status.argtypes = [vp, vp]
         L.qgt_cholesky_solve_f64.argtypes = [vp, vp, C.c_double, C.c_int32, vp, vp]
         L.qgt_plan_profile_step.argtypes = [vp, C.POINTER(StepProfile)]
+        L.qgt_batch_default_options.argtypes = [C.POINTER(BatchOptions)]
+        L.qgt_batch_create.argtypes = [vp, C.c_int32, vp, C.POINTER(BatchOptions), C.POINTER(vp)]
+        L.qgt_batch_execute_host.argtypes = [vp, vp, vp, vp]
+        L.qgt_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
+        L.qgt_batch_destroy.argtypes = [vp]
         L.qgt_last_error.restype = C.c_char_p
         L.qgt_version.restype = C.c_char_p
         _lib = L
@@ -132,18 +148,21 @@ class Plan:
     """A compiled circuit plan (qgt_plan_t)."""
 
     def __init__(self, n, gates, num_params=None, precision=MIXED, hamiltonian=HAM_TFIM, J=1.0, h=1.0,
-                 lam=1e-3, device=0, use_graph=True):
+                 lam=1e-3, device=0, use_graph=True, batch=1, deriv_params=0):
         L = lib()
         self.desc = circuit_desc(n, gates, num_params)
         o = PlanOptions()
         L.qgt_plan_default_options(C.byref(o))
         o.precision, o.hamiltonian, o.tfim_J, o.tfim_h = precision, hamiltonian, J, h
         o.lambda_, o.device, o.use_graph = lam, device, int(use_graph)
+        o.batch, o.num_deriv_params = int(batch), int(deriv_params)
         self.opt = o
         h_ = C.c_void_p()
         _check(L.qgt_plan_create(C.byref(self.desc), C.byref(o), C.byref(h_)), "qgt_plan_create")
         self.h = h_
         self.n, self.P = n, self.desc.num_params
+        self.B = int(batch)
+        self.Pd = int(deriv_params) if deriv_params else self.P
 
     def info(self) -> PlanInfo:
         i = PlanInfo()
@@ -151,15 +170,22 @@ class Plan:
         return i
 
     def run(self, theta, want=("Q", "grad", "energy", "natgrad")):
-        P = self.P
+        """One step.  theta: (P,) or, for a batched plan, (batch, P); outputs
+        gain a leading batch axis when batch > 1."""
+        B, P = self.B, self.Pd
         theta = np.ascontiguousarray(theta, dtype=np.float64)
-        Q = np.zeros((P, P), dtype=np.complex128) if "Q" in want else None
-        g = np.zeros(P) if "grad" in want else None
-        e = np.zeros(1) if "energy" in want else None
-        x = np.zeros(P) if "natgrad" in want else None
+        if theta.size != B * self.P:
+            raise ValueError(f"theta has {theta.size} values, plan wants {B} x {self.P}")
+        Q = np.zeros((B, P, P), dtype=np.complex128) if "Q" in want else None
+        g = np.zeros((B, P)) if "grad" in want else None
+        e = np.zeros(B) if "energy" in want else None
+        x = np.zeros((B, P)) if "natgrad" in want else None
         _check(lib().qgt_plan_execute_host(self.h, _ptr(theta), _ptr(Q), _ptr(g), _ptr(e), _ptr(x)),
                "qgt_plan_execute_host")
-        return {"Q": Q, "grad": g, "energy": None if e is None else float(e[0]), "natgrad": x}
+        if B == 1:
+            return {"Q": None if Q is None else Q[0], "grad": None if g is None else g[0],
+                    "energy": None if e is None else float(e[0]), "natgrad": None if x is None else x[0]}
+        return {"Q": Q, "grad": g, "energy": e, "natgrad": x}
 
     def state(self):
         psi = np.zeros(1 << self.n, dtype=np.complex128)
@@ -182,6 +208,63 @@ class Plan:
     def close(self):
         if getattr(self, "h", None):
             lib().qgt_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Batch:
+    """A ragged batch (qgt_batch_t): circuits = [(n, gates, num_params), ...];
+    berry_params = [(a, b), ...] per circuit when grid > 0."""
+
+    def __init__(self, circuits, berry_params=None, precision=MIXED, grid=32, device=0, streams=4):
+        L = lib()
+        self.descs = [circuit_desc(n, g, P) for (n, g, P) in circuits]
+        arr = (CircuitDesc * len(self.descs))(*self.descs)
+        self._arr = arr
+        self.P = [d.num_params for d in self.descs]
+        o = BatchOptions()
+        L.qgt_batch_default_options(C.byref(o))
+        o.precision, o.berry_grid, o.device, o.streams = precision, int(grid), device, int(streams)
+        self.G = int(grid)
+        bp = None
+        if grid > 0:
+            bp = np.ascontiguousarray(np.asarray(berry_params, dtype=np.int32).reshape(-1))
+        h_ = C.c_void_p()
+        _check(L.qgt_batch_create(C.cast(arr, C.c_void_p), len(self.descs), _ptr(bp), C.byref(o), C.byref(h_)),
+               "qgt_batch_create")
+        self.h = h_
+
+    def info(self) -> BatchInfo:
+        i = BatchInfo()
+        _check(lib().qgt_batch_get_info(self.h, C.byref(i)), "qgt_batch_get_info")
+        return i
+
+    def run(self, thetas):
+        """thetas: one parameter vector per circuit -> (list of P x P complex Q, count x G x G maps or None)."""
+        th = np.ascontiguousarray(np.concatenate([np.asarray(t, dtype=np.float64).reshape(-1) for t in thetas]))
+        Qflat = np.zeros(sum(P * P for P in self.P), dtype=np.complex128)
+        maps = np.zeros((len(self.P), self.G, self.G)) if self.G > 0 else None
+        _check(lib().qgt_batch_execute_host(self.h, _ptr(th), _ptr(Qflat), _ptr(maps)), "qgt_batch_execute_host")
+        out, at = [], 0
+        for P in self.P:
+            out.append(Qflat[at:at + P * P].reshape(P, P))
+            at += P * P
+        return out, maps
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().qgt_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):

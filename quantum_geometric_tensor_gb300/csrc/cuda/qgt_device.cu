@@ -111,10 +111,13 @@ const char* qgt_dev_error_string(void) { return cudaGetErrorString(cudaPeekAtLas
 // RZ = diag(e^{-ia/2}, e^{ia/2}); fixed gates as in
 // hybrid/quantum_classical_algorithms.c:228-276.
 // ---------------------------------------------------------------------------
-__global__ void prepare_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const double* theta, double* coef)
+__global__ void prepare_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const double* theta, double* coef,
+                               int theta_stride)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncoef) return;
+    theta += (int64_t)blockIdx.y * theta_stride;   // parameter point
+    coef += (int64_t)8 * blockIdx.y * ncoef;
     qgt_dev_coef_desc_t g = d[c];
     double a = g.param >= 0 ? theta[g.param] : g.angle;
     double m[8] = {1, 0, 0, 0, 0, 0, 1, 0};
@@ -142,9 +145,12 @@ __global__ void prepare_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const do
 template <typename T, typename R>
 __global__ void tfim_kernel(const T* __restrict__ psi, T* __restrict__ out, int n, R J, R h, R inv,
                             void* split, int64_t sld, int64_t pstride, int32_t srow, float sscale, int bf16,
-                            uint32_t* rowmax)
+                            uint32_t* rowmax, int64_t point_stride, int32_t rowmax_stride)
 {
     int64_t N = (int64_t)1 << n;
+    psi += blockIdx.y * point_stride;   // parameter point
+    out += blockIdx.y * point_stride;
+    if (rowmax) rowmax += (int64_t)blockIdx.y * rowmax_stride;
     float vmax = 0.f;
     int nb = n >= 3 ? n : n - 1;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
@@ -213,6 +219,8 @@ __global__ void post_qgt_kernel(qgt_dev_post_args_t a)
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int P = a.P;
     if (idx >= (int64_t)P * P) return;
+    a.HG += (int64_t)2 * blockIdx.y * a.rows * a.rows;   // parameter point
+    a.Q += (int64_t)2 * blockIdx.y * P * P;
     int p = (int)(idx / P), q = (int)(idx % P);
     double s = a.HG[0];
     double2 B = make_double2(0, 0), vp = make_double2(0, 0), vq = make_double2(0, 0);
@@ -239,6 +247,9 @@ __global__ void post_qgt_kernel(qgt_dev_post_args_t a)
 
 __global__ void post_grad_kernel(qgt_dev_post_args_t a)
 {
+    a.HG += (int64_t)2 * blockIdx.y * a.rows * a.rows;   // parameter point
+    a.grad += (int64_t)blockIdx.y * a.P;
+    if (a.energy) a.energy += blockIdx.y;
     double s = a.HG[0];
     double E = a.hscale * hg(a.HG, a.rows, 0, 1).x / s;
     if (threadIdx.x == 0 && blockIdx.x == 0 && a.energy) a.energy[0] = E;
@@ -263,6 +274,12 @@ __global__ void post_grad_kernel(qgt_dev_post_args_t a)
 __global__ void __launch_bounds__(1024) cholesky_kernel(const double* A, int cplx, const double* b, int P,
                                                         double lambda, double* L, double* x, double* status)
 {
+    // one system per CTA (batched solves: system blockIdx.x)
+    A += (int64_t)blockIdx.x * P * P * (cplx ? 2 : 1);
+    b += (int64_t)blockIdx.x * P;
+    L += (int64_t)blockIdx.x * P * P;
+    x += (int64_t)blockIdx.x * P;
+    status += 2 * blockIdx.x;
     __shared__ int fail;
     __shared__ double red[32];
     double lam = lambda;
@@ -339,38 +356,47 @@ __global__ void __launch_bounds__(1024) cholesky_kernel(const double* A, int cpl
 
 extern "C" {
 
-int qgt_dev_prepare(const qgt_dev_coef_desc_t* d, int32_t ncoef, const double* theta, double* coef, void* s)
+int qgt_dev_prepare(const qgt_dev_coef_desc_t* d, int32_t ncoef, const double* theta, double* coef, int32_t npoints,
+                    int32_t theta_stride, void* s)
 {
     if (ncoef <= 0) return QGT_OK;
-    prepare_kernel<<<(ncoef + 127) / 128, 128, 0, (cudaStream_t)s>>>(d, ncoef, theta, coef);
+    if (npoints < 1 || npoints > 65535) return qgt_set_error(QGT_EINVAL, "prepare: %d points", npoints);
+    prepare_kernel<<<dim3((ncoef + 127) / 128, npoints), 128, 0, (cudaStream_t)s>>>(d, ncoef, theta, coef, theta_stride);
     return qgt_dev_last_error();
 }
 
 int qgt_dev_tfim(const void* psi, void* out, int32_t n, double J, double h, double inv, int fp64,
                  void* split, int64_t sld, int64_t pstride, int32_t srow, float sscale, int32_t bf16,
-                 uint32_t* rowmax, void* s)
+                 uint32_t* rowmax, int32_t npoints, int64_t point_stride, int32_t rowmax_stride, void* s)
 {
     int64_t N = (int64_t)1 << n;
+    if (npoints < 1 || npoints > 65535 || (split && npoints > 1)) return qgt_set_error(QGT_EINVAL, "tfim: %d points", npoints);
+    int64_t want = (152 * 16 + npoints - 1) / npoints;
     int blocks = (int)((N + 255) / 256);
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > want) blocks = (int)want;
+    dim3 grid((unsigned)blocks, (unsigned)npoints);
     if (fp64)
-        tfim_kernel<double2, double><<<blocks, 256, 0, (cudaStream_t)s>>>((const double2*)psi, (double2*)out, n, J, h,
-                                                                            inv, NULL, 0, 0, 0, 0.f, 0, NULL);
+        tfim_kernel<double2, double><<<grid, 256, 0, (cudaStream_t)s>>>((const double2*)psi, (double2*)out, n, J, h,
+                                                                          inv, NULL, 0, 0, 0, 0.f, 0, NULL, point_stride,
+                                                                          0);
     else
-        tfim_kernel<float2, float><<<blocks, 256, 0, (cudaStream_t)s>>>((const float2*)psi, (float2*)out, n, (float)J,
-                                                                          (float)h, (float)inv, split, sld, pstride, srow,
-                                                                          sscale, bf16, rowmax);
+        tfim_kernel<float2, float><<<grid, 256, 0, (cudaStream_t)s>>>((const float2*)psi, (float2*)out, n, (float)J,
+                                                                        (float)h, (float)inv, split, sld, pstride, srow,
+                                                                        sscale, bf16, rowmax, point_stride,
+                                                                        rowmax_stride);
     return qgt_dev_last_error();
 }
 
 int qgt_dev_post(const qgt_dev_post_args_t* a, void* s)
 {
     int64_t PP = (int64_t)a->P * a->P;
-    post_qgt_kernel<<<(unsigned)((PP + 255) / 256), 256, 0, (cudaStream_t)s>>>(*a);
+    const int np = a->npoints > 0 ? a->npoints : 1;
+    if (np > 65535) return qgt_set_error(QGT_EINVAL, "post: %d points", np);
+    post_qgt_kernel<<<dim3((unsigned)((PP + 255) / 256), np), 256, 0, (cudaStream_t)s>>>(*a);
     int rc = qgt_dev_last_error();
     if (rc) return rc;
     if (a->has_h) {
-        post_grad_kernel<<<(a->P + 255) / 256, 256, 0, (cudaStream_t)s>>>(*a);
+        post_grad_kernel<<<dim3((a->P + 255) / 256, np), 256, 0, (cudaStream_t)s>>>(*a);
         rc = qgt_dev_last_error();
     }
     return rc;
@@ -381,6 +407,14 @@ int qgt_dev_cholesky(const double* A, int cplx, const double* b, int32_t P, doub
 {
     if (P <= 0) return qgt_set_error(QGT_EINVAL, "cholesky: P must be positive");
     cholesky_kernel<<<1, 1024, 0, (cudaStream_t)s>>>(A, cplx, b, P, lambda, work, x, status);
+    return qgt_dev_last_error();
+}
+
+int qgt_dev_cholesky_batch(const double* A, int cplx, const double* b, int32_t P, double lambda, double* work,
+                           double* x, double* status, int32_t nsys, void* s)
+{
+    if (P <= 0 || nsys < 1 || nsys > 0x7fffffff) return qgt_set_error(QGT_EINVAL, "cholesky: bad batch");
+    cholesky_kernel<<<nsys, 1024, 0, (cudaStream_t)s>>>(A, cplx, b, P, lambda, work, x, status);
     return qgt_dev_last_error();
 }
 
@@ -479,6 +513,11 @@ int qgt_dev_event_create(void** ev)
 }
 int qgt_dev_event_destroy(void* ev) { if (ev) CK(cudaEventDestroy((cudaEvent_t)ev), "cudaEventDestroy"); return QGT_OK; }
 int qgt_dev_event_record(void* ev, void* s) { CK(cudaEventRecord((cudaEvent_t)ev, (cudaStream_t)s), "cudaEventRecord"); return QGT_OK; }
+int qgt_dev_stream_wait_event(void* s, void* ev)
+{
+    CK(cudaStreamWaitEvent((cudaStream_t)s, (cudaEvent_t)ev, 0), "cudaStreamWaitEvent");
+    return QGT_OK;
+}
 int qgt_dev_event_elapsed(void* a, void* b, float* ms)
 {
     CK(cudaEventSynchronize((cudaEvent_t)b), "cudaEventSynchronize");
@@ -498,11 +537,14 @@ int qgt_dev_event_elapsed(void* a, void* b, float* ms)
 // ~1e-10 instead of ~6e-8.  Diagonal fixed gates get equal-modulus entries.
 // One warp per coefficient; 8 floats per coefficient (2x2 complex, row-major).
 // ---------------------------------------------------------------------------
-__global__ void prepare32_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const double* theta, float* coef)
+__global__ void prepare32_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const double* theta, float* coef,
+                                 int theta_stride)
 {
     const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (c >= ncoef) return;
+    theta += (int64_t)blockIdx.y * theta_stride;   // parameter point
+    coef += (int64_t)8 * blockIdx.y * ncoef;
     qgt_dev_coef_desc_t g = d[c];
     float m[8] = {1.f, 0.f, 0.f, 0.f, 0.f, 0.f, 1.f, 0.f};
     if (g.type == QGT_GATE_RX || g.type == QGT_GATE_RY || g.type == QGT_GATE_RZ) {
@@ -541,9 +583,11 @@ __global__ void prepare32_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const 
     if (lane < 8) coef[8 * c + lane] = m[lane];
 }
 
-extern "C" int qgt_dev_prepare32(const qgt_dev_coef_desc_t* d, int32_t ncoef, const double* theta, float* coef, void* s)
+extern "C" int qgt_dev_prepare32(const qgt_dev_coef_desc_t* d, int32_t ncoef, const double* theta, float* coef,
+                                 int32_t npoints, int32_t theta_stride, void* s)
 {
     if (ncoef <= 0) return QGT_OK;
-    prepare32_kernel<<<(ncoef + 7) / 8, 256, 0, (cudaStream_t)s>>>(d, ncoef, theta, coef);
+    if (npoints < 1 || npoints > 65535) return qgt_set_error(QGT_EINVAL, "prepare32: %d points", npoints);
+    prepare32_kernel<<<dim3((ncoef + 7) / 8, npoints), 256, 0, (cudaStream_t)s>>>(d, ncoef, theta, coef, theta_stride);
     return qgt_dev_last_error();
 }

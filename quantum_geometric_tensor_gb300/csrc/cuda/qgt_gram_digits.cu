@@ -11,13 +11,15 @@
 // FP16 residual leaves ~1e-6 relative error in Q on real derivative states,
 // where the representation errors of rows with equal magnitudes coincide).  The D*D' products are
 // integers and every partial sum of them over a CTA's K range is at most
-// 2^23 (Cauchy-Schwarz; M is chosen per plan from the K range, M = 32 for
-// 4096 amplitudes, up to 1024 for short ranges), so their FP32 tensor
-// accumulation is EXACT.  The D*l1', l1*D', l1*l1', D*l2', l2*D' terms (a few
+// 2^23 (Cauchy-Schwarz; M is chosen per plan from the K range, M = 64 for
+// 1024 amplitudes, up to 1024 for short ranges), so their FP32 tensor
+// accumulation is EXACT.  K ranges stay at <= 1024 amplitudes: the residual
+// accumulator's truncating FP32 chain over 4096 amplitudes left 9.7e-7 of
+// relative metric error at 20 qubits, over 1024 it leaves 1.2e-7.  The D*l1', l1*D', l1*l1', D*l2', l2*D' terms (a few
 // percent of the total) accumulate in a second TMEM accumulator; their
 // rounding is ~1e-8 relative to the sum.
 //
-// Data path per CTA (tile pair mb <= nb, K range of <= 4096 amplitudes):
+// Data path per CTA (tile pair mb <= nb, K range of <= 1024 amplitudes):
 //   TMA: 128 rows x 16 amplitudes of complex64 per row block -> raw smem
 //   8 converter warps: raw -> 6 FP16 planes {Re D, Re l1, Re l2, Im D, Im l1,
 //                      Im l2} in the SWIZZLE_32B K-major UMMA layout
@@ -47,7 +49,7 @@
 #define DG_CONV_WARPS 8
 #define DG_THREADS (64 + 32 * DG_CONV_WARPS)
 #define DG_SMEM_BYTES (DG_RAW_STAGES * 2 * DG_RAW_BYTES + DG_PL_STAGES * 12 * DG_PLANE_BYTES + 1024)
-#define DG_KMAX 4096                                // amplitudes per CTA (exactness bound)
+#define DG_KMAX 1024                                // amplitudes per CTA (exactness bound; shorter FP32 chains)
 #define DG_TIMEOUT_NS 4000000000ull
 #define DG_ERR_TIMEOUT (-13)
 #define DG_ERR_INEXACT (-24)
@@ -56,7 +58,7 @@ struct qgt_dg_gram {
     CUtensorMap tmap;
     const void* V;
     int64_t N;
-    int rows, nbk, ntp, nsplit;
+    int rows, nbk, ntp, nsplit, npoints;
     int64_t kchunk;
     int mbits;                 /* digits D in [-2^mbits, 2^mbits] */
     const uint32_t* rowmax;
@@ -104,11 +106,12 @@ static __device__ __forceinline__ bool bar_wait(uint32_t b, uint32_t parity, uin
     }
 }
 
-static __device__ __forceinline__ void tma_2d(uint32_t dst, const CUtensorMap* m, int c0, int c1, uint32_t bar)
+// 3D box {32 floats, 128 rows, 1 point}: coordinates (float index, row, point)
+static __device__ __forceinline__ void tma_3d(uint32_t dst, const CUtensorMap* m, int c0, int c1, int c2, uint32_t bar)
 {
     asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
-        "l"((uint64_t)m), "r"(c0), "r"(c1), "r"(bar)
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+        "l"((uint64_t)m), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
         : "memory");
 }
 
@@ -209,14 +212,17 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
     uint8_t* pl_base = sb + DG_RAW_STAGES * 2 * DG_RAW_BYTES;       // DG_PL_STAGES x 2 blocks x 6 planes x 4 KiB
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int mb, nbo;
-    pair_of(blockIdx.x, nbk, &mb, &nbo);
+    const int ntp = nbk * (nbk + 1) / 2;   // blockIdx.x = K range x ntp + tile pair
+    pair_of((int)(blockIdx.x % ntp), nbk, &mb, &nbo);
     const bool diag = (mb == nbo);
     const int nblk = diag ? 1 : 2;
-    const int64_t k0 = (int64_t)blockIdx.y * kchunk;
+    const int64_t k0 = (int64_t)(blockIdx.x / ntp) * kchunk;
     int64_t k1 = k0 + kchunk;
     if (k1 > N) k1 = N;
     const int nk = (int)((k1 - k0) / DG_BK);
     const uint64_t deadline = gtimer() + DG_TIMEOUT_NS;
+    rowmax += (int64_t)blockIdx.z * rows;   // parameter point
+    part += (int64_t)blockIdx.z * gridDim.x * (2 * 128 * 128);
 
     if (threadIdx.x < 128) {
         for (int b = 0; b < 2; b++) {
@@ -266,8 +272,8 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
             const uint32_t fb = smem_u32(&raw_full[s]);
             bar_expect_tx(fb, bytes);
             const int x = (int)(2 * (k0 + (int64_t)kt * DG_BK));  // float index
-            tma_2d(st, &tmap, x, mb * 128, fb);
-            if (!diag) tma_2d(st + DG_RAW_BYTES, &tmap, x, nbo * 128, fb);
+            tma_3d(st, &tmap, x, mb * 128, (int)blockIdx.z, fb);
+            if (!diag) tma_3d(st + DG_RAW_BYTES, &tmap, x, nbo * 128, (int)blockIdx.z, fb);
             issued = kt + 1;
         }
         for (int u = issued - DG_RAW_STAGES; u < issued; u++)
@@ -340,7 +346,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
         }
         // ---------- epilogue: warps 2..9; lane quadrant = warp & 3, column half = (warp - 2) / 4 ----------
         const bool ok = nk > 0 && !abort_sh && bar_wait(smem_u32(&done_bar), 0, deadline);
-        float* out = part + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * (2 * 128 * 128);
+        float* out = part + (int64_t)blockIdx.x * (2 * 128 * 128);
         const int quad = warp & 3, half = (warp - 2) >> 2;
         const int row = quad * 32 + lane;
         if (ok) {
@@ -379,6 +385,9 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
 __global__ void dg_reduce_kernel(const float* __restrict__ part, const uint32_t* __restrict__ rowmax, int rows, int nbk,
                                  int ntp, int nsplit, int mbits, double2* __restrict__ HG)
 {
+    part += (int64_t)blockIdx.y * nsplit * ntp * (2 * 128 * 128);   // parameter point
+    rowmax += (int64_t)blockIdx.y * rows;
+    HG += (int64_t)blockIdx.y * rows * rows;
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= (int64_t)rows * rows) return;
     int i = (int)(idx / rows), j = (int)(idx % rows);
@@ -410,11 +419,14 @@ static PFN_cuTensorMapEncodeTiled_v12000 dg_encode(void)
     return fn;
 }
 
-extern "C" int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, const uint32_t* rowmax, qgt_dg_gram_t** out)
+extern "C" int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, const uint32_t* rowmax, int32_t npoints,
+                                      int32_t point_rows, qgt_dg_gram_t** out)
 {
     *out = NULL;
     if (N % DG_BK || rows < 1 || ((uintptr_t)V & 15))
         return qgt_set_error(-1, "digit gram: row length %lld must be a multiple of %d", (long long)N, DG_BK);
+    if (npoints < 1 || npoints > 65535 || point_rows < rows)
+        return qgt_set_error(-1, "digit gram: %d points of %d rows (stride %d rows)", npoints, rows, point_rows);
     if (2 * N > 0x7fffffffLL) return qgt_set_error(-1, "digit gram: row length too large for TMA coordinates");
     PFN_cuTensorMapEncodeTiled_v12000 enc = dg_encode();
     if (!enc) return qgt_set_error(-6, "digit gram: cuTensorMapEncodeTiled unavailable");
@@ -424,15 +436,20 @@ extern "C" int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, co
     g->N = N;
     g->rows = rows;
     g->rowmax = rowmax;
+    g->npoints = npoints;
     int rows_pad = (rows + 127) / 128 * 128;
     g->nbk = rows_pad / 128;
     g->ntp = g->nbk * (g->nbk + 1) / 2;
     /* K per CTA: at most DG_KMAX (exactness), and enough CTAs to fill the GPU */
     int64_t kc = DG_KMAX;
     int64_t want = (2 * 152 + g->ntp - 1) / g->ntp;
-    while (kc > 4 * DG_BK && (N + kc - 1) / kc < want) kc /= 2;
+    while (kc > 4 * DG_BK && (N + kc - 1) / kc * npoints < want) kc /= 2;
     g->kchunk = kc;
     g->nsplit = (int)((N + kc - 1) / kc);
+    if ((int64_t)g->ntp * g->nsplit > 0x7fffffffLL) {
+        free(g);
+        return qgt_set_error(-1, "digit gram: %d tile pairs x %d K ranges exceed the grid", g->ntp, g->nsplit);
+    }
     /* widest digits whose products sum exactly over kc amplitudes:
      * kc (M^2 + sqrt(2) M + 1/2) <= 2^23 with M = 2^mbits, |D_re|^2 + |D_im|^2 bounded through |x| < M u;
      * M <= 1024 keeps D exact in FP16 */
@@ -442,18 +459,19 @@ extern "C" int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, co
         if ((double)kc * (M * M + 1.4143 * M + 0.5) <= 8388608.0) break;
         g->mbits--;
     }
-    cuuint64_t dims[2] = {(cuuint64_t)(2 * N), (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)(2 * N * 4)};
-    cuuint32_t box[2] = {2 * DG_BK, 128};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(&g->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)V, dims, strides, box, estr,
+    /* rows past `rows` inside a point read as zeros (out-of-bounds fill) */
+    cuuint64_t dims[3] = {(cuuint64_t)(2 * N), (cuuint64_t)rows, (cuuint64_t)npoints};
+    cuuint64_t strides[2] = {(cuuint64_t)(2 * N * 4), (cuuint64_t)(2 * N * 4) * (cuuint64_t)point_rows};
+    cuuint32_t box[3] = {2 * DG_BK, 128, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(&g->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)V, dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         free(g);
         return qgt_set_error(-6, "digit gram: cuTensorMapEncodeTiled failed (%d)", (int)r);
     }
-    size_t pbytes = (size_t)g->nsplit * g->ntp * 2 * 128 * 128 * sizeof(float);
+    size_t pbytes = (size_t)npoints * g->nsplit * g->ntp * 2 * 128 * 128 * sizeof(float);
     cudaError_t e = cudaMalloc((void**)&g->part, pbytes);
     if (e == cudaSuccess) e = cudaMalloc((void**)&g->err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(g->err, 0, sizeof(int));
@@ -472,12 +490,12 @@ extern "C" int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, co
 extern "C" int qgt_dev_dg_gram_run(qgt_dg_gram_t* g, double* HG, void* stream)
 {
     cudaStream_t s = (cudaStream_t)stream;
-    dg_gram_kernel<<<dim3(g->ntp, g->nsplit), DG_THREADS, DG_SMEM_BYTES, s>>>(g->tmap, g->nbk, g->N, g->kchunk, g->rowmax,
+    dg_gram_kernel<<<dim3((unsigned)(g->ntp * g->nsplit), 1, g->npoints), DG_THREADS, DG_SMEM_BYTES, s>>>(g->tmap, g->nbk, g->N, g->kchunk, g->rowmax,
                                                                        g->rows, g->mbits, g->part, g->err);
     int rc = qgt_dev_last_error();
     if (rc) return rc;
     int64_t cnt = (int64_t)g->rows * g->rows;
-    dg_reduce_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>(g->part, g->rowmax, g->rows, g->nbk, g->ntp, g->nsplit,
+    dg_reduce_kernel<<<dim3((unsigned)((cnt + 255) / 256), g->npoints), 256, 0, s>>>(g->part, g->rowmax, g->rows, g->nbk, g->ntp, g->nsplit,
                                                                    g->mbits, (double2*)HG);
     return qgt_dev_last_error();
 }
@@ -501,7 +519,7 @@ extern "C" void qgt_dev_dg_gram_destroy(qgt_dg_gram_t* g)
 
 extern "C" int64_t qgt_dev_dg_gram_scratch_bytes(const qgt_dg_gram_t* g)
 {
-    return g ? (int64_t)g->nsplit * g->ntp * 2 * 128 * 128 * (int64_t)sizeof(float) : 0;
+    return g ? (int64_t)g->npoints * g->nsplit * g->ntp * 2 * 128 * 128 * (int64_t)sizeof(float) : 0;
 }
 
 extern "C" void qgt_dev_dg_gram_shape(const qgt_dg_gram_t* g, int* ntp, int* nsplit, int64_t* kchunk)

@@ -25,8 +25,10 @@ __device__ __forceinline__ void tile_pair_index(int tp, int nt, int* ti, int* tj
 }
 
 __global__ void __launch_bounds__(256) gram_f64_kernel(const double2* __restrict__ V, int64_t N, int rows, int nt,
-                                                       int64_t kchunk, double2* __restrict__ part)
+                                                       int64_t kchunk, double2* __restrict__ part, int64_t point_stride)
 {
+    V += blockIdx.z * point_stride;   // parameter point
+    part += (int64_t)blockIdx.z * gridDim.y * gridDim.x * (GT * GT);
     __shared__ double2 As[KT][GT + 1];
     __shared__ double2 Bs[KT][GT + 1];
     int ti, tj;
@@ -74,6 +76,8 @@ __global__ void __launch_bounds__(256) gram_f64_kernel(const double2* __restrict
 __global__ void gram_f64_reduce_kernel(const double2* __restrict__ part, int rows, int nt, int ntp, int nsplit,
                                        double2* __restrict__ HG)
 {
+    part += (int64_t)blockIdx.y * nsplit * ntp * (GT * GT);
+    HG += (int64_t)blockIdx.y * rows * rows;
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= (int64_t)rows * rows) return;
     int i = (int)(idx / rows), j = (int)(idx % rows);
@@ -92,19 +96,122 @@ __global__ void gram_f64_reduce_kernel(const double2* __restrict__ part, int row
 }
 
 extern "C" int qgt_dev_gram_f64(const void* V, int64_t N, int32_t rows, double* part, int32_t nsplit, double* HG,
-                                void* stream)
+                                int32_t npoints, int64_t point_stride, void* stream)
 {
+    if (npoints < 1 || npoints > 65535) return qgt_set_error(-1, "gram_f64: %d points", npoints);
     int nt = (rows + GT - 1) / GT;
     int ntp = nt * (nt + 1) / 2;
     int64_t kchunk = (N + nsplit - 1) / nsplit;
     kchunk = (kchunk + KT - 1) / KT * KT;
     int ns = (int)((N + kchunk - 1) / kchunk);
     cudaStream_t s = (cudaStream_t)stream;
-    gram_f64_kernel<<<dim3(ntp, ns), 256, 0, s>>>((const double2*)V, N, rows, nt, kchunk, (double2*)part);
+    gram_f64_kernel<<<dim3(ntp, ns, npoints), 256, 0, s>>>((const double2*)V, N, rows, nt, kchunk, (double2*)part,
+                                                           point_stride);
     int rc = qgt_dev_last_error();
     if (rc) return rc;
     int64_t cnt = (int64_t)rows * rows;
-    gram_f64_reduce_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>((const double2*)part, rows, nt, ntp, ns,
-                                                                         (double2*)HG);
+    gram_f64_reduce_kernel<<<dim3((unsigned)((cnt + 255) / 256), npoints), 256, 0, s>>>((const double2*)part, rows, nt,
+                                                                                        ntp, ns, (double2*)HG);
+    return qgt_dev_last_error();
+}
+
+// ---------------------------------------------------------------------------
+// Small Gram: rows <= 8 (a few vectors per point, e.g. psi and two derivative
+// slots of a Berry-curvature point).  Memory-bound: every thread reads its
+// amplitudes of all rows once and keeps the rows (rows + 1) / 2 products in
+// FP64 registers (complex64 inputs multiply exactly in FP64).  Block sums go
+// to part[point][split][pair]; a second kernel adds the splits and writes the
+// Hermitian HG of each point.
+// ---------------------------------------------------------------------------
+template <typename T, int ROWS>
+__global__ void __launch_bounds__(256) gram_small_kernel(const T* __restrict__ V, int64_t N, int64_t point_stride,
+                                                         double2* __restrict__ part)
+{
+    constexpr int NP = ROWS * (ROWS + 1) / 2;
+    __shared__ double2 red[8][NP];
+    V += blockIdx.y * point_stride;
+    double2 acc[NP];
+#pragma unroll
+    for (int p = 0; p < NP; p++) acc[p] = make_double2(0, 0);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < N; k += (int64_t)gridDim.x * blockDim.x) {
+        double xr[ROWS], xi[ROWS];
+#pragma unroll
+        for (int r = 0; r < ROWS; r++) {
+            T v = V[(int64_t)r * N + k];
+            xr[r] = (double)v.x;
+            xi[r] = (double)v.y;
+        }
+        int p = 0;
+#pragma unroll
+        for (int i = 0; i < ROWS; i++)
+#pragma unroll
+            for (int j = i; j < ROWS; j++, p++) {
+                // conj(x_i) x_j
+                acc[p].x += xr[i] * xr[j] + xi[i] * xi[j];
+                acc[p].y += xr[i] * xi[j] - xi[i] * xr[j];
+            }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int p = 0; p < NP; p++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            acc[p].x += __shfl_xor_sync(0xffffffffu, acc[p].x, o);
+            acc[p].y += __shfl_xor_sync(0xffffffffu, acc[p].y, o);
+        }
+        if (lane == 0) red[warp][p] = acc[p];
+    }
+    __syncthreads();
+    if (threadIdx.x < NP) {
+        double2 s = make_double2(0, 0);
+        for (int w = 0; w < 8; w++) { s.x += red[w][threadIdx.x].x; s.y += red[w][threadIdx.x].y; }
+        part[((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * NP + threadIdx.x] = s;
+    }
+}
+
+__global__ void gram_small_reduce_kernel(const double2* __restrict__ part, int rows, int nsplit, double2* __restrict__ HG)
+{
+    const int np = rows * (rows + 1) / 2;
+    const int p = threadIdx.x;
+    if (p >= np) return;
+    part += (int64_t)blockIdx.x * nsplit * np;
+    HG += (int64_t)blockIdx.x * rows * rows;
+    int i = 0, rem = p;
+    while (rem >= rows - i) { rem -= rows - i; i++; }
+    const int j = i + rem;
+    double2 s = make_double2(0, 0);
+    for (int sp = 0; sp < nsplit; sp++) { s.x += part[(int64_t)sp * np + p].x; s.y += part[(int64_t)sp * np + p].y; }
+    HG[(int64_t)i * rows + j] = s;
+    HG[(int64_t)j * rows + i] = make_double2(s.x, -s.y);
+}
+
+template <typename T>
+static void gram_small_launch(const void* V, int64_t N, int rows, int nsplit, double2* part, int npoints, int64_t ps,
+                              cudaStream_t s)
+{
+    dim3 g((unsigned)nsplit, (unsigned)npoints);
+    const T* v = (const T*)V;
+    switch (rows) {
+    case 1: gram_small_kernel<T, 1><<<g, 256, 0, s>>>(v, N, ps, part); break;
+    case 2: gram_small_kernel<T, 2><<<g, 256, 0, s>>>(v, N, ps, part); break;
+    case 3: gram_small_kernel<T, 3><<<g, 256, 0, s>>>(v, N, ps, part); break;
+    case 4: gram_small_kernel<T, 4><<<g, 256, 0, s>>>(v, N, ps, part); break;
+    case 5: gram_small_kernel<T, 5><<<g, 256, 0, s>>>(v, N, ps, part); break;
+    case 6: gram_small_kernel<T, 6><<<g, 256, 0, s>>>(v, N, ps, part); break;
+    case 7: gram_small_kernel<T, 7><<<g, 256, 0, s>>>(v, N, ps, part); break;
+    default: gram_small_kernel<T, 8><<<g, 256, 0, s>>>(v, N, ps, part); break;
+    }
+}
+
+extern "C" int qgt_dev_gram_small(const void* V, int64_t N, int32_t rows, int32_t fp64, double* part, int32_t nsplit,
+                                  double* HG, int32_t npoints, int64_t point_stride, void* stream)
+{
+    if (rows < 1 || rows > 8 || nsplit < 1 || nsplit > 65535 || npoints < 1 || npoints > 65535)
+        return qgt_set_error(-1, "gram_small: %d rows, %d splits, %d points", rows, nsplit, npoints);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (fp64) gram_small_launch<double2>(V, N, rows, nsplit, (double2*)part, npoints, point_stride, s);
+    else gram_small_launch<float2>(V, N, rows, nsplit, (double2*)part, npoints, point_stride, s);
+    int rc = qgt_dev_last_error();
+    if (rc) return rc;
+    gram_small_reduce_kernel<<<npoints, 64, 0, s>>>((const double2*)part, rows, nsplit, (double2*)HG);
     return qgt_dev_last_error();
 }

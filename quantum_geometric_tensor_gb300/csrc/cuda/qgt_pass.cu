@@ -217,6 +217,8 @@ __global__ void __launch_bounds__(QGT_PASS_THREADS) pass_kernel(const qgt_dev_pa
     const int t = a.tile_bits, TS = 1 << t;
     if (threadIdx.x < 16) l2p[threadIdx.x] = a.local_to_phys[threadIdx.x];
     const qgt_dev_entry_t e = a.entries[blockIdx.y];
+    const int pt = blockIdx.z;
+    const double* coef = a.coef + (int64_t)8 * pt * a.coef_stride;
     // physical base of this tile: scatter blockIdx.x over the qubits outside S
     uint64_t base = 0;
     {
@@ -225,7 +227,7 @@ __global__ void __launch_bounds__(QGT_PASS_THREADS) pass_kernel(const qgt_dev_pa
             if (!((a.tile_mask >> q) & 1)) { base |= (uint64_t)(rest & 1u) << q; rest >>= 1; }
     }
     __syncthreads();
-    const T* src = reinterpret_cast<const T*>(a.V) + (int64_t)e.src_row * a.N;
+    const T* src = reinterpret_cast<const T*>(a.V) + pt * a.point_stride + (int64_t)e.src_row * a.N;
     for (int l = threadIdx.x; l < TS; l += blockDim.x) {
         uint64_t ph = base | scatter_local(l, t, l2p);
         T v;
@@ -236,14 +238,14 @@ __global__ void __launch_bounds__(QGT_PASS_THREADS) pass_kernel(const qgt_dev_pa
     __syncthreads();
     for (int j = 0; j < a.nops; j++) {
         qgt_dev_op_t op = a.ops[j];
-        apply_op<R>(op, a.coef, tile, TS, base);
+        apply_op<R>(op, coef, tile, TS, base);
         __syncthreads();
         if (j == e.spawn_op) {
             apply_generator<R>(op, tile, TS, base);
             __syncthreads();
         }
     }
-    T* dst = reinterpret_cast<T*>(a.V) + (int64_t)e.dst_row * a.N;
+    T* dst = reinterpret_cast<T*>(a.V) + pt * a.point_stride + (int64_t)e.dst_row * a.N;
     float vmax = 0.f;
     for (int l = threadIdx.x; l < TS; l += blockDim.x) {
         uint64_t ph = base | scatter_local(l, t, l2p);
@@ -280,7 +282,7 @@ __global__ void __launch_bounds__(QGT_PASS_THREADS) pass_kernel(const qgt_dev_pa
         if (threadIdx.x == 0) {
             float m = 0.f;
             for (int w = 0; w < (int)(blockDim.x >> 5); w++) m = fmaxf(m, red[w]);
-            atomicMax(a.rowmax + e.dst_row, __float_as_uint(m));
+            atomicMax(a.rowmax + (int64_t)pt * a.rowmax_stride + e.dst_row, __float_as_uint(m));
         }
     }
 }
@@ -290,9 +292,11 @@ extern "C" int qgt_dev_pass(const qgt_dev_pass_args_t* a, int fp64, void* stream
     if (a->nentries <= 0) return 0;
     int TS = 1 << a->tile_bits;
     int64_t ntiles = (int64_t)1 << (a->n - a->tile_bits);
-    if (a->nentries > 65535 || ntiles > 0x7fffffff)
-        return qgt_set_error(-1, "pass: %d entries / %lld tiles exceed the grid", a->nentries, (long long)ntiles);
-    dim3 grid((unsigned)ntiles, (unsigned)a->nentries);
+    const int np = a->npoints > 0 ? a->npoints : 1;
+    if (a->nentries > 65535 || ntiles > 0x7fffffff || np > 65535)
+        return qgt_set_error(-1, "pass: %d entries / %lld tiles / %d points exceed the grid", a->nentries,
+                             (long long)ntiles, np);
+    dim3 grid((unsigned)ntiles, (unsigned)a->nentries, (unsigned)np);
     size_t smem = (size_t)TS * (fp64 ? sizeof(double2) : sizeof(float2));
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaSuccess;

@@ -185,7 +185,8 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
     qgt_dev_op2_t* sops = reinterpret_cast<qgt_dev_op2_t*>(p2_smem + ((size_t)sizeof(T) << (5 + RB + 3)));
     R* scoef = reinterpret_cast<R*>(sops + a.nops);
     {
-        const R* ctab = (sizeof(R) == 4) ? reinterpret_cast<const R*>(a.coef32) : reinterpret_cast<const R*>(a.coef);
+        const R* ctab = ((sizeof(R) == 4) ? reinterpret_cast<const R*>(a.coef32) : reinterpret_cast<const R*>(a.coef)) +
+                        (int64_t)8 * blockIdx.z * a.coef_stride;
         for (int i = threadIdx.x; i < a.nops; i += blockDim.x) sops[i] = a.ops[i];
         for (int i = threadIdx.x; i < 8 * a.nops; i += blockDim.x) {
             const int c = a.ops[i >> 3].coef;
@@ -233,7 +234,7 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
     T v[NR];
     set_layout(sops[0].seg);
     {
-        const T* src = reinterpret_cast<const T*>(a.V) + (int64_t)e.src_row * a.N;
+        const T* src = reinterpret_cast<const T*>(a.V) + blockIdx.z * a.point_stride + (int64_t)e.src_row * a.N;
 #pragma unroll
         for (int j = 0; j < NR; j++) {
             const uint32_t ph = pidx(j);
@@ -345,7 +346,7 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
         }
     }
     // store
-    T* dst = reinterpret_cast<T*>(a.V) + (int64_t)e.dst_row * a.N;
+    T* dst = reinterpret_cast<T*>(a.V) + blockIdx.z * a.point_stride + (int64_t)e.dst_row * a.N;
     float vmax = 0.f;
 #pragma unroll
     for (int j = 0; j < NR; j++) {
@@ -372,7 +373,7 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
         if (threadIdx.x == 0) {
             float mx = 0.f;
             for (int w = 0; w < 8; w++) mx = fmaxf(mx, red[w]);
-            atomicMax(a.rowmax + e.dst_row, __float_as_uint(mx));
+            atomicMax(a.rowmax + (int64_t)blockIdx.z * a.rowmax_stride + e.dst_row, __float_as_uint(mx));
         }
     }
 }
@@ -383,8 +384,9 @@ extern "C" int qgt_dev_pass2(const qgt_dev_pass2_args_t* a, int fp64, void* stre
     const int tb = fp64 ? QGT_TILE_MAX_F64 : QGT_TILE_MAX_F32;
     if (a->tile_bits != tb) return qgt_set_error(-1, "pass2: tile of %d bits (needs %d)", a->tile_bits, tb);
     int64_t ntiles = (int64_t)1 << (a->n - a->tile_bits);
-    if (a->nentries > 65535 || ntiles > 0x7fffffff) return qgt_set_error(-1, "pass2: grid too large");
-    dim3 grid((unsigned)ntiles, (unsigned)a->nentries);
+    const int np = a->npoints > 0 ? a->npoints : 1;
+    if (a->nentries > 65535 || ntiles > 0x7fffffff || np > 65535) return qgt_set_error(-1, "pass2: grid too large");
+    dim3 grid((unsigned)ntiles, (unsigned)a->nentries, (unsigned)np);
     size_t smem = ((size_t)1 << (tb + (fp64 ? 4 : 3))) +                               /* 64 KiB tile */
                   (size_t)a->nops * (sizeof(qgt_dev_op2_t) + 8 * (fp64 ? sizeof(double) : sizeof(float)));
     if (smem > 112 * 1024) return qgt_set_error(-1, "pass2: program of %d ops too large", a->nops);

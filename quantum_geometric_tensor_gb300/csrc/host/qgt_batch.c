@@ -1,0 +1,367 @@
+/*
+ * qgt_batch.c -- ragged batches of circuits in one CUDA-graph launch.
+ *
+ * The reference evaluates circuits one at a time, each QGT element by its own
+ * network contractions (src/quantum_geometric/core/quantum_geometric_curvature.c:
+ * 289-320), and the Berry curvature pointwise from a 2 x 2 QGT
+ * (quantum_geometric_curvature.c:181-198).  Here a batch is compiled once:
+ *
+ *   - circuits with the same structure (qubits, gate list, fixed angles) form
+ *     a group and share ONE batched plan: the parameter point is a grid
+ *     dimension of every kernel, so a group costs one launch per kernel;
+ *   - a Berry map Omega_ab = Im Q_ab on a G x G lattice over [0, 2pi)^2 (the
+ *     other parameters at the circuit's theta) runs as a second batched plan
+ *     per (group, pair): the circuit truncated after the last gate of a or b,
+ *     parameters permuted so that a, b are derivative parameters 0, 1;
+ *   - all plans, with the uploads of theta and downloads of Q, are captured
+ *     into one CUDA graph over a few streams (independent groups overlap).
+ *
+ * Exact reduction used for the maps: when a and b each drive one gate and a's
+ * gate comes first, Q_ab does not depend on theta_b (R_b commutes with its
+ * generator and is unitary on both derivative states), so the lattice needs
+ * G points, one per theta_a, and column j repeats them; likewise with the
+ * roles swapped.  Parameters shared by several gates get all G^2 points.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../qgt_internal.h"
+#include "qgt_gb300.h"
+
+#define E_INVAL (-1)
+#define E_NOMEM (-2)
+#define MAX_STREAMS 16
+
+typedef struct {
+    int berry;              /* 0: full QGT plan, 1: Berry-map plan */
+    qgt_plan_t* plan;
+    int P, Pd;              /* theta width; output width */
+    int nmem, per;          /* circuits in the plan; points per circuit */
+    int* mem;               /* circuit indices */
+    int pa, pb;             /* Berry parameters (circuit numbering) */
+    int compact;            /* G points per circuit (exact reduction) instead of G^2 */
+    int early_is_a;         /* a's gate precedes b's */
+    int* perm;              /* circuit parameter k -> plan parameter perm[k] */
+    size_t th_off, out_off; /* doubles into the pinned staging buffers */
+} bplan_t;
+
+struct qgt_batch {
+    qgt_batch_options_t opt;
+    int count, G;
+    int* P;                 /* per circuit */
+    size_t *th_at, *q_at;   /* per circuit offsets into the caller's theta / Q arrays */
+    bplan_t* bp;
+    int nbp, ngroups, nberry;
+    double *th_pin, *out_pin;
+    size_t th_len, out_len;
+    int nstreams;
+    void* s[MAX_STREAMS];
+    void* ev[MAX_STREAMS + 1];
+    void* graph;
+    int nodes;
+    int64_t device_bytes;
+};
+
+void qgt_batch_default_options(qgt_batch_options_t* o)
+{
+    memset(o, 0, sizeof *o);
+    o->precision = QGT_PRECISION_MIXED;
+    o->berry_grid = 32;
+    o->device = 0;
+    o->streams = 4;
+}
+
+static int same_structure(const qgt_circuit_desc_t* a, const qgt_circuit_desc_t* b)
+{
+    if (a->num_qubits != b->num_qubits || a->num_gates != b->num_gates || a->num_params != b->num_params) return 0;
+    for (int g = 0; g < a->num_gates; g++) {
+        const qgt_gate_desc_t *x = &a->gates[g], *y = &b->gates[g];
+        if (x->type != y->type || x->qubits[0] != y->qubits[0] || x->param != y->param) return 0;
+        int two = x->type == QGT_GATE_CNOT || x->type == QGT_GATE_CZ || x->type == QGT_GATE_SWAP;
+        if (two && x->qubits[1] != y->qubits[1]) return 0;
+        if (x->param < 0 && memcmp(&x->angle, &y->angle, sizeof(double)) != 0) return 0;
+    }
+    return 1;
+}
+
+static int make_plan(const qgt_circuit_desc_t* c, const qgt_batch_options_t* bo, int batch, int Pd, qgt_plan_t** out)
+{
+    qgt_plan_options_t o;
+    qgt_plan_default_options(&o);
+    o.precision = bo->precision;
+    o.hamiltonian = QGT_HAMILTONIAN_NONE;
+    o.device = bo->device;
+    o.use_graph = 0;
+    o.batch = batch;
+    o.num_deriv_params = Pd;
+    return qgt_plan_create(c, &o, out);
+}
+
+void qgt_batch_destroy(qgt_batch_t* b)
+{
+    if (!b) return;
+    if (b->nstreams > 0 && b->s[0]) qgt_dev_stream_sync(b->s[0]);
+    qgt_dev_graph_destroy(b->graph);
+    for (int i = 0; i < b->nbp; i++) {
+        qgt_plan_destroy(b->bp[i].plan);
+        free(b->bp[i].mem);
+        free(b->bp[i].perm);
+    }
+    for (int k = 0; k < MAX_STREAMS; k++) if (b->s[k]) qgt_dev_stream_destroy(b->s[k]);
+    for (int k = 0; k <= MAX_STREAMS; k++) if (b->ev[k]) qgt_dev_event_destroy(b->ev[k]);
+    qgt_dev_host_free(b->th_pin);
+    qgt_dev_host_free(b->out_pin);
+    free(b->bp); free(b->P); free(b->th_at); free(b->q_at);
+    free(b);
+}
+
+int qgt_batch_create(const qgt_circuit_desc_t* circuits, int32_t count, const int32_t* berry_params,
+                     const qgt_batch_options_t* opt, qgt_batch_t** out)
+{
+    if (!out) return qgt_set_error(E_INVAL, "qgt_batch_create: NULL output");
+    *out = NULL;
+    if (!circuits || count < 1) return qgt_set_error(E_INVAL, "qgt_batch_create: no circuits");
+    qgt_batch_t* b = (qgt_batch_t*)calloc(1, sizeof *b);
+    if (!b) return qgt_set_error(E_NOMEM, "qgt_batch_create: out of memory");
+    if (opt) b->opt = *opt; else qgt_batch_default_options(&b->opt);
+    int rc = 0;
+    b->count = count;
+    b->G = b->opt.berry_grid;
+    if (b->G < 0 || b->G > 1024) { rc = qgt_set_error(E_INVAL, "qgt_batch_create: berry_grid %d outside [0, 1024]", b->G); goto fail; }
+    if (b->opt.precision != QGT_PRECISION_FP64 && b->opt.precision != QGT_PRECISION_MIXED) {
+        rc = qgt_set_error(E_INVAL, "qgt_batch_create: batches run FP64 or MIXED precision");
+        goto fail;
+    }
+    if (b->G > 0 && !berry_params) { rc = qgt_set_error(E_INVAL, "qgt_batch_create: berry_grid > 0 needs berry_params"); goto fail; }
+    b->nstreams = b->opt.streams < 1 ? 1 : (b->opt.streams > MAX_STREAMS ? MAX_STREAMS : b->opt.streams);
+    b->P = (int*)calloc((size_t)count, sizeof(int));
+    b->th_at = (size_t*)calloc((size_t)count + 1, sizeof(size_t));
+    b->q_at = (size_t*)calloc((size_t)count + 1, sizeof(size_t));
+    int* group = (int*)malloc(sizeof(int) * (size_t)count);
+    int* rep = (int*)malloc(sizeof(int) * (size_t)count);
+    b->bp = (bplan_t*)calloc(2 * (size_t)count, sizeof(bplan_t));
+    if (!b->P || !b->th_at || !b->q_at || !group || !rep || !b->bp) {
+        free(group); free(rep);
+        rc = qgt_set_error(E_NOMEM, "qgt_batch_create: out of memory");
+        goto fail;
+    }
+    for (int c = 0; c < count; c++) {
+        b->P[c] = circuits[c].num_params;
+        b->th_at[c + 1] = b->th_at[c] + (size_t)b->P[c];
+        b->q_at[c + 1] = b->q_at[c] + 2 * (size_t)b->P[c] * b->P[c];
+        if (b->G > 0) {
+            int pa = berry_params[2 * c], pb = berry_params[2 * c + 1];
+            if (pa < 0 || pb < 0 || pa >= b->P[c] || pb >= b->P[c] || pa == pb) {
+                free(group); free(rep);
+                rc = qgt_set_error(E_INVAL, "qgt_batch_create: circuit %d: Berry parameters (%d, %d) invalid", c, pa, pb);
+                goto fail;
+            }
+        }
+    }
+    /* structural groups */
+    int ng = 0;
+    for (int c = 0; c < count; c++) {
+        int g = -1;
+        for (int k = 0; k < ng && g < 0; k++)
+            if (same_structure(&circuits[rep[k]], &circuits[c])) g = k;
+        if (g < 0) { g = ng; rep[ng++] = c; }
+        group[c] = g;
+    }
+    b->ngroups = ng;
+    for (int g = 0; g < ng; g++) {
+        bplan_t* bp = &b->bp[b->nbp];
+        const qgt_circuit_desc_t* rc0 = &circuits[rep[g]];
+        bp->berry = 0;
+        bp->P = bp->Pd = rc0->num_params;
+        bp->per = 1;
+        bp->mem = (int*)malloc(sizeof(int) * (size_t)count);
+        if (!bp->mem) { free(group); free(rep); rc = qgt_set_error(E_NOMEM, "qgt_batch_create: oom"); goto fail; }
+        for (int c = 0; c < count; c++) if (group[c] == g) bp->mem[bp->nmem++] = c;
+        b->nbp++;
+        if ((rc = make_plan(rc0, &b->opt, bp->nmem, 0, &bp->plan)) != 0) { free(group); free(rep); goto fail; }
+    }
+    /* Berry plans: one per (group, parameter pair) */
+    if (b->G > 0) {
+        char* done = (char*)calloc((size_t)count, 1);
+        qgt_gate_desc_t* tg = NULL;
+        if (!done) { free(group); free(rep); rc = qgt_set_error(E_NOMEM, "qgt_batch_create: oom"); goto fail; }
+        for (int c = 0; c < count && !rc; c++) {
+            if (done[c]) continue;
+            const int pa = berry_params[2 * c], pb = berry_params[2 * c + 1];
+            const qgt_circuit_desc_t* cc = &circuits[c];
+            bplan_t* bp = &b->bp[b->nbp];
+            bp->berry = 1;
+            bp->pa = pa;
+            bp->pb = pb;
+            bp->P = cc->num_params;
+            bp->Pd = 2;
+            bp->mem = (int*)malloc(sizeof(int) * (size_t)count);
+            bp->perm = (int*)malloc(sizeof(int) * (size_t)cc->num_params);
+            tg = (qgt_gate_desc_t*)malloc(sizeof(qgt_gate_desc_t) * (size_t)(cc->num_gates + 1));
+            if (!bp->mem || !bp->perm || !tg) { rc = qgt_set_error(E_NOMEM, "qgt_batch_create: oom"); break; }
+            for (int d = c; d < count; d++)
+                if (!done[d] && group[d] == group[c] && berry_params[2 * d] == pa && berry_params[2 * d + 1] == pb) {
+                    bp->mem[bp->nmem++] = d;
+                    done[d] = 1;
+                }
+            b->nbp++;
+            int na = 0, nb = 0, ga = -1, gb = -1;
+            for (int g = 0; g < cc->num_gates; g++) {
+                if (cc->gates[g].param == pa) { na++; if (ga < 0) ga = g; }
+                if (cc->gates[g].param == pb) { nb++; if (gb < 0) gb = g; }
+            }
+            if (na == 0 || nb == 0) {
+                rc = qgt_set_error(E_INVAL, "qgt_batch_create: Berry parameter %d drives no gate", na == 0 ? pa : pb);
+                break;
+            }
+            int glast = -1;
+            for (int g = 0; g < cc->num_gates; g++)
+                if (cc->gates[g].param == pa || cc->gates[g].param == pb) glast = g;
+            bp->compact = (na == 1 && nb == 1);
+            bp->early_is_a = ga < gb;
+            bp->per = bp->compact ? b->G : b->G * b->G;
+            for (int k = 0, nxt = 2; k < cc->num_params; k++)
+                bp->perm[k] = (k == pa) ? 0 : (k == pb) ? 1 : nxt++;
+            for (int g = 0; g <= glast; g++) {
+                tg[g] = cc->gates[g];
+                if (tg[g].param >= 0) tg[g].param = bp->perm[tg[g].param];
+            }
+            qgt_circuit_desc_t tc = {cc->num_qubits, glast + 1, tg, cc->num_params};
+            if (bp->nmem * bp->per > 65535) {
+                rc = qgt_set_error(E_INVAL, "qgt_batch_create: %d Berry points in one group exceed 65535", bp->nmem * bp->per);
+                break;
+            }
+            rc = make_plan(&tc, &b->opt, bp->nmem * bp->per, 2, &bp->plan);
+            free(tg);
+            tg = NULL;
+            b->nberry++;
+        }
+        free(tg);
+        free(done);
+    }
+    free(group);
+    free(rep);
+    if (rc) goto fail;
+    /* pinned staging */
+    for (int i = 0; i < b->nbp; i++) {
+        bplan_t* bp = &b->bp[i];
+        const size_t pts = (size_t)bp->nmem * bp->per;
+        bp->th_off = b->th_len;
+        bp->out_off = b->out_len;
+        b->th_len += pts * (size_t)bp->P;
+        b->out_len += pts * 2 * (size_t)bp->Pd * bp->Pd;
+        qgt_plan_info_t in;
+        if (qgt_plan_get_info(bp->plan, &in) == 0) b->device_bytes += in.device_bytes;
+    }
+    if ((rc = qgt_dev_host_alloc((void**)&b->th_pin, sizeof(double) * (b->th_len + 1))) != 0) goto fail;
+    if ((rc = qgt_dev_host_alloc((void**)&b->out_pin, sizeof(double) * (b->out_len + 1))) != 0) goto fail;
+    memset(b->th_pin, 0, sizeof(double) * (b->th_len + 1));
+    for (int k = 0; k < b->nstreams; k++)
+        if ((rc = qgt_dev_stream_create(&b->s[k])) != 0) goto fail;
+    for (int k = 0; k <= b->nstreams; k++)
+        if ((rc = qgt_dev_event_create(&b->ev[k])) != 0) goto fail;
+    /* one graph: fork over the streams, per plan upload theta -> step -> download Q, join */
+    {
+        const int K = b->nstreams;
+        int cr = qgt_dev_graph_begin(b->s[0]);
+        if (!cr) cr = qgt_dev_event_record(b->ev[K], b->s[0]);
+        for (int k = 1; k < K && !cr; k++) cr = qgt_dev_stream_wait_event(b->s[k], b->ev[K]);
+        for (int i = 0; i < b->nbp && !cr; i++) {
+            bplan_t* bp = &b->bp[i];
+            void* st = b->s[i % K];
+            const size_t pts = (size_t)bp->nmem * bp->per;
+            if (bp->P > 0)
+                cr = qgt_dev_memcpy_h2d(qgt_plan_dev_theta(bp->plan), b->th_pin + bp->th_off,
+                                        sizeof(double) * pts * (size_t)bp->P, st);
+            if (!cr) cr = qgt_plan_enqueue_step(bp->plan, st);
+            if (!cr && bp->Pd > 0)
+                cr = qgt_dev_memcpy_d2h(b->out_pin + bp->out_off, qgt_plan_dev_Q(bp->plan),
+                                        sizeof(double) * pts * 2 * (size_t)bp->Pd * bp->Pd, st);
+            b->nodes += qgt_plan_launches(bp->plan) + 2;
+        }
+        for (int k = 1; k < K && !cr; k++) {
+            cr = qgt_dev_event_record(b->ev[k], b->s[k]);
+            if (!cr) cr = qgt_dev_stream_wait_event(b->s[0], b->ev[k]);
+        }
+        void* exec = NULL;
+        int re = qgt_dev_graph_end(b->s[0], &exec);
+        if (cr) { qgt_dev_graph_destroy(exec); rc = cr; goto fail; }
+        if (re) { rc = re; goto fail; }
+        b->graph = exec;
+    }
+    *out = b;
+    return 0;
+fail:
+    qgt_batch_destroy(b);
+    return rc ? rc : qgt_set_error(E_INVAL, "qgt_batch_create failed");
+}
+
+int qgt_batch_execute_host(qgt_batch_t* b, const double* theta, double* Q, double* berry)
+{
+    if (!b || !theta) return qgt_set_error(E_INVAL, "qgt_batch_execute_host: NULL argument");
+    if (berry && b->G == 0) return qgt_set_error(E_INVAL, "qgt_batch_execute_host: batch built without Berry maps");
+    for (size_t k = 0; k < b->th_at[b->count]; k++)
+        if (!isfinite(theta[k])) return qgt_set_error(E_INVAL, "qgt_batch_execute_host: theta[%zu] is not finite", k);
+    const double step = 2.0 * M_PI / (b->G > 0 ? b->G : 1);
+    for (int i = 0; i < b->nbp; i++) {
+        const bplan_t* bp = &b->bp[i];
+        for (int m = 0; m < bp->nmem; m++) {
+            const double* th = theta + b->th_at[bp->mem[m]];
+            for (int t = 0; t < bp->per; t++) {
+                double* dst = b->th_pin + bp->th_off + ((size_t)m * bp->per + t) * (size_t)bp->P;
+                if (!bp->berry) { memcpy(dst, th, sizeof(double) * (size_t)bp->P); continue; }
+                for (int k = 0; k < bp->P; k++) dst[bp->perm[k]] = th[k];
+                if (bp->compact) {
+                    dst[0] = bp->early_is_a ? step * t : 0.0;
+                    dst[1] = bp->early_is_a ? 0.0 : step * t;
+                } else {
+                    dst[0] = step * (t / b->G);
+                    dst[1] = step * (t % b->G);
+                }
+            }
+        }
+    }
+    int rc = qgt_dev_graph_launch(b->graph, b->s[0]);
+    if (!rc) rc = qgt_dev_stream_sync(b->s[0]);
+    if (rc) return rc;
+    for (int i = 0; i < b->nbp; i++) {
+        int st = qgt_plan_device_status(b->bp[i].plan, NULL);
+        if (st) return qgt_set_error(st, "qgt_batch_execute_host: plan %d reported device status %d", i, st);
+    }
+    const size_t G = (size_t)b->G;
+    for (int i = 0; i < b->nbp; i++) {
+        const bplan_t* bp = &b->bp[i];
+        const size_t blk = 2 * (size_t)bp->Pd * bp->Pd;
+        for (int m = 0; m < bp->nmem; m++) {
+            const int c = bp->mem[m];
+            const double* src = b->out_pin + bp->out_off + (size_t)m * bp->per * blk;
+            if (!bp->berry) {
+                if (Q) memcpy(Q + b->q_at[c], src, sizeof(double) * blk);
+                continue;
+            }
+            if (!berry) continue;
+            double* map = berry + (size_t)c * G * G;
+            /* Omega_ab = Im Q_01 of the 2 x 2 block (imaginary part at double index 3) */
+            for (size_t x = 0; x < G; x++)
+                for (size_t y = 0; y < G; y++) {
+                    size_t t = bp->compact ? (bp->early_is_a ? x : y) : x * G + y;
+                    map[x * G + y] = src[t * blk + 3];
+                }
+        }
+    }
+    return 0;
+}
+
+int qgt_batch_get_info(const qgt_batch_t* b, qgt_batch_info_t* info)
+{
+    if (!b || !info) return qgt_set_error(E_INVAL, "qgt_batch_get_info: NULL argument");
+    memset(info, 0, sizeof *info);
+    info->num_circuits = b->count;
+    info->num_groups = b->ngroups;
+    info->num_berry_plans = b->nberry;
+    info->graph_kernels = b->nodes;
+    info->device_bytes = b->device_bytes;
+    return 0;
+}

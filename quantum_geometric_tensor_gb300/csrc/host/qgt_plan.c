@@ -70,6 +70,9 @@ typedef struct {
 struct qgt_plan {
     qgt_plan_options_t opt;
     int n, P, nslots, rows, rows_pad;
+    int B;                        /* parameter points per step (theta batch) */
+    int Pd;                       /* parameters [0, Pd) get derivative rows; Q is Pd x Pd */
+    int64_t pstride;              /* amplitudes between points in V: (rows + 1) N */
     int64_t N, split_ld;
     int fp64;
     /* schedule */
@@ -106,6 +109,8 @@ struct qgt_plan {
     int part_nsplit;
     qgt_tc_gram_t* tc;            /* split-BF16 x3 Gram (operands written by the last pass) */
     qgt_dg_gram_t* dg;            /* integer-digit FP16 Gram (mixed default) */
+    double* small_part_d;         /* partials of the small Gram (rows <= 8) */
+    int small_nsplit;
     uint32_t* rowmax_d;           /* per-row max |amplitude| (float bits) for the digit Gram */
     double *Q_d, *grad_d, *energy_d, *natgrad_d, *chol_work_d, *status_d;
     int32_t *slot_param_d, *param_ptr_d, *param_slots_d;
@@ -309,7 +314,7 @@ static int build_entries(qgt_plan_t* p)
     if (!live) return qgt_set_error(E_NOMEM, "entries: oom");
     const int last = p->npasses - 1;
     const int split = p->opt.precision == QGT_PRECISION_MIXED_BF16X3;
-    const int rmax = p->opt.precision == QGT_PRECISION_MIXED ? QENT_ROWMAX : 0;
+    const int rmax = (p->opt.precision == QGT_PRECISION_MIXED && !p->small_nsplit) ? QENT_ROWMAX : 0;
     p->vector_passes = 0;
     p->gate_bytes = 0;
     const int64_t ab = p->fp64 ? 16 : 8; /* bytes per amplitude */
@@ -535,6 +540,17 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
     p->n = c->num_qubits;
     p->N = (int64_t)1 << p->n;
     p->P = c->num_params;
+    p->B = p->opt.batch > 0 ? p->opt.batch : 1;
+    p->Pd = p->opt.num_deriv_params > 0 ? p->opt.num_deriv_params : p->P;
+    if (p->B > 65535 || p->Pd > p->P || p->opt.batch < 0 || p->opt.num_deriv_params < 0) {
+        int b = p->opt.batch, d = p->opt.num_deriv_params;
+        free(p);
+        return qgt_set_error(E_INVAL, "qgt_plan_create: batch %d (max 65535) / num_deriv_params %d (max num_params)", b, d);
+    }
+    if (p->B > 1 && p->opt.precision == QGT_PRECISION_MIXED_BF16X3) {
+        free(p);
+        return qgt_set_error(E_INVAL, "qgt_plan_create: batched plans support FP64 and MIXED precision");
+    }
     p->fp64 = p->opt.precision == QGT_PRECISION_FP64;
     p->ngates = c->num_gates;
     p->gates = (sgate_t*)calloc((size_t)p->ngates + 1, sizeof(sgate_t));
@@ -544,7 +560,7 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
         if ((rc = classify(&c->gates[g], p->n, p->P, &p->gates[g])) != 0) goto fail;
         sgate_t* sg = &p->gates[g];
         int rot = sg->type == QGT_GATE_RX || sg->type == QGT_GATE_RY || sg->type == QGT_GATE_RZ;
-        if (rot && sg->param >= 0) sg->slot = p->nslots++;
+        if (rot && sg->param >= 0 && sg->param < p->Pd) sg->slot = p->nslots++;
         if (sg->type != QGT_GATE_CNOT && sg->type != QGT_GATE_CZ && sg->type != QGT_GATE_SWAP && sg->type != QGT_GATE_I) {
             sg->coef = p->ncoef;
             p->coef_h[p->ncoef].type = sg->type;
@@ -555,17 +571,19 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
     }
     p->rows = 2 + p->nslots;
     p->rows_pad = (p->rows + 127) / 128 * 128;
+    p->pstride = (int64_t)(p->rows + 1) * p->N;
+    p->small_nsplit = p->rows <= 8 ? 1 : 0;   /* few rows: memory-bound FP64 small Gram */
     p->split_ld = p->N < 32 ? 32 : p->N;
     /* slot -> param CSR */
     p->slot_param_h = (int32_t*)calloc((size_t)p->nslots + 1, sizeof(int32_t));
-    p->param_ptr_h = (int32_t*)calloc((size_t)p->P + 2, sizeof(int32_t));
+    p->param_ptr_h = (int32_t*)calloc((size_t)p->Pd + 2, sizeof(int32_t));
     p->param_slots_h = (int32_t*)calloc((size_t)p->nslots + 1, sizeof(int32_t));
     if (!p->slot_param_h || !p->param_ptr_h || !p->param_slots_h) { rc = qgt_set_error(E_NOMEM, "oom"); goto fail; }
     for (int g = 0; g < p->ngates; g++)
         if (p->gates[g].slot >= 0) { p->slot_param_h[p->gates[g].slot] = p->gates[g].param; p->param_ptr_h[p->gates[g].param + 1]++; }
-    for (int q = 0; q < p->P; q++) p->param_ptr_h[q + 1] += p->param_ptr_h[q];
+    for (int q = 0; q < p->Pd; q++) p->param_ptr_h[q + 1] += p->param_ptr_h[q];
     {
-        int32_t* fill = (int32_t*)calloc((size_t)p->P + 1, sizeof(int32_t));
+        int32_t* fill = (int32_t*)calloc((size_t)p->Pd + 1, sizeof(int32_t));
         if (!fill) { rc = qgt_set_error(E_NOMEM, "oom"); goto fail; }
         for (int s = 0; s < p->nslots; s++) {
             int q = p->slot_param_h[s];
@@ -588,8 +606,8 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
     if ((rc = qgt_dev_stream_create(&p->stream)) != 0) goto fail;
     {
         size_t ab = p->fp64 ? 16 : 8;
-        DALLOC(p->V, (size_t)(p->rows + 1) * (size_t)p->N * ab);
-        if ((rc = qgt_dev_memset(p->V, 0, (size_t)(p->rows + 1) * (size_t)p->N * ab, p->stream)) != 0) goto fail;
+        DALLOC(p->V, (size_t)p->B * (size_t)p->pstride * ab);
+        if ((rc = qgt_dev_memset(p->V, 0, (size_t)p->B * (size_t)p->pstride * ab, p->stream)) != 0) goto fail;
         if (p->opt.precision == QGT_PRECISION_MIXED_BF16X3) {
             size_t sb = (size_t)4 * p->rows_pad * (size_t)p->split_ld * 2;
             DALLOC(p->split, sb);
@@ -599,54 +617,68 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
     DALLOC(p->ops_d, sizeof(qgt_dev_op_t) * (size_t)(p->nops + 1));
     DALLOC(p->ents_d, sizeof(qgt_dev_entry_t) * (size_t)(p->nents + 1));
     DALLOC(p->coef_desc_d, sizeof(qgt_dev_coef_desc_t) * (size_t)(p->ncoef + 1));
-    DALLOC(p->coef_d, sizeof(double) * 8 * (size_t)(p->ncoef + 1));
-    DALLOC(p->coef32_d, sizeof(float) * 8 * (size_t)(p->ncoef + 1));
+    DALLOC(p->coef_d, sizeof(double) * 8 * (size_t)p->B * (size_t)(p->ncoef + 1));
+    DALLOC(p->coef32_d, sizeof(float) * 8 * (size_t)p->B * (size_t)(p->ncoef + 1));
     DALLOC(p->prog_d, sizeof(qgt_dev_op2_t) * (size_t)(p->nprog + 1));
     DALLOC(p->segs_d, (size_t)16 * (p->nsegs + 1));
-    DALLOC(p->theta_d, sizeof(double) * (size_t)(p->P + 1));
-    DALLOC(p->HG_d, sizeof(double) * 2 * (size_t)p->rows * p->rows);
-    DALLOC(p->Q_d, sizeof(double) * 2 * (size_t)p->P * p->P);
-    DALLOC(p->grad_d, sizeof(double) * (size_t)(p->P + 1));
-    DALLOC(p->energy_d, sizeof(double) * 2);
-    DALLOC(p->natgrad_d, sizeof(double) * (size_t)(p->P + 1));
-    DALLOC(p->chol_work_d, sizeof(double) * (size_t)p->P * p->P);
-    DALLOC(p->status_d, sizeof(double) * 2);
+    {
+        const size_t B = (size_t)p->B, Pd = (size_t)p->Pd;
+        DALLOC(p->theta_d, sizeof(double) * (B * (size_t)p->P + 1));
+        DALLOC(p->HG_d, sizeof(double) * 2 * B * (size_t)p->rows * p->rows);
+        DALLOC(p->Q_d, sizeof(double) * 2 * B * Pd * Pd);
+        DALLOC(p->grad_d, sizeof(double) * (B * Pd + 1));
+        DALLOC(p->energy_d, sizeof(double) * (B + 1));
+        DALLOC(p->natgrad_d, sizeof(double) * (B * Pd + 1));
+        DALLOC(p->chol_work_d, sizeof(double) * B * Pd * Pd);
+        DALLOC(p->status_d, sizeof(double) * 2 * B);
+    }
     DALLOC(p->slot_param_d, sizeof(int32_t) * (size_t)(p->nslots + 1));
-    DALLOC(p->param_ptr_d, sizeof(int32_t) * (size_t)(p->P + 2));
+    DALLOC(p->param_ptr_d, sizeof(int32_t) * (size_t)(p->Pd + 2));
     DALLOC(p->param_slots_d, sizeof(int32_t) * (size_t)(p->nslots + 1));
-    if (p->fp64) {
+    if (p->small_nsplit) {
+        /* rows <= 8: about 4 CTAs per SM over all points, >= 1024 amplitudes per CTA */
+        int64_t ns = (4 * 152 + p->B - 1) / p->B;
+        int64_t maxs = p->N / 1024;
+        if (ns > maxs) ns = maxs;
+        if (ns < 1) ns = 1;
+        p->small_nsplit = (int)ns;
+        DALLOC(p->small_part_d, sizeof(double) * 2 * 36 * (size_t)p->B * (size_t)ns);
+    } else if (p->fp64) {
         int nt = (p->rows + 31) / 32, ntp = nt * (nt + 1) / 2;
-        int ns = (int)(4 * 152 / ntp);
+        int ns = (int)(4 * 152 / ((int64_t)ntp * p->B));
         if (ns < 1) ns = 1;
         int64_t maxs = p->N / 64;
         if (maxs < 1) maxs = 1;
         if (ns > maxs) ns = (int)maxs;
         p->part_nsplit = ns;
-        DALLOC(p->part_d, sizeof(double) * 2 * 1024 * (size_t)ntp * ns);
+        DALLOC(p->part_d, sizeof(double) * 2 * 1024 * (size_t)ntp * ns * (size_t)p->B);
     } else if (p->opt.precision == QGT_PRECISION_MIXED_BF16X3) {
         if ((rc = qgt_dev_tc_gram_create(p->split, p->split_ld, p->rows, p->rows_pad, 1, &p->tc)) != 0) goto fail;
         p->device_bytes += qgt_dev_tc_gram_scratch_bytes(p->tc);
     } else {
         if (p->n < 4) { rc = qgt_set_error(E_INVAL, "mixed precision needs at least 4 qubits (use FP64)"); goto fail; }
-        DALLOC(p->rowmax_d, sizeof(uint32_t) * (size_t)p->rows);
-        if ((rc = qgt_dev_dg_gram_create(p->V, p->N, p->rows, p->rowmax_d, &p->dg)) != 0) goto fail;
+        DALLOC(p->rowmax_d, sizeof(uint32_t) * (size_t)p->rows * p->B);
+        if ((rc = qgt_dev_dg_gram_create(p->V, p->N, p->rows, p->rowmax_d, p->B, p->rows + 1, &p->dg)) != 0) goto fail;
         p->device_bytes += qgt_dev_dg_gram_scratch_bytes(p->dg);
     }
-    if ((rc = qgt_dev_memset(p->theta_d, 0, sizeof(double) * (size_t)(p->P + 1), p->stream)) != 0) goto fail;
+    if ((rc = qgt_dev_memset(p->theta_d, 0, sizeof(double) * ((size_t)p->B * p->P + 1), p->stream)) != 0) goto fail;
     if ((rc = qgt_dev_memcpy_h2d(p->ops_d, p->ops_h, sizeof(qgt_dev_op_t) * (size_t)p->nops, p->stream)) != 0) goto fail;
     if ((rc = qgt_dev_memcpy_h2d(p->ents_d, p->ents_h, sizeof(qgt_dev_entry_t) * (size_t)p->nents, p->stream)) != 0) goto fail;
     if (p->nprog && (rc = qgt_dev_memcpy_h2d(p->prog_d, p->prog_h, sizeof(qgt_dev_op2_t) * (size_t)p->nprog, p->stream)) != 0) goto fail;
     if (p->nsegs && (rc = qgt_dev_memcpy_h2d(p->segs_d, p->segs_h, (size_t)16 * p->nsegs, p->stream)) != 0) goto fail;
     if ((rc = qgt_dev_memcpy_h2d(p->coef_desc_d, p->coef_h, sizeof(qgt_dev_coef_desc_t) * (size_t)p->ncoef, p->stream)) != 0) goto fail;
     if ((rc = qgt_dev_memcpy_h2d(p->slot_param_d, p->slot_param_h, sizeof(int32_t) * (size_t)p->nslots, p->stream)) != 0) goto fail;
-    if ((rc = qgt_dev_memcpy_h2d(p->param_ptr_d, p->param_ptr_h, sizeof(int32_t) * (size_t)(p->P + 1), p->stream)) != 0) goto fail;
+    if ((rc = qgt_dev_memcpy_h2d(p->param_ptr_d, p->param_ptr_h, sizeof(int32_t) * (size_t)(p->Pd + 1), p->stream)) != 0) goto fail;
     if ((rc = qgt_dev_memcpy_h2d(p->param_slots_d, p->param_slots_h, sizeof(int32_t) * (size_t)p->nslots, p->stream)) != 0) goto fail;
-    if ((rc = qgt_dev_host_alloc((void**)&p->theta_pin, sizeof(double) * (size_t)(p->P + 1))) != 0) goto fail;
-    if ((rc = qgt_dev_host_alloc((void**)&p->Q_pin, sizeof(double) * 2 * (size_t)p->P * p->P + 16)) != 0) goto fail;
-    if ((rc = qgt_dev_host_alloc((void**)&p->grad_pin, sizeof(double) * (size_t)(p->P + 1))) != 0) goto fail;
-    if ((rc = qgt_dev_host_alloc((void**)&p->natgrad_pin, sizeof(double) * (size_t)(p->P + 1))) != 0) goto fail;
-    if ((rc = qgt_dev_host_alloc((void**)&p->energy_pin, sizeof(double) * 2)) != 0) goto fail;
-    if ((rc = qgt_dev_host_alloc((void**)&p->status_pin, sizeof(double) * 2)) != 0) goto fail;
+    {
+        const size_t B = (size_t)p->B, Pd = (size_t)p->Pd;
+        if ((rc = qgt_dev_host_alloc((void**)&p->theta_pin, sizeof(double) * (B * p->P + 1))) != 0) goto fail;
+        if ((rc = qgt_dev_host_alloc((void**)&p->Q_pin, sizeof(double) * 2 * B * Pd * Pd + 16)) != 0) goto fail;
+        if ((rc = qgt_dev_host_alloc((void**)&p->grad_pin, sizeof(double) * (B * Pd + 1))) != 0) goto fail;
+        if ((rc = qgt_dev_host_alloc((void**)&p->natgrad_pin, sizeof(double) * (B * Pd + 1))) != 0) goto fail;
+        if ((rc = qgt_dev_host_alloc((void**)&p->energy_pin, sizeof(double) * (B + 1))) != 0) goto fail;
+        if ((rc = qgt_dev_host_alloc((void**)&p->status_pin, sizeof(double) * 2 * B)) != 0) goto fail;
+    }
     if ((rc = qgt_dev_stream_sync(p->stream)) != 0) goto fail;
     /* first step eagerly (sets kernel attributes, validates), then capture */
     if ((rc = run_step(p)) != 0) goto fail;
@@ -675,7 +707,7 @@ void qgt_plan_destroy(qgt_plan_t* p)
     qgt_dev_tc_gram_destroy(p->tc);
     qgt_dev_dg_gram_destroy(p->dg);
     qgt_dev_free(p->rowmax_d);
-    void* dev[] = {p->V, p->split, p->ops_d, p->ents_d, p->prog_d, p->segs_d, p->coef32_d, p->coef_desc_d, p->coef_d, p->theta_d, p->HG_d, p->part_d,
+    void* dev[] = {p->V, p->split, p->small_part_d, p->ops_d, p->ents_d, p->prog_d, p->segs_d, p->coef32_d, p->coef_desc_d, p->coef_d, p->theta_d, p->HG_d, p->part_d,
                    p->Q_d, p->grad_d, p->energy_d, p->natgrad_d, p->chol_work_d, p->status_d, p->slot_param_d,
                    p->param_ptr_d, p->param_slots_d};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++) qgt_dev_free(dev[i]);
@@ -700,9 +732,11 @@ int qgt_plan_get_info(const qgt_plan_t* p, qgt_plan_info_t* info)
     int tb = 0;
     for (int k = 0; k < p->npasses; k++) if (p->passes[k].tile_bits > tb) tb = p->passes[k].tile_bits;
     info->tile_bits = tb;
-    info->vector_passes = p->vector_passes;
-    info->gate_bytes = p->gate_bytes;
-    info->gram_flops = (int64_t)4 * p->P * (p->P + 1) * p->N;
+    info->vector_passes = p->vector_passes * p->B;
+    info->gate_bytes = p->gate_bytes * p->B;
+    info->gram_flops = (int64_t)4 * p->Pd * (p->Pd + 1) * p->N * p->B;
+    info->batch = p->B;
+    info->num_deriv_params = p->Pd;
     info->device_bytes = p->device_bytes;
     return 0;
 }
@@ -718,13 +752,15 @@ static int run_step(qgt_plan_t* p)
     int rc;
     int launches = 0;
     MARK(0);
-    if ((rc = qgt_dev_prepare(p->coef_desc_d, p->ncoef, p->theta_d, p->coef_d, p->stream)) != 0) return rc;
+    if ((rc = qgt_dev_prepare(p->coef_desc_d, p->ncoef, p->theta_d, p->coef_d, p->B, p->P, p->stream)) != 0) return rc;
     launches += p->ncoef > 0;
     if (!p->fp64 && p->nprog > 0) {
-        if ((rc = qgt_dev_prepare32(p->coef_desc_d, p->ncoef, p->theta_d, p->coef32_d, p->stream)) != 0) return rc;
+        if ((rc = qgt_dev_prepare32(p->coef_desc_d, p->ncoef, p->theta_d, p->coef32_d, p->B, p->P, p->stream)) != 0)
+            return rc;
         launches += p->ncoef > 0;
     }
-    if (p->dg && (rc = qgt_dev_memset(p->rowmax_d, 0, sizeof(uint32_t) * (size_t)p->rows, p->stream)) != 0) return rc;
+    if (p->dg && (rc = qgt_dev_memset(p->rowmax_d, 0, sizeof(uint32_t) * (size_t)p->rows * p->B, p->stream)) != 0)
+        return rc;
     MARK(1);
     for (int k = 0; k < p->npasses; k++) {
         const spass_t* ps = &p->passes[k];
@@ -747,6 +783,10 @@ static int run_step(qgt_plan_t* p)
         a.tile_mask = ps->tile_mask;
         memcpy(a.local_to_phys, ps->l2p, sizeof a.local_to_phys);
         a.rowmax = p->rowmax_d;
+        a.npoints = p->B;
+        a.coef_stride = p->ncoef;
+        a.point_stride = p->pstride;
+        a.rowmax_stride = p->rows;
         if (ps->prog_count > 0) {
             qgt_dev_pass2_args_t b;
             memset(&b, 0, sizeof b);
@@ -768,6 +808,10 @@ static int run_step(qgt_plan_t* p)
             b.tile_mask = a.tile_mask;
             memcpy(b.local_to_phys, a.local_to_phys, sizeof b.local_to_phys);
             b.rowmax = a.rowmax;
+            b.npoints = a.npoints;
+            b.coef_stride = a.coef_stride;
+            b.point_stride = a.point_stride;
+            b.rowmax_stride = a.rowmax_stride;
             if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) return rc;
         } else if ((rc = qgt_dev_pass(&a, p->fp64, p->stream)) != 0) {
             return rc;
@@ -779,9 +823,13 @@ static int run_step(qgt_plan_t* p)
         size_t ab = p->fp64 ? 16 : 8;
         double one[2] = {1.0, 0.0};
         float onef[2] = {1.0f, 0.0f};
-        if ((rc = qgt_dev_memset(p->V, 0, (size_t)p->N * ab, p->stream)) != 0) return rc;
-        if ((rc = qgt_dev_memcpy_h2d(p->V, p->fp64 ? (const void*)one : (const void*)onef, ab, p->stream)) != 0) return rc;
         if (!p->fp64) return qgt_set_error(E_INVAL, "mixed plan needs at least one gate");
+        for (int b = 0; b < p->B; b++) {
+            char* row0 = (char*)p->V + (size_t)b * p->pstride * ab;
+            if ((rc = qgt_dev_memset(row0, 0, (size_t)p->N * ab, p->stream)) != 0) return rc;
+            if ((rc = qgt_dev_memcpy_h2d(row0, one, ab, p->stream)) != 0) return rc;
+        }
+        (void)onef;
     }
     MARK(2);
     const int has_h = p->opt.hamiltonian == QGT_HAMILTONIAN_TFIM;
@@ -790,13 +838,19 @@ static int run_step(qgt_plan_t* p)
         void* row1 = (char*)p->V + (size_t)p->N * ab;
         if ((rc = qgt_dev_tfim(p->V, row1, p->n, p->opt.tfim_J, p->opt.tfim_h, 1.0 / p->hscale, p->fp64,
                                p->split, p->split_ld, (int64_t)p->rows_pad * p->split_ld, 1, p->split_scale, 1,
-                               p->rowmax_d ? p->rowmax_d + 1 : NULL, p->stream)) != 0)
+                               p->rowmax_d ? p->rowmax_d + 1 : NULL, p->B, p->pstride, p->rows, p->stream)) != 0)
             return rc;
         launches++;
     }
     MARK(3);
-    if (p->fp64) {
-        if ((rc = qgt_dev_gram_f64(p->V, p->N, p->rows, p->part_d, p->part_nsplit, p->HG_d, p->stream)) != 0) return rc;
+    if (p->small_nsplit) {
+        if ((rc = qgt_dev_gram_small(p->V, p->N, p->rows, p->fp64, p->small_part_d, p->small_nsplit, p->HG_d, p->B,
+                                     p->pstride, p->stream)) != 0)
+            return rc;
+    } else if (p->fp64) {
+        if ((rc = qgt_dev_gram_f64(p->V, p->N, p->rows, p->part_d, p->part_nsplit, p->HG_d, p->B, p->pstride,
+                                   p->stream)) != 0)
+            return rc;
     } else if (p->dg) {
         if ((rc = qgt_dev_dg_gram_run(p->dg, p->HG_d, p->stream)) != 0) return rc;
     } else {
@@ -805,12 +859,13 @@ static int run_step(qgt_plan_t* p)
     }
     launches += 2;
     MARK(4);
-    if (p->P > 0) {
+    if (p->Pd > 0) {
         qgt_dev_post_args_t pa;
         memset(&pa, 0, sizeof pa);
         pa.HG = p->HG_d;
         pa.rows = p->rows;
-        pa.P = p->P;
+        pa.P = p->Pd;
+        pa.npoints = p->B;
         pa.slot_param = p->slot_param_d;
         pa.param_ptr = p->param_ptr_d;
         pa.param_slots = p->param_slots_d;
@@ -823,20 +878,26 @@ static int run_step(qgt_plan_t* p)
         launches += 1 + has_h;
         MARK(5);
         if (has_h) {
-            if (p->P <= 4096) {
-                if ((rc = qgt_dev_cholesky_blocked(p->Q_d, 1, p->grad_d, p->P, p->opt.lambda, p->chol_work_d,
+            if (p->B > 1) {
+                /* one CTA per point, lambda x10 retries inside */
+                if ((rc = qgt_dev_cholesky_batch(p->Q_d, 1, p->grad_d, p->Pd, p->opt.lambda, p->chol_work_d,
+                                                 p->natgrad_d, p->status_d, p->B, p->stream)) != 0)
+                    return rc;
+                launches++;
+            } else if (p->Pd <= 4096) {
+                if ((rc = qgt_dev_cholesky_blocked(p->Q_d, 1, p->grad_d, p->Pd, p->opt.lambda, p->chol_work_d,
                                                    p->natgrad_d, p->status_d, p->stream)) != 0)
                     return rc;
-                launches += qgt_dev_cholesky_launches(p->P);
+                launches += qgt_dev_cholesky_launches(p->Pd);
             } else {
-                if ((rc = qgt_dev_cholesky(p->Q_d, 1, p->grad_d, p->P, p->opt.lambda, p->chol_work_d, p->natgrad_d,
+                if ((rc = qgt_dev_cholesky(p->Q_d, 1, p->grad_d, p->Pd, p->opt.lambda, p->chol_work_d, p->natgrad_d,
                                            p->status_d, p->stream)) != 0)
                     return rc;
                 launches++;
             }
         }
     }
-    if (p->P <= 0) MARK(5);
+    if (p->Pd <= 0) MARK(5);
     MARK(6);
     p->launches = launches;
     return 0;
@@ -877,15 +938,16 @@ int qgt_plan_execute_device(qgt_plan_t* p, const double* theta_dev, double* Q_de
 {
     int rc;
     if (!p) return qgt_set_error(E_INVAL, "qgt_plan_execute_device: plan is NULL");
+    const size_t B = (size_t)p->B, Pd = (size_t)p->Pd;
     if (p->P > 0 && theta_dev && theta_dev != p->theta_d)
-        if ((rc = qgt_dev_memcpy_d2d(p->theta_d, theta_dev, sizeof(double) * (size_t)p->P, p->stream)) != 0) return rc;
+        if ((rc = qgt_dev_memcpy_d2d(p->theta_d, theta_dev, sizeof(double) * B * (size_t)p->P, p->stream)) != 0) return rc;
     if ((rc = launch_step(p)) != 0) return rc;
     int has_h = p->opt.hamiltonian == QGT_HAMILTONIAN_TFIM;
-    if (Q_dev && Q_dev != p->Q_d && (rc = qgt_dev_memcpy_d2d(Q_dev, p->Q_d, sizeof(double) * 2 * (size_t)p->P * p->P, p->stream)) != 0) return rc;
+    if (Q_dev && Q_dev != p->Q_d && (rc = qgt_dev_memcpy_d2d(Q_dev, p->Q_d, sizeof(double) * 2 * B * Pd * Pd, p->stream)) != 0) return rc;
     if (has_h) {
-        if (grad_dev && grad_dev != p->grad_d && (rc = qgt_dev_memcpy_d2d(grad_dev, p->grad_d, sizeof(double) * (size_t)p->P, p->stream)) != 0) return rc;
-        if (energy_dev && energy_dev != p->energy_d && (rc = qgt_dev_memcpy_d2d(energy_dev, p->energy_d, sizeof(double), p->stream)) != 0) return rc;
-        if (natgrad_dev && natgrad_dev != p->natgrad_d && (rc = qgt_dev_memcpy_d2d(natgrad_dev, p->natgrad_d, sizeof(double) * (size_t)p->P, p->stream)) != 0) return rc;
+        if (grad_dev && grad_dev != p->grad_d && (rc = qgt_dev_memcpy_d2d(grad_dev, p->grad_d, sizeof(double) * B * Pd, p->stream)) != 0) return rc;
+        if (energy_dev && energy_dev != p->energy_d && (rc = qgt_dev_memcpy_d2d(energy_dev, p->energy_d, sizeof(double) * B, p->stream)) != 0) return rc;
+        if (natgrad_dev && natgrad_dev != p->natgrad_d && (rc = qgt_dev_memcpy_d2d(natgrad_dev, p->natgrad_d, sizeof(double) * B * Pd, p->stream)) != 0) return rc;
     }
     return 0;
 }
@@ -895,35 +957,42 @@ int qgt_plan_execute_host(qgt_plan_t* p, const double* theta, double* Q, double*
     int rc;
     if (!p) return qgt_set_error(E_INVAL, "qgt_plan_execute_host: plan is NULL");
     if (p->P > 0 && !theta) return qgt_set_error(E_INVAL, "qgt_plan_execute_host: theta is NULL");
-    for (int k = 0; k < p->P; k++)
-        if (!isfinite(theta[k])) return qgt_set_error(E_INVAL, "qgt_plan_execute_host: theta[%d] is not finite", k);
+    const size_t B = (size_t)p->B, Pd = (size_t)p->Pd, nth = B * (size_t)p->P;
+    for (size_t k = 0; k < nth; k++)
+        if (!isfinite(theta[k])) return qgt_set_error(E_INVAL, "qgt_plan_execute_host: theta[%zu] is not finite", k);
     int has_h = p->opt.hamiltonian == QGT_HAMILTONIAN_TFIM;
     if ((grad || energy || natgrad) && !has_h)
         return qgt_set_error(E_INVAL, "qgt_plan_execute_host: energy outputs need a Hamiltonian");
     if (p->P > 0) {
-        memcpy(p->theta_pin, theta, sizeof(double) * (size_t)p->P);
-        if ((rc = qgt_dev_memcpy_h2d(p->theta_d, p->theta_pin, sizeof(double) * (size_t)p->P, p->stream)) != 0) return rc;
+        memcpy(p->theta_pin, theta, sizeof(double) * nth);
+        if ((rc = qgt_dev_memcpy_h2d(p->theta_d, p->theta_pin, sizeof(double) * nth, p->stream)) != 0) return rc;
     }
     if ((rc = launch_step(p)) != 0) return rc;
-    if (has_h && p->P > 0) {
-        /* the graph's blocked solve has no retries: on a non-positive pivot
-         * rerun the solve with lambda x 10 retries (outside the graph) */
-        if ((rc = qgt_dev_memcpy_d2h(p->status_pin, p->status_d, sizeof(double) * 2, p->stream)) != 0) return rc;
+    if (has_h && p->Pd > 0) {
+        if ((rc = qgt_dev_memcpy_d2h(p->status_pin, p->status_d, sizeof(double) * 2 * B, p->stream)) != 0) return rc;
         if ((rc = qgt_dev_stream_sync(p->stream)) != 0) return rc;
-        if ((int)p->status_pin[0] != 0 &&
-            (rc = qgt_dev_cholesky(p->Q_d, 1, p->grad_d, p->P, p->opt.lambda * 10.0, p->chol_work_d, p->natgrad_d,
-                                   p->status_d, p->stream)) != 0)
-            return rc;
+        if (B == 1) {
+            /* the graph's blocked solve has no retries: on a non-positive pivot
+             * rerun the solve with lambda x 10 retries (outside the graph) */
+            if ((int)p->status_pin[0] != 0 &&
+                (rc = qgt_dev_cholesky(p->Q_d, 1, p->grad_d, p->Pd, p->opt.lambda * 10.0, p->chol_work_d, p->natgrad_d,
+                                       p->status_d, p->stream)) != 0)
+                return rc;
+        } else {
+            for (size_t b = 0; b < B; b++)
+                if ((int)p->status_pin[2 * b] != 0)
+                    return qgt_set_error((int)p->status_pin[2 * b], "cholesky: point %zu not positive definite after lambda retries", b);
+        }
     }
-    if (Q && (rc = qgt_dev_memcpy_d2h(p->Q_pin, p->Q_d, sizeof(double) * 2 * (size_t)p->P * p->P, p->stream)) != 0) return rc;
-    if (grad && (rc = qgt_dev_memcpy_d2h(p->grad_pin, p->grad_d, sizeof(double) * (size_t)p->P, p->stream)) != 0) return rc;
-    if (energy && (rc = qgt_dev_memcpy_d2h(p->energy_pin, p->energy_d, sizeof(double), p->stream)) != 0) return rc;
-    if (natgrad && (rc = qgt_dev_memcpy_d2h(p->natgrad_pin, p->natgrad_d, sizeof(double) * (size_t)p->P, p->stream)) != 0) return rc;
+    if (Q && (rc = qgt_dev_memcpy_d2h(p->Q_pin, p->Q_d, sizeof(double) * 2 * B * Pd * Pd, p->stream)) != 0) return rc;
+    if (grad && (rc = qgt_dev_memcpy_d2h(p->grad_pin, p->grad_d, sizeof(double) * B * Pd, p->stream)) != 0) return rc;
+    if (energy && (rc = qgt_dev_memcpy_d2h(p->energy_pin, p->energy_d, sizeof(double) * B, p->stream)) != 0) return rc;
+    if (natgrad && (rc = qgt_dev_memcpy_d2h(p->natgrad_pin, p->natgrad_d, sizeof(double) * B * Pd, p->stream)) != 0) return rc;
     if ((rc = qgt_dev_stream_sync(p->stream)) != 0) return rc;
-    if (Q) memcpy(Q, p->Q_pin, sizeof(double) * 2 * (size_t)p->P * p->P);
-    if (grad) memcpy(grad, p->grad_pin, sizeof(double) * (size_t)p->P);
-    if (energy) *energy = p->energy_pin[0];
-    if (natgrad) memcpy(natgrad, p->natgrad_pin, sizeof(double) * (size_t)p->P);
+    if (Q) memcpy(Q, p->Q_pin, sizeof(double) * 2 * B * Pd * Pd);
+    if (grad) memcpy(grad, p->grad_pin, sizeof(double) * B * Pd);
+    if (energy) memcpy(energy, p->energy_pin, sizeof(double) * B);
+    if (natgrad) memcpy(natgrad, p->natgrad_pin, sizeof(double) * B * Pd);
     if (p->tc || p->dg) {
         int st = p->tc ? qgt_dev_tc_gram_status(p->tc, p->stream) : qgt_dev_dg_gram_status(p->dg, p->stream);
         if (st) return qgt_set_error(st, "tensor-core Gram reported device status %d", st);
@@ -981,11 +1050,12 @@ int qgt_plan_get_row(qgt_plan_t* p, int row, double* out)
 int qgt_plan_device_status(qgt_plan_t* p, double* lambda_used)
 {
     if (!p) return qgt_set_error(E_INVAL, "qgt_plan_device_status: plan is NULL");
-    int rc = qgt_dev_memcpy_d2h(p->status_pin, p->status_d, sizeof(double) * 2, p->stream);
+    int rc = qgt_dev_memcpy_d2h(p->status_pin, p->status_d, sizeof(double) * 2 * (size_t)p->B, p->stream);
     if (!rc) rc = qgt_dev_stream_sync(p->stream);
     if (rc) return rc;
     if (lambda_used) *lambda_used = p->status_pin[1];
-    int st = (int)p->status_pin[0];
+    int st = 0;
+    for (int b = 0; b < p->B && !st; b++) st = (int)p->status_pin[2 * b];
     if (!st && p->tc) st = qgt_dev_tc_gram_status(p->tc, p->stream);
     if (!st && p->dg) st = qgt_dev_dg_gram_status(p->dg, p->stream);
     return st;
@@ -1047,11 +1117,28 @@ int qgt_cholesky_solve_f64(const double* A, const double* g, double lambda, int3
     return 0;
 }
 
+int qgt_plan_enqueue_step(qgt_plan_t* p, void* stream)
+{
+    void* own = p->stream;
+    p->stream = stream;
+    int rc = run_step(p);
+    p->stream = own;
+    p->has_run = 1;
+    return rc;
+}
+
+double* qgt_plan_dev_theta(qgt_plan_t* p) { return p->theta_d; }
+double* qgt_plan_dev_Q(qgt_plan_t* p) { return p->Q_d; }
+int qgt_plan_launches(const qgt_plan_t* p) { return p->launches; }
+double* qgt_plan_dev_grad(qgt_plan_t* p) { return p->grad_d; }
+double* qgt_plan_dev_energy(qgt_plan_t* p) { return p->energy_d; }
+double* qgt_plan_dev_natgrad(qgt_plan_t* p) { return p->natgrad_d; }
+
 /* out = sum_s c[s] d_s over the derivative slots of an FP64 plan (2^n complex, host) */
 int qgt_plan_combine_slots(qgt_plan_t* p, const double* c, double* out)
 {
     if (!p || !c || !out) return qgt_set_error(E_INVAL, "qgt_plan_combine_slots: bad argument");
-    if (!p->fp64) return qgt_set_error(E_STATE, "qgt_plan_combine_slots: FP64 plans only");
+    if (!p->fp64 || p->B != 1) return qgt_set_error(E_STATE, "qgt_plan_combine_slots: unbatched FP64 plans only");
     if (p->nslots == 0) { memset(out, 0, sizeof(double) * 2 * (size_t)p->N); return 0; }
     double *cd = NULL, *od = NULL;
     int rc = qgt_dev_malloc((void**)&cd, sizeof(double) * (size_t)p->nslots);

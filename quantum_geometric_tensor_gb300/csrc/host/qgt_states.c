@@ -60,7 +60,7 @@ int qgt_qgt_from_states(const double* psi, const double* D, int64_t dim, int32_t
         if (ns < 1) ns = 1;
         if (ns > dim / 16) ns = (int)(dim / 16 > 0 ? dim / 16 : 1);
         rc = qgt_dev_malloc((void**)&part, sizeof(double) * 2 * 1024 * (size_t)ntp * ns);
-        if (!rc) rc = qgt_dev_gram_f64(X, dim, rows, part, ns, HG, s);
+        if (!rc) rc = qgt_dev_gram_f64(X, dim, rows, part, ns, HG, 1, 0, s);
     } else if (!rc && prec == QGT_PRECISION_MIXED) {
         /* complex64 rows (row length padded to 16 with zeros), per-row maxima, digit Gram */
         int64_t ld = (dim + 15) / 16 * 16;
@@ -74,7 +74,7 @@ int qgt_qgt_from_states(const double* psi, const double* D, int64_t dim, int32_t
         if (!rc) rc = qgt_dev_malloc((void**)&rmax, sizeof(uint32_t) * (size_t)rows);
         if (!rc) rc = qgt_dev_memset(rmax, 0, sizeof(uint32_t) * (size_t)rows, s);
         if (!rc) rc = qgt_dev_rowmax(Y, ld, 0, rows, rmax, s);
-        if (!rc) rc = qgt_dev_dg_gram_create(Y, ld, rows, rmax, &dg);
+        if (!rc) rc = qgt_dev_dg_gram_create(Y, ld, rows, rmax, 1, rows, &dg);
         if (!rc) rc = qgt_dev_dg_gram_run(dg, HG, s);
         if (!rc) rc = qgt_dev_stream_sync(s);
         if (!rc) {

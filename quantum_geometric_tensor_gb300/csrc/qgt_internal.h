@@ -94,6 +94,13 @@ typedef struct {
     uint32_t tile_mask;             /* physical qubits held in the tile */
     int8_t local_to_phys[16];
     uint32_t* rowmax;               /* per-row max |amplitude| as float bits (QENT_ROWMAX) */
+    /* parameter-point batch: grid.z = point; point p works on V + p point_stride
+     * (amplitudes), coefficients + p coef_stride and rowmax + p rowmax_stride
+     * (npoints 0 = one point) */
+    int32_t npoints;
+    int32_t coef_stride;
+    int64_t point_stride;
+    int32_t rowmax_stride;
 } qgt_dev_pass_args_t;
 
 /* ---- register-resident passes (qgt_pass2.cu) ----
@@ -130,14 +137,23 @@ typedef struct {
     uint32_t tile_mask;
     int8_t local_to_phys[16];
     uint32_t* rowmax;
+    int32_t npoints;                /* batch fields as in qgt_dev_pass_args_t */
+    int32_t coef_stride;
+    int64_t point_stride;
+    int32_t rowmax_stride;
 } qgt_dev_pass2_args_t;
 int qgt_dev_pass2(const qgt_dev_pass2_args_t* args, int fp64, void* stream);
 int qgt_dev_prepare32(const qgt_dev_coef_desc_t* descs_dev, int32_t ncoef, const double* theta_dev,
-                      float* coef32_dev, void* stream);
+                      float* coef32_dev, int32_t npoints, int32_t theta_stride, void* stream);
 
-/* internal plan helpers used by the reference API layer */
+/* internal plan helpers used by the reference API layer and the batch driver */
 struct qgt_plan;
 int qgt_plan_combine_slots(struct qgt_plan* p, const double* c, double* out);
+/* enqueue one step of the plan on `stream` (theta already in qgt_plan_dev_theta) */
+int qgt_plan_enqueue_step(struct qgt_plan* p, void* stream);
+double* qgt_plan_dev_theta(struct qgt_plan* p);   /* batch x num_params */
+double* qgt_plan_dev_Q(struct qgt_plan* p);       /* batch x Pd x Pd complex */
+int qgt_plan_launches(const struct qgt_plan* p);
 
 /* thread-local last error (host/qgt_error.c): stores the message and returns code */
 int qgt_set_error(int code, const char* fmt, ...);
@@ -166,16 +182,20 @@ const char* qgt_dev_error_string(void);
 int qgt_dev_event_create(void** ev);
 int qgt_dev_event_destroy(void* ev);
 int qgt_dev_event_record(void* ev, void* stream);
+int qgt_dev_stream_wait_event(void* stream, void* ev);
 int qgt_dev_event_elapsed(void* start, void* end, float* ms);
 
 /* ---- kernels ---- */
+/* gate matrices for npoints parameter points: theta + p theta_stride -> coef + 8 p ncoef */
 int qgt_dev_prepare(const qgt_dev_coef_desc_t* descs_dev, int32_t ncoef, const double* theta_dev,
-                    double* coef_dev, void* stream);
+                    double* coef_dev, int32_t npoints, int32_t theta_stride, void* stream);
 int qgt_dev_pass(const qgt_dev_pass_args_t* args, int fp64, void* stream);
-/* out (row 1 of V, and split row 1 when split != NULL) = H psi / hscale */
+/* out (row 1 of V, and split row 1 when split != NULL) = H psi / hscale, for
+ * npoints points point_stride amplitudes apart (rowmax slots rowmax_stride apart) */
 int qgt_dev_tfim(const void* psi, void* out, int32_t n, double J, double h, double inv_hscale,
                  int fp64, void* split, int64_t split_ld, int64_t split_plane_stride, int32_t split_row,
-                 float split_scale, int32_t split_bf16, uint32_t* rowmax_slot, void* stream);
+                 float split_scale, int32_t split_bf16, uint32_t* rowmax_slot, int32_t npoints,
+                 int64_t point_stride, int32_t rowmax_stride, void* stream);
 /* complex128 -> complex64 rows */
 int qgt_dev_c128_to_c64(const double* X, int64_t count, float* Y, void* stream);
 /* rowmax[row0 + r] = max(rowmax, max_k |V[row0 + r][k]|) over complex64 rows (float bits) */
@@ -183,7 +203,10 @@ int qgt_dev_rowmax(const void* V, int64_t N, int32_t row0, int32_t nrows, uint32
 /* mixed-precision Gram of complex64 rows [0, rows) of V with exactly accumulated
  * integer high digits (per-row power-of-two units from rowmax); HG as above */
 typedef struct qgt_dg_gram qgt_dg_gram_t;
-int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, const uint32_t* rowmax, qgt_dg_gram_t** g);
+/* npoints points point_rows rows apart; rowmax holds npoints x rows maxima and
+ * HG npoints x rows x rows blocks */
+int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, const uint32_t* rowmax, int32_t npoints,
+                           int32_t point_rows, qgt_dg_gram_t** g);
 int qgt_dev_dg_gram_run(qgt_dg_gram_t* g, double* HG, void* stream);
 int qgt_dev_dg_gram_status(qgt_dg_gram_t* g, void* stream);
 void qgt_dev_dg_gram_destroy(qgt_dg_gram_t* g);
@@ -194,9 +217,11 @@ int qgt_dev_split_rows(const double* X, int32_t rows, int64_t N, void* split, in
                        int32_t row0, float scale, int32_t bf16, void* stream);
 /* out = sum_k c[k] V[row0 + k] over complex128 rows (c on the device) */
 int qgt_dev_combine_rows(const void* V, int64_t N, int32_t row0, const double* c, int32_t K, void* out, void* stream);
-/* FP64 Gram of rows [0, rows) of V (complex128): HG = V V^H (HG_ij = <V_i|V_j>) */
+/* FP64 Gram of rows [0, rows) of V (complex128): HG = V V^H (HG_ij = <V_i|V_j>),
+ * for npoints points point_stride amplitudes apart (part holds
+ * npoints x nsplit x tile pairs blocks, HG npoints x rows x rows) */
 int qgt_dev_gram_f64(const void* V, int64_t N, int32_t rows, double* part, int32_t nsplit,
-                     double* HG, void* stream);
+                     double* HG, int32_t npoints, int64_t point_stride, void* stream);
 /* tensor-core Gram on the split operands; HG as above, scaled back by 1/scale^2 */
 typedef struct qgt_tc_gram qgt_tc_gram_t;
 int qgt_dev_tc_gram_create(void* split, int64_t N, int32_t rows, int32_t rows_pad, int32_t bf16,
@@ -219,6 +244,7 @@ typedef struct {
     double* Q;              /* P x P complex */
     double* grad;           /* P */
     double* energy;         /* 1 */
+    int32_t npoints;        /* parameter points (0 = 1): HG, Q, grad, energy blocks per point */
 } qgt_dev_post_args_t;
 int qgt_dev_post(const qgt_dev_post_args_t* a, void* stream);
 /* (Re Q + lambda I) x = b, FP64 Cholesky; A taken as Re of the complex Q when
@@ -231,6 +257,44 @@ int qgt_dev_cholesky(const double* A, int complex_input, const double* b, int32_
 int qgt_dev_cholesky_blocked(const double* A, int complex_input, const double* b, int32_t P,
                              double lambda, double* work, double* x, double* status, void* stream);
 int qgt_dev_cholesky_launches(int32_t P);
+/* nsys independent single-CTA solves with retries, systems contiguous
+ * (A: nsys x P x P, b / x: nsys x P, work: nsys x P x P, status: nsys x 2) */
+int qgt_dev_cholesky_batch(const double* A, int complex_input, const double* b, int32_t P, double lambda,
+                           double* work, double* x, double* status, int32_t nsys, void* stream);
+/* small Gram (rows <= 8) of complex64 (fp64 = 0) or complex128 rows, FP64
+ * sums: HG per point (npoints points point_stride amplitudes apart); part
+ * holds npoints x nsplit x 36 complex partials */
+int qgt_dev_gram_small(const void* V, int64_t N, int32_t rows, int32_t fp64, double* part, int32_t nsplit,
+                       double* HG, int32_t npoints, int64_t point_stride, void* stream);
+
+/* ---- learned preconditioner and PCG (qgt_learned.cu) ---- */
+/* X = [cos theta, sin theta] of theta rows idx[0..S) (idx NULL: rows 0..S) */
+int qgt_dev_lr_features(const double* theta, const int32_t* idx, int32_t S, int32_t P, float* X, void* stream);
+int qgt_dev_lr_linear(int32_t M, int32_t N, int32_t K, const float* X, const void* Wbf16, const float* b, float* Y,
+                      int32_t act, float* Z, void* stream);
+int qgt_dev_lr_linear_dx(int32_t M, int32_t N, int32_t K, const float* dY, const void* Wbf16, float* dX, void* stream);
+int qgt_dev_lr_linear_dw(int32_t M, int32_t N, int32_t K, const float* dY, const float* X, float* dW, float* db,
+                         void* stream);
+int qgt_dev_lr_silu_back(const float* Z, float* dH, int64_t n, void* stream);
+/* mean loss over S samples (metric rows idx[s]) added to *loss; dO = its gradient */
+int qgt_dev_lr_loss(const float* O, const float* metric, const int32_t* idx, int32_t S, int32_t P, int32_t r,
+                    float lambda, float u_scale, float* dO, float* loss, void* stream);
+int qgt_dev_lr_outputs(const float* O, int32_t S, int32_t P, int32_t r, float lambda, float u_scale, double* d,
+                       double* U, void* stream);
+int qgt_dev_lr_adam(float* w, void* wbf16, const float* g, float* m1, float* m2, int64_t n, float lr, float b1,
+                    float b2, float eps, int32_t step, float wd, void* stream);
+int qgt_dev_lr_to_bf16(const float* w, void* wbf16, int64_t n, void* stream);
+int qgt_dev_metric_f32(const double* Q, int64_t count, float* out, void* stream);
+/* nsys PCG solves of (Re Q + lambda I) x = b, systems sys_stride doubles apart */
+int qgt_dev_pcg(const double* Q, int32_t complex_input, int64_t sys_stride, const double* b, int32_t P, double lambda,
+                const double* d, const double* U, int32_t r, double tol, int32_t max_iter, double* x, int32_t* iters,
+                double* resid, int32_t nsys, void* stream);
+int qgt_dev_axpy_update(double* theta, const double* x, double eta, int32_t n, void* stream);
+
+/* more plan accessors (device buffers of a plan) */
+double* qgt_plan_dev_grad(struct qgt_plan* p);
+double* qgt_plan_dev_energy(struct qgt_plan* p);
+double* qgt_plan_dev_natgrad(struct qgt_plan* p);
 
 #ifdef __cplusplus
 }
