@@ -117,7 +117,7 @@ def init_dist(ws, local):
     return dist
 
 
-def cpu_baseline(threads: int | None = None):
+def cpu_baseline(threads: int | None = None, S: int = 16):
     """The FP64 oracle on the host cores on a bounded sample of the workload,
     extrapolated to one full QGT step:
       derivative generation: all 480 gates on psi + the first S parameters'
@@ -133,7 +133,6 @@ def cpu_baseline(threads: int | None = None):
     g = O.ansatz(N_QUBITS, LAYERS, ENT)
     P = O.num_params(g)
     th = O.splitmix64_params(SEED, P)
-    S = 16
     # keep only the first S parameters as parameters (others fixed) for the sample
     gs = g.copy()
     for i in range(len(gs)):
@@ -178,7 +177,7 @@ def run_reference(args, ws, rank):
         return 0
     vals = []
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline()
+        cb = cpu_baseline(S=4)   # ~7 s of host work per step
         if i >= args.warmup:
             vals.append(cb["value"])
     v = statistics.mean(vals)
@@ -357,6 +356,147 @@ def run_gb300(args, ws, rank, local):
     return 0
 
 
+def _line(metric, value, unit, steps, warmup, ms, cfg, extra):
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": steps, "warmup": warmup,
+         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic",
+         "config": cfg}
+    d.update(extra)
+    print(json.dumps(d), flush=True)
+
+
+def run_ragged(args):
+    """1024 circuits (qubits U{12..18}, layers U{2..6}, RY/RZ + CNOT ladder), full QGT of each plus a
+    32 x 32 Berry map over (first RY, first RZ of qubit 0), one graph launch per batch."""
+    import quantum_geometric_tensor_gb300 as Q
+    from oracle import oracle as O
+    rng = np.random.default_rng(SEED)
+    ns, Ls = rng.integers(12, 19, 1024), rng.integers(2, 7, 1024)
+    spec = [(int(n), Q.ansatz_gates(int(n), int(L), "cnot"), 2 * int(n) * int(L)) for n, L in zip(ns, Ls)]
+    thetas = [O.splitmix64_params(5000 + c, s_[2]) for c, s_ in enumerate(spec)]
+    t0 = time.perf_counter()
+    b = Q.Batch(spec, [(0, s_[0]) for s_ in spec], precision=Q.MIXED, grid=32)
+    t_create = time.perf_counter() - t0
+    info = b.info()
+    for _ in range(args.warmup):
+        Qs, maps = b.run(thetas)
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            Qs, maps = b.run(thetas)
+        ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+    errs = []
+    for c in (0, 511, 1023):
+        n, g, P = spec[c]
+        with Q.Plan(n, g, P, precision=Q.FP64, hamiltonian=Q.HAM_NONE) as p64:
+            r = p64.run(thetas[c], want=("Q",))
+        errs.append(float(np.linalg.norm(Qs[c].real - r["Q"].real) / np.linalg.norm(r["Q"].real)))
+    b.close()
+    _line("QGTs/sec (ragged batch of 1024 circuits, 12-18 qubits, each with a 32x32 Berry map)", 1024000.0 / ms,
+          "QGTs/sec", args.steps, args.warmup, ms,
+          {"workload": "ragged1024_q12-18_L2-6_cnot_berry32", "circuits": 1024, "groups": info.num_groups,
+           "berry_plans": info.num_berry_plans, "precision": "mixed"},
+          {"dtype": "c64/fp16-digits/f64", "e2e": {"value": 1024000.0 / ms, "unit": "QGTs/sec",
+                                                    "h2d_bytes_per_step": int(sum(len(t) for t in thetas) * 8),
+                                                    "d2h_bytes_per_step": int(sum(s_[2] ** 2 * 16 for s_ in spec)
+                                                                              + 1024 * 32 * 32 * 8)},
+           "graph_kernels": info.graph_kernels, "device_gb": info.device_bytes / 1e9, "create_s": t_create,
+           "metric_rel_err_vs_fp64": errs, "clocks": clk.summary()})
+
+
+def run_hea26(args):
+    """26 qubits, 2 layers RY/RZ + CNOT ladder (P = 104), mixed step against the FP64 GPU step."""
+    import quantum_geometric_tensor_gb300 as Q
+    from oracle import oracle as O
+    n, L = 26, 2
+    g = Q.ansatz_gates(n, L, "cnot")
+    P = 2 * n * L
+    th = O.splitmix64_params(26, P)
+    with Q.Plan(n, g, P, precision=Q.MIXED) as pm:
+        info = pm.info()
+        for _ in range(args.warmup):
+            om = pm.run(th)
+        with ClockSampler(0) as clk:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                om = pm.run(th)
+            ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+        prof = Q.StepProfile()
+        Q.lib().qgt_plan_profile_step(pm.h, C_byref(prof))
+    with Q.Plan(n, g, P, precision=Q.FP64) as p64:
+        p64.run(th)
+        t0 = time.perf_counter()
+        o64 = p64.run(th)
+        ms64 = (time.perf_counter() - t0) * 1000.0
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    hbm, tfl, src = peaks()
+    gate_gbs = info.gate_bytes / (prof.passes_ms * 1e-3) / 1e9
+    _line("QGTs/sec @26q,P=104 (mixed vs FP64 GPU)", 1000.0 / ms, "QGTs/sec", args.steps, args.warmup, ms,
+          {"workload": "hea26_L2_cnot_P104_tfim_natgrad", "qubits": n, "layers": L, "params": P, "precision": "mixed"},
+          {"dtype": "c64/fp16-digits/f64",
+           "e2e": {"value": 1000.0 / ms, "unit": "QGTs/sec", "h2d_bytes_per_step": P * 8,
+                   "d2h_bytes_per_step": P * P * 16 + 2 * P * 8 + 8},
+           "phases_ms": {"passes": prof.passes_ms, "gram": prof.gram_ms, "solve": prof.solve_ms},
+           "roofline": {"bound": "hbm", "achieved": gate_gbs, "peak": hbm, "unit": "GB/s", "frac": gate_gbs / hbm,
+                        "traffic": None, "peak_source": src},
+           "gram_tflops_algorithmic": info.gram_flops / (prof.gram_ms * 1e-3) / 1e12,
+           "device_gb": info.device_bytes / 1e9,
+           "fp64_gpu": {"ms_per_step": ms64, "speedup_mixed_vs_fp64": ms64 / ms,
+                        "rel_err": {"metric": rel(om["Q"].real, o64["Q"].real), "berry": rel(om["Q"].imag, o64["Q"].imag),
+                                    "grad": rel(om["grad"], o64["grad"]), "natgrad_step": rel(om["natgrad"], o64["natgrad"])}},
+           "clocks": clk.summary()})
+
+
+def run_learned(args):
+    """Learned preconditioner: 16 qubits, 6 layers RY/RZ + CNOT ladder (P = 192); train the MLP
+    (width 512, rank 16) on 20000 exact metrics generated on the GPU, then PCG iterations on held-out
+    points and a 500-step natural-gradient VQE (TFIM ring) against the Cholesky step."""
+    import quantum_geometric_tensor_gb300 as Q
+    from oracle import oracle as O
+    n, L = 16, 6
+    g = Q.ansatz_gates(n, L, "cnot")
+    P = 2 * n * L
+    rng = np.random.default_rng(SEED)
+    S = 20000
+    th = rng.uniform(0, 2 * np.pi, (S, P))
+    pc = Q.Precond(P, width=512, rank=16)
+    t0 = time.perf_counter()
+    hist = pc.train_circuit(n, g, th, precision=Q.MIXED, epochs=30, batch=256)
+    t_train = time.perf_counter() - t0
+    H = 32
+    th_h = rng.uniform(0, 2 * np.pi, (H, P))
+    met = Q.metric_dataset(n, g, th_h, precision=Q.FP64)
+    d, U = pc.predict(th_h)
+    its = {"cg": [], "jacobi": [], "learned": []}
+    for k in range(H):
+        b = rng.standard_normal(P)
+        its["cg"].append(Q.pcg_solve(met[k], b, 1e-3, tol=1e-8, max_iter=5000)[1])
+        its["jacobi"].append(Q.pcg_solve(met[k], b, 1e-3, d=np.diag(met[k]) + 1e-3, tol=1e-8, max_iter=5000)[1])
+        its["learned"].append(Q.pcg_solve(met[k], b, 1e-3, d=d[k], U=U[k], tol=1e-8, max_iter=5000)[1])
+    th0 = O.splitmix64_params(500, P)
+    vqe = {}
+    for name, solver, p_ in (("cholesky", Q.VQE_CHOLESKY, None), ("cg", Q.VQE_CG, None),
+                             ("learned", Q.VQE_PCG_LEARNED, pc)):
+        t0 = time.perf_counter()
+        E, it, _ = Q.vqe_run(n, g, th0, steps=500, eta=0.05, solver=solver, precond=p_, pcg_tol=1e-8,
+                             pcg_max_iter=5000)
+        vqe[name] = {"E_first": float(E[0]), "E_last": float(E[-1]), "s": time.perf_counter() - t0,
+                     "pcg_iters_mean": float(it.mean()), "E": E}
+    dE = float(np.abs(vqe["learned"]["E"] - vqe["cholesky"]["E"]).max())
+    for v in vqe.values():
+        v.pop("E")
+    ratio = float(np.mean(its["cg"]) / np.mean(its["learned"]))
+    pc.close()
+    _line("PCG iteration reduction, learned vs unpreconditioned (16q, P=192, held-out points)", ratio, "x",
+          1, 0, 0.0,
+          {"workload": "hea16_L6_cnot_P192_learned_precond", "samples": S, "width": 512, "rank": 16},
+          {"dtype": "bf16-weights/f32-acc; f64 PCG",
+           "heldout_pcg_iters_mean": {k: float(np.mean(v)) for k, v in its.items()},
+           "train_s": t_train, "loss_first": float(hist[0]), "loss_last": float(hist[-1]),
+           "vqe_500": vqe, "vqe_max_abs_dE_learned_vs_cholesky": dE})
+
+
 def C_byref(x):
     import ctypes
     return ctypes.byref(x)
@@ -372,10 +512,19 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison")
     ap.add_argument("--qubits", type=int, default=N_QUBITS, help="smaller register for profiling captures")
     ap.add_argument("--layers", type=int, default=LAYERS)
+    ap.add_argument("--workload", default="hea20", choices=["hea20", "ragged1024", "hea26", "learned16"],
+                    help="hea20: the headline step; the others reproduce the batch, 26-qubit and "
+                         "learned-preconditioner measurements")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, ws, rank)
+    if args.workload == "ragged1024":
+        return run_ragged(args)
+    if args.workload == "hea26":
+        return run_hea26(args)
+    if args.workload == "learned16":
+        return run_learned(args)
     return run_gb300(args, ws, rank, local)
 
 

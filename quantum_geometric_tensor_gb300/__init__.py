@@ -53,6 +53,24 @@ class BatchInfo(C.Structure):
                 ("graph_kernels", C.c_int32), ("device_bytes", C.c_int64)]
 
 
+class PrecondConfig(C.Structure):
+    _fields_ = [("num_params", C.c_int32), ("width", C.c_int32), ("rank", C.c_int32), ("lam", C.c_double),
+                ("u_scale", C.c_double), ("seed", C.c_uint64), ("device", C.c_int32)]
+
+
+class PrecondTrainOptions(C.Structure):
+    _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_double), ("weight_decay", C.c_double),
+                ("seed", C.c_uint64)]
+
+
+class VQEOptions(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("eta", C.c_double), ("pcg_tol", C.c_double), ("pcg_max_iter", C.c_int32),
+                ("solver", C.c_int32)]
+
+
+VQE_CHOLESKY, VQE_CG, VQE_PCG_LEARNED = 0, 1, 2
+
+
 class StepProfile(C.Structure):
     _fields_ = [("total_ms", C.c_double), ("prepare_ms", C.c_double), ("passes_ms", C.c_double),
                 ("hamiltonian_ms", C.c_double), ("gram_ms", C.c_double), ("post_ms", C.c_double),
@@ -89,6 +107,25 @@ def lib() -> C.CDLL:
         L.qgt_batch_execute_host.argtypes = [vp, vp, vp, vp]
         L.qgt_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
         L.qgt_batch_destroy.argtypes = [vp]
+        L.qgt_precond_default_config.argtypes = [C.POINTER(PrecondConfig)]
+        L.qgt_precond_default_train_options.argtypes = [C.POINTER(PrecondTrainOptions)]
+        L.qgt_precond_create.argtypes = [C.POINTER(PrecondConfig), C.POINTER(vp)]
+        L.qgt_precond_destroy.argtypes = [vp]
+        L.qgt_precond_num_weights.argtypes = [vp]
+        L.qgt_precond_num_weights.restype = C.c_int64
+        L.qgt_precond_get_weights.argtypes = [vp, vp]
+        L.qgt_precond_set_weights.argtypes = [vp, vp]
+        L.qgt_precond_loss_grad.argtypes = [vp, vp, vp, C.c_int32, vp, vp]
+        L.qgt_precond_predict.argtypes = [vp, vp, C.c_int32, vp, vp]
+        L.qgt_precond_train.argtypes = [vp, vp, vp, C.c_int32, C.POINTER(PrecondTrainOptions), vp]
+        L.qgt_precond_train_circuit.argtypes = [vp, C.POINTER(CircuitDesc), vp, C.c_int32, C.c_int,
+                                                C.POINTER(PrecondTrainOptions), vp]
+        L.qgt_metric_dataset.argtypes = [C.POINTER(CircuitDesc), vp, C.c_int32, C.c_int, C.c_int32, vp]
+        L.qgt_pcg_solve_f64.argtypes = [vp, vp, C.c_double, C.c_int32, vp, vp, C.c_int32, C.c_double, C.c_int32,
+                                        vp, vp, vp]
+        L.qgt_vqe_default_options.argtypes = [C.POINTER(VQEOptions)]
+        L.qgt_vqe_run.argtypes = [C.POINTER(CircuitDesc), C.POINTER(PlanOptions), vp, C.POINTER(VQEOptions), vp,
+                                  vp, vp, vp]
         L.qgt_last_error.restype = C.c_char_p
         L.qgt_version.restype = C.c_char_p
         _lib = L
@@ -278,6 +315,131 @@ class Batch:
 
     def __exit__(self, *a):
         self.close()
+
+
+class Precond:
+    """Learned metric preconditioner (qgt_precond_t)."""
+
+    def __init__(self, P, width=512, rank=16, lam=1e-3, seed=1, device=0):
+        L = lib()
+        c = PrecondConfig()
+        L.qgt_precond_default_config(C.byref(c))
+        c.num_params, c.width, c.rank, c.lam, c.seed, c.device = P, width, rank, lam, seed, device
+        self.cfg = c
+        h_ = C.c_void_p()
+        _check(L.qgt_precond_create(C.byref(c), C.byref(h_)), "qgt_precond_create")
+        self.h, self.P, self.r = h_, P, rank
+
+    def _opts(self, epochs, batch, lr, seed):
+        o = PrecondTrainOptions()
+        lib().qgt_precond_default_train_options(C.byref(o))
+        o.epochs, o.batch, o.lr, o.seed = epochs, batch, lr, seed
+        return o
+
+    def train(self, theta, metric, epochs=30, batch=256, lr=1e-3, seed=7):
+        theta = np.ascontiguousarray(theta, dtype=np.float64)
+        metric = np.ascontiguousarray(metric, dtype=np.float64)
+        o = self._opts(epochs, batch, lr, seed)
+        hist = np.zeros(epochs)
+        _check(lib().qgt_precond_train(self.h, _ptr(theta), _ptr(metric), theta.shape[0], C.byref(o), _ptr(hist)),
+               "qgt_precond_train")
+        return hist
+
+    def train_circuit(self, n, gates, theta, precision=MIXED, epochs=30, batch=256, lr=1e-3, seed=7):
+        theta = np.ascontiguousarray(theta, dtype=np.float64)
+        d = circuit_desc(n, gates, self.P)
+        o = self._opts(epochs, batch, lr, seed)
+        hist = np.zeros(epochs)
+        _check(lib().qgt_precond_train_circuit(self.h, C.byref(d), _ptr(theta), theta.shape[0], precision,
+                                               C.byref(o), _ptr(hist)), "qgt_precond_train_circuit")
+        return hist
+
+    def predict(self, theta):
+        theta = np.ascontiguousarray(np.atleast_2d(theta), dtype=np.float64)
+        S = theta.shape[0]
+        d = np.zeros((S, self.P))
+        U = np.zeros((S, self.P, self.r))
+        _check(lib().qgt_precond_predict(self.h, _ptr(theta), S, _ptr(d), _ptr(U)), "qgt_precond_predict")
+        return d, U
+
+    def num_weights(self):
+        return int(lib().qgt_precond_num_weights(self.h))
+
+    def weights(self):
+        w = np.zeros(self.num_weights(), dtype=np.float32)
+        _check(lib().qgt_precond_get_weights(self.h, _ptr(w)), "qgt_precond_get_weights")
+        return w
+
+    def set_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        _check(lib().qgt_precond_set_weights(self.h, _ptr(w)), "qgt_precond_set_weights")
+
+    def loss_grad(self, theta, metric):
+        theta = np.ascontiguousarray(theta, dtype=np.float64)
+        metric = np.ascontiguousarray(metric, dtype=np.float64)
+        loss = np.zeros(1)
+        g = np.zeros(self.num_weights(), dtype=np.float32)
+        _check(lib().qgt_precond_loss_grad(self.h, _ptr(theta), _ptr(metric), theta.shape[0], _ptr(loss), _ptr(g)),
+               "qgt_precond_loss_grad")
+        return float(loss[0]), g
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().qgt_precond_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def metric_dataset(n, gates, theta, precision=FP64, device=0):
+    """Re Q of S parameter points (theta S x P) on the GPU -> S x P x P."""
+    theta = np.ascontiguousarray(theta, dtype=np.float64)
+    S, P = theta.shape
+    d = circuit_desc(n, gates, P)
+    out = np.zeros((S, P, P))
+    _check(lib().qgt_metric_dataset(C.byref(d), _ptr(theta), S, precision, device, _ptr(out)), "qgt_metric_dataset")
+    return out
+
+
+def pcg_solve(A, b, lam, d=None, U=None, tol=1e-10, max_iter=1000):
+    """GPU PCG of (A + lam I) x = b with M = diag(d) + U U^T -> (x, iterations, relative residual)."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    P = b.shape[0]
+    dd = None if d is None else np.ascontiguousarray(d, dtype=np.float64)
+    UU = None if U is None else np.ascontiguousarray(U, dtype=np.float64)
+    r = 0 if UU is None else UU.shape[1]
+    x = np.zeros(P)
+    it = np.zeros(1, dtype=np.int32)
+    res = np.zeros(1)
+    _check(lib().qgt_pcg_solve_f64(_ptr(A), _ptr(b), lam, P, _ptr(dd), _ptr(UU), r, tol, max_iter, _ptr(x),
+                                   _ptr(it), _ptr(res)), "qgt_pcg_solve_f64")
+    return x, int(it[0]), float(res[0])
+
+
+def vqe_run(n, gates, theta0, steps=500, eta=0.05, solver=VQE_CHOLESKY, precond=None, precision=MIXED,
+            pcg_tol=1e-10, pcg_max_iter=1000, lam=1e-3):
+    """Natural-gradient VQE on the TFIM ring, looped on the device -> (energies, pcg iterations, final theta)."""
+    L = lib()
+    th0 = np.ascontiguousarray(theta0, dtype=np.float64)
+    P = th0.shape[0]
+    d = circuit_desc(n, gates, P)
+    po = PlanOptions()
+    L.qgt_plan_default_options(C.byref(po))
+    po.precision, po.lambda_ = precision, lam
+    vo = VQEOptions()
+    L.qgt_vqe_default_options(C.byref(vo))
+    vo.steps, vo.eta, vo.solver, vo.pcg_tol, vo.pcg_max_iter = steps, eta, solver, pcg_tol, pcg_max_iter
+    E = np.zeros(steps)
+    its = np.zeros(steps, dtype=np.int32)
+    th = np.zeros(P)
+    _check(L.qgt_vqe_run(C.byref(d), C.byref(po), None if precond is None else precond.h, C.byref(vo), _ptr(th0),
+                         _ptr(E), _ptr(its), _ptr(th)), "qgt_vqe_run")
+    return E, its, th
 
 
 def cholesky_solve(A, b, lam):

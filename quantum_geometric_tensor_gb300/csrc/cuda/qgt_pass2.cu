@@ -256,6 +256,109 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
             for (int j = 0; j < NR; j++) v[j] = tile[lidx(j)];
             continue;
         }
+        if (op.kind == Q2_DIAG) {
+            // combined phase of the run: c (thread factor) x prod_i f_i(reg bit i) x sign(static mask)
+            const int cnt = op.seg;
+            R cr = (R)1, ci = (R)0;
+            R f0r[RB], f0i[RB], f1r[RB], f1i[RB];
+#pragma unroll
+            for (int i = 0; i < RB; i++) { f0r[i] = (R)1; f0i[i] = (R)0; f1r[i] = (R)1; f1i[i] = (R)0; }
+            for (int u = 1; u <= cnt; u++) {
+                const qgt_dev_op2_t so = sops[pc + u];
+                const bool ra_reg = so.ra >= RL_REG && so.ra < RL_WARP;
+                if (so.kind == Q2_PHASE) {
+                    const R* c8 = scoef + 8 * (pc + u);
+                    const R p0r = c8[0], p0i = c8[1], p1r = c8[6], p1i = c8[7];
+                    if (ra_reg) {
+                        const int ri = so.ra - RL_REG;
+#pragma unroll
+                        for (int i = 0; i < RB; i++)
+                            if (i == ri) {
+                                R t = f0r[i] * p0r - f0i[i] * p0i;
+                                f0i[i] = f0r[i] * p0i + f0i[i] * p0r;
+                                f0r[i] = t;
+                                t = f1r[i] * p1r - f1i[i] * p1i;
+                                f1i[i] = f1r[i] * p1i + f1i[i] * p1r;
+                                f1r[i] = t;
+                            }
+                    } else {
+                        const int bit = role_bit(so.ra, so.q, lane, warp, base);
+                        const R pr = bit ? p1r : p0r, pi = bit ? p1i : p0i;
+                        const R t = cr * pr - ci * pi;
+                        ci = cr * pi + ci * pr;
+                        cr = t;
+                    }
+                } else {  // Q2_CZ
+                    const bool rb_reg = so.rb >= RL_REG && so.rb < RL_WARP;
+                    if (ra_reg && rb_reg) continue;  // in the static mask
+                    if (ra_reg || rb_reg) {
+                        const int ri = (ra_reg ? so.ra : so.rb) - RL_REG;
+                        const int tb = ra_reg ? role_bit(so.rb, so.q2, lane, warp, base) : role_bit(so.ra, so.q, lane, warp, base);
+                        if (tb) {
+#pragma unroll
+                            for (int i = 0; i < RB; i++)
+                                if (i == ri) { f1r[i] = -f1r[i]; f1i[i] = -f1i[i]; }
+                        }
+                    } else if (role_bit(so.ra, so.q, lane, warp, base) & role_bit(so.rb, so.q2, lane, warp, base)) {
+                        cr = -cr;
+                        ci = -ci;
+                    }
+                }
+            }
+            // tables over register bits 0..2 (with c) and 3..RB-1, then one product per amplitude
+            constexpr int LB = 3, HB = RB - 3;
+            R tlr[1 << LB], tli[1 << LB], thr[1 << HB], thi[1 << HB];
+            tlr[0] = cr;
+            tli[0] = ci;
+#pragma unroll
+            for (int i = 0; i < LB; i++)
+#pragma unroll
+                for (int j = 0; j < (1 << i); j++) {
+                    const R ar = tlr[j], ai = tli[j];
+                    tlr[j + (1 << i)] = ar * f1r[i] - ai * f1i[i];
+                    tli[j + (1 << i)] = ar * f1i[i] + ai * f1r[i];
+                    tlr[j] = ar * f0r[i] - ai * f0i[i];
+                    tli[j] = ar * f0i[i] + ai * f0r[i];
+                }
+            thr[0] = (R)1;
+            thi[0] = (R)0;
+#pragma unroll
+            for (int i = 0; i < HB; i++)
+#pragma unroll
+                for (int j = 0; j < (1 << i); j++) {
+                    const R ar = thr[j], ai = thi[j];
+                    thr[j + (1 << i)] = ar * f1r[LB + i] - ai * f1i[LB + i];
+                    thi[j + (1 << i)] = ar * f1i[LB + i] + ai * f1r[LB + i];
+                    thr[j] = ar * f0r[LB + i] - ai * f0i[LB + i];
+                    thi[j] = ar * f0i[LB + i] + ai * f0r[LB + i];
+                }
+            const uint32_t sgn = (uint32_t)op.slot;
+#pragma unroll
+            for (int j = 0; j < NR; j++) {
+                const R hr = thr[j >> LB], hi2 = thi[j >> LB], lr = tlr[j & ((1 << LB) - 1)], li = tli[j & ((1 << LB) - 1)];
+                R pr = lr * hr - li * hi2, pi = lr * hi2 + li * hr;
+                if ((sgn >> j) & 1u) { pr = -pr; pi = -pi; }
+                const T x = v[j];
+                v[j].x = pr * x.x - pi * x.y;
+                v[j].y = pr * x.y + pi * x.x;
+            }
+            if (e.spawn_op > pc && e.spawn_op <= pc + cnt) {
+                // (-i/2) Z of the spawning rotation, after the run (diagonal ops commute)
+                const qgt_dev_op2_t so = sops[e.spawn_op];
+                const uint32_t mk = role_mask<NR>(so.ra, so.q, lane, warp, base);
+                const R h = (R)0.5;
+#pragma unroll
+                for (int j = 0; j < NR; j++) {
+                    const R sg = ((mk >> j) & 1u) ? h : -h;
+                    T o;
+                    o.x = -sg * v[j].y;
+                    o.y = sg * v[j].x;
+                    v[j] = o;
+                }
+            }
+            pc += cnt;
+            continue;
+        }
         if (op.kind == Q2_U || op.kind == Q2_UR) {
 #pragma unroll
             for (int i = 0; i < 8; i++) m[i] = scoef[8 * pc + i];
@@ -266,12 +369,24 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
                 RB_SWITCH(ri, U_CALL)
 #undef U_CALL
             } else {
+                // lane bit: v' = c_self v + c_partner w (w = the partner lane's amplitude);
+                // row 1 of the matrix for the upper lane, row 0 for the lower one
                 const int b = op.ra, hi = (lane >> b) & 1;
+                R cs[2] = {hi ? m[6] : m[0], hi ? m[7] : m[1]};
+                R cp[2] = {hi ? m[4] : m[2], hi ? m[5] : m[3]};
+                if (real) {
 #pragma unroll
-                for (int j = 0; j < NR; j++) {
-                    T w = shfl_x<T>(v[j], 1 << b);
-                    if (real) v[j] = hi ? rmad2<T, R>(m[4], w, m[6], v[j]) : rmad2<T, R>(m[0], v[j], m[2], w);
-                    else v[j] = hi ? cmad2<T, R>(m + 4, w, v[j]) : cmad2<T, R>(m, v[j], w);
+                    for (int j = 0; j < NR; j++) {
+                        T w = shfl_x<T>(v[j], 1 << b);
+                        v[j] = rmad2<T, R>(cs[0], v[j], cp[0], w);
+                    }
+                } else {
+                    R mm[4] = {cs[0], cs[1], cp[0], cp[1]};
+#pragma unroll
+                    for (int j = 0; j < NR; j++) {
+                        T w = shfl_x<T>(v[j], 1 << b);
+                        v[j] = cmad2<T, R>(mm, v[j], w);
+                    }
                 }
             }
         } else if (op.kind == Q2_PHASE) {

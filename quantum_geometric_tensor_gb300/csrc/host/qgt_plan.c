@@ -506,6 +506,65 @@ static int build_programs(qgt_plan_t* p)
     return 0;
 }
 
+/* Runs of two or more consecutive diagonal ops (RZ / Z / S / T phases and
+ * CZs) inside a segment get a Q2_DIAG header, so that the kernel multiplies
+ * each amplitude once by the run's combined phase instead of once per gate.
+ * Diagonal ops commute, so a derivative generator (-i/2) Z spawned inside the
+ * run is applied after it. */
+static int fold_diagonal_runs(qgt_plan_t* p)
+{
+    if (p->nprog == 0) return 0;
+    const int cap = p->nprog + p->nprog / 2 + 16;
+    qgt_dev_op2_t* np2 = (qgt_dev_op2_t*)calloc((size_t)cap, sizeof(qgt_dev_op2_t));
+    int* remap = (int*)malloc(sizeof(int) * ((size_t)p->nprog + 1));
+    if (!np2 || !remap) { free(np2); free(remap); return qgt_set_error(E_NOMEM, "programs: oom"); }
+    int out = 0;
+    for (int k = 0; k < p->npasses; k++) {
+        spass_t* ps = &p->passes[k];
+        if (ps->prog_count == 0) { ps->prog_begin = out; continue; }
+        const qgt_dev_op2_t* src = p->prog_h + ps->prog_begin;
+        const int n = ps->prog_count, nb = out;
+        for (int j = 0; j < n;) {
+            int e = j;
+            while (e < n && (src[e].kind == Q2_PHASE || src[e].kind == Q2_CZ)) e++;
+            if (e - j >= 2 && out + (e - j) + 1 < cap) {
+                qgt_dev_op2_t h;
+                memset(&h, 0, sizeof h);
+                h.kind = Q2_DIAG;
+                h.seg = (int16_t)(e - j);
+                h.coef = -1;
+                uint32_t mask = 0;
+                for (int t = j; t < e; t++) {
+                    const qgt_dev_op2_t* o = &src[t];
+                    if (o->kind == Q2_CZ && o->ra >= RL_REG_ && o->ra < RL_WARP_ && o->rb >= RL_REG_ && o->rb < RL_WARP_) {
+                        const int a = o->ra - RL_REG_, b = o->rb - RL_REG_;
+                        for (int r = 0; r < 32; r++)
+                            if (((r >> a) & 1) && ((r >> b) & 1)) mask ^= 1u << r;
+                    }
+                }
+                h.slot = (int32_t)mask;
+                np2[out++] = h;
+                for (int t = j; t < e; t++) { remap[t] = out - nb; np2[out++] = src[t]; }
+                j = e;
+            } else {
+                if (e == j) e = j + 1;
+                for (int t = j; t < e; t++) { remap[t] = out - nb; np2[out++] = src[t]; }
+                j = e;
+            }
+            if (out + 2 >= cap) { free(np2); free(remap); return qgt_set_error(E_STATE, "programs: capacity"); }
+        }
+        for (int en = ps->ent_begin; en < ps->ent_begin + ps->ent_count; en++)
+            if (p->ents_h[en].spawn_op >= 0) p->ents_h[en].spawn_op = remap[p->ents_h[en].spawn_op];
+        ps->prog_begin = nb;
+        ps->prog_count = out - nb;
+    }
+    free(p->prog_h);
+    p->prog_h = np2;
+    p->nprog = out;
+    free(remap);
+    return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* plan lifecycle                                                            */
 /* ------------------------------------------------------------------------ */
@@ -594,6 +653,7 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
     if ((rc = compile_schedule(p)) != 0) goto fail;
     if ((rc = build_entries(p)) != 0) goto fail;
     if ((rc = build_programs(p)) != 0) goto fail;
+    if ((rc = fold_diagonal_runs(p)) != 0) goto fail;
     {
         int nb = p->n >= 3 ? p->n : p->n - 1;
         p->hscale = fabs(p->opt.tfim_J) * nb + fabs(p->opt.tfim_h) * p->n;

@@ -108,7 +108,11 @@ typedef struct {
  * bits are register bits / warp bits) through shared memory.  Bits are
  * role-encoded: 0..4 lane bit, 8 + i register bit i, 16 + w warp bit w,
  * 32 outside the tile (physical qubit in q / q2). */
-enum { Q2_SEG = 1, Q2_U = 2, Q2_UR = 3, Q2_PHASE = 4, Q2_CZ = 5, Q2_CNOT = 6 };
+enum { Q2_SEG = 1, Q2_U = 2, Q2_UR = 3, Q2_PHASE = 4, Q2_CZ = 5, Q2_CNOT = 6, Q2_DIAG = 7 };
+/* Q2_DIAG: header of a run of `seg` diagonal ops (Q2_PHASE / Q2_CZ) that
+ * follow it; the run is applied as one per-thread phase table.  `slot` holds
+ * the sign mask over the register index of the run's CZs between two register
+ * bits (those CZ ops stay in the run and are skipped). */
 typedef struct {
     uint8_t kind;
     uint8_t ra;     /* target / first bit (role-encoded) */
