@@ -75,7 +75,13 @@ typedef enum {
     QGT_HAMILTONIAN_NONE = 0,
     /* transverse-field Ising ring H = -J sum_i Z_i Z_{i+1 mod n} - h sum_i X_i
      * (n bonds for n >= 3, an open chain below) */
-    QGT_HAMILTONIAN_TFIM = 1
+    QGT_HAMILTONIAN_TFIM = 1,
+    /* sum_k c_k P_k over Pauli strings (pauli_strings / pauli_coeffs of the
+     * options), the convention of compute_pauli_expectation
+     * (src/quantum_geometric/hybrid/quantum_classical_algorithms.c:320-382):
+     * character [n-1-q] of a string acts on qubit q, X / Y / Z in either case,
+     * any other character is the identity */
+    QGT_HAMILTONIAN_PAULI = 2
 } qgt_hamiltonian_t;
 
 typedef struct {
@@ -93,6 +99,12 @@ typedef struct {
      * are num_deriv_params wide (Q: Pd x Pd, grad / natgrad: Pd); the others
      * only set gate angles.  0 = all num_params. */
     int32_t num_deriv_params;
+    /* QGT_HAMILTONIAN_PAULI: num_pauli_terms strings of num_qubits characters
+     * back to back (term k at pauli_strings + k n) and their real coefficients;
+     * copied at plan creation */
+    int32_t num_pauli_terms;
+    const char* pauli_strings;
+    const double* pauli_coeffs;
 } qgt_plan_options_t;
 
 typedef struct qgt_plan qgt_plan_t;

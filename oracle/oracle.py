@@ -101,6 +101,7 @@ class Oracle:
         L.or_derivatives.argtypes = [i32, vp, i32, vp, i32, vp, vp]
         L.or_qgt.argtypes = [sz, i32, vp, vp, vp]
         L.or_tfim_apply.argtypes = [i32, f64, f64, vp, vp]
+        L.or_pauli_apply.argtypes = [i32, i32, C.POINTER(C.c_char_p), vp, vp, vp]
         L.or_tfim_energy.argtypes = [i32, f64, f64, vp]
         L.or_tfim_energy.restype = f64
         L.or_energy_grad.argtypes = [sz, i32, vp, vp, vp]
@@ -145,6 +146,14 @@ class Oracle:
     def tfim_apply(self, n, psi, J=1.0, h=1.0):
         out = np.zeros_like(psi)
         self.lib.or_tfim_apply(n, J, h, _p(np.ascontiguousarray(psi)), _p(out))
+        return out
+
+    def pauli_apply(self, n, psi, terms):
+        """H psi for terms = [(coeff, "XZIY..."), ...] (character n-1-q acts on qubit q)."""
+        strs = (C.c_char_p * len(terms))(*[s.encode() for _, s in terms])
+        co = np.ascontiguousarray([c for c, _ in terms], dtype=np.float64)
+        out = np.zeros_like(psi)
+        self.lib.or_pauli_apply(n, len(terms), strs, _p(co), _p(np.ascontiguousarray(psi)), _p(out))
         return out
 
     def tfim_energy(self, n, psi, J=1.0, h=1.0):

@@ -270,6 +270,47 @@ void or_tfim_apply(int n, double J, double h, const double* psi, double* out)
     }
 }
 
+/* H psi for H = sum_k c_k P_k, P_k a Pauli string (compute_pauli_expectation,
+ * hybrid/quantum_classical_algorithms.c:320-382): character [n-1-q] of the
+ * string acts on qubit q; X, Y, Z (either case), anything else is the
+ * identity; a string whose length is not n contributes nothing.  Each
+ * operator is applied qubit by qubit to a copy of psi, as the reference does. */
+void or_pauli_apply(int n, int nterms, const char* const* strings, const double* coeffs, const double* psi,
+                    double* out)
+{
+    size_t dim = (size_t)1 << n;
+    cd* o = (cd*)out;
+    cd* t = (cd*)malloc(dim * sizeof(cd));
+    memset(out, 0, 2 * dim * sizeof(double));
+    if (!t) return;
+    for (int k = 0; k < nterms; k++) {
+        const char* s = strings[k];
+        if (!s || (int)strlen(s) != n) continue;
+        memcpy(t, psi, dim * sizeof(cd));
+        for (int q = 0; q < n; q++) {
+            char c = s[n - 1 - q];
+            size_t m = (size_t)1 << q;
+            if (c == 'X' || c == 'x') {
+                for (size_t i = 0; i < dim; i++)
+                    if (!(i & m)) { cd a = t[i]; t[i] = t[i | m]; t[i | m] = a; }
+            } else if (c == 'Y' || c == 'y') {
+                /* Y = [[0, -i], [i, 0]]: new0 = -i old1, new1 = i old0 */
+                for (size_t i = 0; i < dim; i++)
+                    if (!(i & m)) {
+                        cd a0 = t[i], a1 = t[i | m];
+                        t[i].re = a1.im; t[i].im = -a1.re;
+                        t[i | m].re = -a0.im; t[i | m].im = a0.re;
+                    }
+            } else if (c == 'Z' || c == 'z') {
+                for (size_t i = 0; i < dim; i++)
+                    if (i & m) { t[i].re = -t[i].re; t[i].im = -t[i].im; }
+            }
+        }
+        for (size_t i = 0; i < dim; i++) { o[i].re += coeffs[k] * t[i].re; o[i].im += coeffs[k] * t[i].im; }
+    }
+    free(t);
+}
+
 double or_tfim_energy(int n, double J, double h, const double* psi)
 {
     size_t dim = (size_t)1 << n;

@@ -74,6 +74,9 @@ int or_qgt(size_t dim, int nparams, const double* psi, const double* D, double* 
  * an open chain for n < 3).  out = H psi. */
 void or_tfim_apply(int n, double J, double h, const double* psi, double* out);
 double or_tfim_energy(int n, double J, double h, const double* psi);
+/* H psi, H = sum_k coeffs[k] P(strings[k]) (reference Pauli-string convention) */
+void or_pauli_apply(int n, int nterms, const char* const* strings, const double* coeffs, const double* psi,
+                    double* out);
 
 /* grad_k = 2 Re <d_k psi | H psi> */
 void or_energy_grad(size_t dim, int nparams, const double* D, const double* Hpsi, double* grad);

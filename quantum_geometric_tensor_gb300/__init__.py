@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(PKG, "lib", "libqgt_gb300.so")
 # gate codes (reference gate_type_t values)
 I, X, Y, Z, H, S, T, RX, RY, RZ, CNOT, CZ, SWAP = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 12, 13
 FP64, MIXED, MIXED_BF16X3 = 0, 1, 2
-HAM_NONE, HAM_TFIM = 0, 1
+HAM_NONE, HAM_TFIM, HAM_PAULI = 0, 1, 2
 
 
 class GateDesc(C.Structure):
@@ -33,7 +33,8 @@ class CircuitDesc(C.Structure):
 class PlanOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("hamiltonian", C.c_int), ("tfim_J", C.c_double), ("tfim_h", C.c_double),
                 ("lambda_", C.c_double), ("device", C.c_int32), ("use_graph", C.c_int32), ("batch", C.c_int32),
-                ("num_deriv_params", C.c_int32)]
+                ("num_deriv_params", C.c_int32), ("num_pauli_terms", C.c_int32), ("pauli_strings", C.c_char_p),
+                ("pauli_coeffs", C.c_void_p)]
 
 
 class PlanInfo(C.Structure):
@@ -185,12 +186,21 @@ class Plan:
     """A compiled circuit plan (qgt_plan_t)."""
 
     def __init__(self, n, gates, num_params=None, precision=MIXED, hamiltonian=HAM_TFIM, J=1.0, h=1.0,
-                 lam=1e-3, device=0, use_graph=True, batch=1, deriv_params=0):
+                 lam=1e-3, device=0, use_graph=True, batch=1, deriv_params=0, pauli=None):
+        """pauli: [(coeff, "XZIY..."), ...] selects the Pauli-sum Hamiltonian (character n-1-q acts on qubit q)."""
         L = lib()
         self.desc = circuit_desc(n, gates, num_params)
         o = PlanOptions()
         L.qgt_plan_default_options(C.byref(o))
         o.precision, o.hamiltonian, o.tfim_J, o.tfim_h = precision, hamiltonian, J, h
+        if pauli is not None:
+            strs = "".join(s_ for _, s_ in pauli)
+            if any(len(s_) != n for _, s_ in pauli):
+                raise ValueError("every Pauli string needs one character per qubit")
+            self._pauli = (strs.encode(), np.ascontiguousarray([c for c, _ in pauli], dtype=np.float64))
+            o.hamiltonian, o.num_pauli_terms = HAM_PAULI, len(pauli)
+            o.pauli_strings = self._pauli[0]
+            o.pauli_coeffs = self._pauli[1].ctypes.data
         o.lambda_, o.device, o.use_graph = lam, device, int(use_graph)
         o.batch, o.num_deriv_params = int(batch), int(deriv_params)
         self.opt = o

@@ -140,6 +140,55 @@ __global__ void prepare_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const do
 }
 
 // ---------------------------------------------------------------------------
+// Pauli sum: (H psi)_i = sum_k c_k i^ny_k (-1)^popc((i ^ x_k) & z_k) psi_{i ^ x_k}, scaled.
+// Terms are staged in shared memory; psi stays L2-resident across the terms.
+// ---------------------------------------------------------------------------
+template <typename T, typename R>
+__global__ void pauli_kernel(const T* __restrict__ psi, T* __restrict__ out, int64_t N,
+                             const qgt_dev_pauli_term_t* __restrict__ terms, int nterms, double inv,
+                             uint32_t* rowmax, int64_t point_stride, int32_t rowmax_stride)
+{
+    extern __shared__ qgt_dev_pauli_term_t st[];
+    for (int k = threadIdx.x; k < nterms; k += blockDim.x) st[k] = terms[k];
+    __syncthreads();
+    psi += blockIdx.y * point_stride;   // parameter point
+    out += blockIdx.y * point_stride;
+    if (rowmax) rowmax += (int64_t)blockIdx.y * rowmax_stride;
+    float vmax = 0.f;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        double ar = 0, ai = 0;
+        for (int k = 0; k < nterms; k++) {
+            const uint64_t j = (uint64_t)i ^ st[k].x;
+            const T v = psi[j];
+            double c = st[k].c;
+            if (__popcll(j & st[k].z) & 1) c = -c;
+            switch (st[k].ny & 3) {   // c i^ny
+            case 0: ar += c * (double)v.x; ai += c * (double)v.y; break;
+            case 1: ar -= c * (double)v.y; ai += c * (double)v.x; break;
+            case 2: ar -= c * (double)v.x; ai -= c * (double)v.y; break;
+            default: ar += c * (double)v.y; ai -= c * (double)v.x; break;
+            }
+        }
+        T o;
+        o.x = (R)(ar * inv);
+        o.y = (R)(ai * inv);
+        out[i] = o;
+        vmax = fmaxf(vmax, sqrtf((float)(o.x * o.x + o.y * o.y)));
+    }
+    if (rowmax) {
+        __shared__ float red[32];
+        for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = vmax;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float m = 0.f;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) m = fmaxf(m, red[w]);
+            atomicMax(rowmax, __float_as_uint(m));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // TFIM ring: (H psi)_i = -J zz(i) psi_i - h sum_q psi_{i ^ 2^q}, scaled
 // ---------------------------------------------------------------------------
 template <typename T, typename R>
@@ -384,6 +433,27 @@ int qgt_dev_tfim(const void* psi, void* out, int32_t n, double J, double h, doub
                                                                         (float)h, (float)inv, split, sld, pstride, srow,
                                                                         sscale, bf16, rowmax, point_stride,
                                                                         rowmax_stride);
+    return qgt_dev_last_error();
+}
+
+int qgt_dev_pauli(const void* psi, void* out, int32_t n, const qgt_dev_pauli_term_t* terms, int32_t nterms,
+                  double inv, int fp64, uint32_t* rowmax, int32_t npoints, int64_t point_stride, int32_t rowmax_stride,
+                  void* s)
+{
+    int64_t N = (int64_t)1 << n;
+    if (npoints < 1 || npoints > 65535 || nterms < 0) return qgt_set_error(QGT_EINVAL, "pauli: %d points", npoints);
+    int64_t want = (152 * 16 + npoints - 1) / npoints;
+    int blocks = (int)((N + 255) / 256);
+    if (blocks > want) blocks = (int)want;
+    dim3 grid((unsigned)blocks, (unsigned)npoints);
+    size_t smem = sizeof(qgt_dev_pauli_term_t) * (size_t)nterms;
+    if (smem > 48 * 1024) return qgt_set_error(QGT_EINVAL, "pauli: %d terms exceed shared memory", nterms);
+    if (fp64)
+        pauli_kernel<double2, double><<<grid, 256, smem, (cudaStream_t)s>>>((const double2*)psi, (double2*)out, N, terms,
+                                                                          nterms, inv, NULL, point_stride, 0);
+    else
+        pauli_kernel<float2, float><<<grid, 256, smem, (cudaStream_t)s>>>((const float2*)psi, (float2*)out, N, terms,
+                                                                        nterms, inv, rowmax, point_stride, rowmax_stride);
     return qgt_dev_last_error();
 }
 

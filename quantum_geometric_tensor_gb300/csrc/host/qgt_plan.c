@@ -110,6 +110,9 @@ struct qgt_plan {
     qgt_tc_gram_t* tc;            /* split-BF16 x3 Gram (operands written by the last pass) */
     qgt_dg_gram_t* dg;            /* integer-digit FP16 Gram (mixed default) */
     double* small_part_d;         /* partials of the small Gram (rows <= 8) */
+    qgt_dev_pauli_term_t* pauli_h; /* Pauli-sum Hamiltonian terms (host / device) */
+    qgt_dev_pauli_term_t* pauli_d;
+    int npauli;
     int small_nsplit;
     uint32_t* rowmax_d;           /* per-row max |amplitude| (float bits) for the digit Gram */
     double *Q_d, *grad_d, *energy_d, *natgrad_d, *chol_work_d, *status_d;
@@ -596,6 +599,11 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
         return qgt_set_error(E_INVAL, "qgt_plan_create: unknown precision %d", bad);
     }
     if (!(p->opt.lambda >= 0) || !isfinite(p->opt.lambda)) { free(p); return qgt_set_error(E_INVAL, "lambda must be >= 0"); }
+    if (p->opt.hamiltonian < QGT_HAMILTONIAN_NONE || p->opt.hamiltonian > QGT_HAMILTONIAN_PAULI) {
+        int bad = (int)p->opt.hamiltonian;
+        free(p);
+        return qgt_set_error(E_INVAL, "qgt_plan_create: unknown Hamiltonian %d", bad);
+    }
     p->n = c->num_qubits;
     p->N = (int64_t)1 << p->n;
     p->P = c->num_params;
@@ -654,7 +662,34 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
     if ((rc = build_entries(p)) != 0) goto fail;
     if ((rc = build_programs(p)) != 0) goto fail;
     if ((rc = fold_diagonal_runs(p)) != 0) goto fail;
-    {
+    if (p->opt.hamiltonian == QGT_HAMILTONIAN_PAULI) {
+        /* parse the strings: character [n-1-q] acts on qubit q */
+        const int T = p->opt.num_pauli_terms;
+        if (T < 1 || T > 2048 || !p->opt.pauli_strings || !p->opt.pauli_coeffs) {
+            rc = qgt_set_error(E_INVAL, "Pauli Hamiltonian: 1..2048 terms with strings and coefficients required");
+            goto fail;
+        }
+        p->pauli_h = (qgt_dev_pauli_term_t*)calloc((size_t)T, sizeof(qgt_dev_pauli_term_t));
+        if (!p->pauli_h) { rc = qgt_set_error(E_NOMEM, "oom"); goto fail; }
+        p->hscale = 0;
+        for (int k = 0; k < T; k++) {
+            const char* str = p->opt.pauli_strings + (size_t)k * p->n;
+            qgt_dev_pauli_term_t* t = &p->pauli_h[k];
+            t->c = p->opt.pauli_coeffs[k];
+            if (!isfinite(t->c)) { rc = qgt_set_error(E_INVAL, "Pauli coefficient %d is not finite", k); goto fail; }
+            for (int q = 0; q < p->n; q++) {
+                const char ch = str[p->n - 1 - q];
+                if (ch == 'X' || ch == 'x') t->x |= 1u << q;
+                else if (ch == 'Y' || ch == 'y') { t->x |= 1u << q; t->z |= 1u << q; t->ny++; }
+                else if (ch == 'Z' || ch == 'z') t->z |= 1u << q;
+            }
+            p->hscale += fabs(t->c);
+        }
+        p->npauli = T;
+        p->opt.pauli_strings = NULL;   /* copied; the caller's buffers need not outlive the call */
+        p->opt.pauli_coeffs = NULL;
+        if (p->hscale <= 0) p->hscale = 1.0;
+    } else {
         int nb = p->n >= 3 ? p->n : p->n - 1;
         p->hscale = fabs(p->opt.tfim_J) * nb + fabs(p->opt.tfim_h) * p->n;
         if (p->hscale <= 0) p->hscale = 1.0;
@@ -691,6 +726,12 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
         DALLOC(p->natgrad_d, sizeof(double) * (B * Pd + 1));
         DALLOC(p->chol_work_d, sizeof(double) * B * Pd * Pd);
         DALLOC(p->status_d, sizeof(double) * 2 * B);
+    }
+    if (p->npauli) {
+        DALLOC(p->pauli_d, sizeof(qgt_dev_pauli_term_t) * (size_t)p->npauli);
+        if ((rc = qgt_dev_memcpy_h2d(p->pauli_d, p->pauli_h, sizeof(qgt_dev_pauli_term_t) * (size_t)p->npauli,
+                                     p->stream)) != 0)
+            goto fail;
     }
     DALLOC(p->slot_param_d, sizeof(int32_t) * (size_t)(p->nslots + 1));
     DALLOC(p->param_ptr_d, sizeof(int32_t) * (size_t)(p->Pd + 2));
@@ -767,7 +808,8 @@ void qgt_plan_destroy(qgt_plan_t* p)
     qgt_dev_tc_gram_destroy(p->tc);
     qgt_dev_dg_gram_destroy(p->dg);
     qgt_dev_free(p->rowmax_d);
-    void* dev[] = {p->V, p->split, p->small_part_d, p->ops_d, p->ents_d, p->prog_d, p->segs_d, p->coef32_d, p->coef_desc_d, p->coef_d, p->theta_d, p->HG_d, p->part_d,
+    free(p->pauli_h);
+    void* dev[] = {p->V, p->split, p->small_part_d, p->pauli_d, p->ops_d, p->ents_d, p->prog_d, p->segs_d, p->coef32_d, p->coef_desc_d, p->coef_d, p->theta_d, p->HG_d, p->part_d,
                    p->Q_d, p->grad_d, p->energy_d, p->natgrad_d, p->chol_work_d, p->status_d, p->slot_param_d,
                    p->param_ptr_d, p->param_slots_d};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++) qgt_dev_free(dev[i]);
@@ -892,8 +934,15 @@ static int run_step(qgt_plan_t* p)
         (void)onef;
     }
     MARK(2);
-    const int has_h = p->opt.hamiltonian == QGT_HAMILTONIAN_TFIM;
-    if (has_h) {
+    const int has_h = p->opt.hamiltonian != QGT_HAMILTONIAN_NONE;
+    if (p->opt.hamiltonian == QGT_HAMILTONIAN_PAULI) {
+        size_t ab = p->fp64 ? 16 : 8;
+        void* row1 = (char*)p->V + (size_t)p->N * ab;
+        if ((rc = qgt_dev_pauli(p->V, row1, p->n, p->pauli_d, p->npauli, 1.0 / p->hscale, p->fp64,
+                                p->rowmax_d ? p->rowmax_d + 1 : NULL, p->B, p->pstride, p->rows, p->stream)) != 0)
+            return rc;
+        launches++;
+    } else if (has_h) {
         size_t ab = p->fp64 ? 16 : 8;
         void* row1 = (char*)p->V + (size_t)p->N * ab;
         if ((rc = qgt_dev_tfim(p->V, row1, p->n, p->opt.tfim_J, p->opt.tfim_h, 1.0 / p->hscale, p->fp64,
@@ -1002,7 +1051,7 @@ int qgt_plan_execute_device(qgt_plan_t* p, const double* theta_dev, double* Q_de
     if (p->P > 0 && theta_dev && theta_dev != p->theta_d)
         if ((rc = qgt_dev_memcpy_d2d(p->theta_d, theta_dev, sizeof(double) * B * (size_t)p->P, p->stream)) != 0) return rc;
     if ((rc = launch_step(p)) != 0) return rc;
-    int has_h = p->opt.hamiltonian == QGT_HAMILTONIAN_TFIM;
+    int has_h = p->opt.hamiltonian != QGT_HAMILTONIAN_NONE;
     if (Q_dev && Q_dev != p->Q_d && (rc = qgt_dev_memcpy_d2d(Q_dev, p->Q_d, sizeof(double) * 2 * B * Pd * Pd, p->stream)) != 0) return rc;
     if (has_h) {
         if (grad_dev && grad_dev != p->grad_d && (rc = qgt_dev_memcpy_d2d(grad_dev, p->grad_d, sizeof(double) * B * Pd, p->stream)) != 0) return rc;
@@ -1020,7 +1069,7 @@ int qgt_plan_execute_host(qgt_plan_t* p, const double* theta, double* Q, double*
     const size_t B = (size_t)p->B, Pd = (size_t)p->Pd, nth = B * (size_t)p->P;
     for (size_t k = 0; k < nth; k++)
         if (!isfinite(theta[k])) return qgt_set_error(E_INVAL, "qgt_plan_execute_host: theta[%zu] is not finite", k);
-    int has_h = p->opt.hamiltonian == QGT_HAMILTONIAN_TFIM;
+    int has_h = p->opt.hamiltonian != QGT_HAMILTONIAN_NONE;
     if ((grad || energy || natgrad) && !has_h)
         return qgt_set_error(E_INVAL, "qgt_plan_execute_host: energy outputs need a Hamiltonian");
     if (p->P > 0) {

@@ -471,7 +471,7 @@ int qgt_vqe_run(const qgt_circuit_desc_t* c, const qgt_plan_options_t* popt, qgt
         return qgt_set_error(E_INVAL, "qgt_vqe_run: the learned solver needs a preconditioner for %d parameters", c->num_params);
     qgt_plan_options_t o;
     if (popt) o = *popt; else qgt_plan_default_options(&o);
-    o.hamiltonian = QGT_HAMILTONIAN_TFIM;
+    if (o.hamiltonian == QGT_HAMILTONIAN_NONE) o.hamiltonian = QGT_HAMILTONIAN_TFIM;
     o.batch = 1;
     o.num_deriv_params = 0;
     const int P = c->num_params;

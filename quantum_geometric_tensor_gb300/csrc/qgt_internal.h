@@ -200,6 +200,16 @@ int qgt_dev_tfim(const void* psi, void* out, int32_t n, double J, double h, doub
                  int fp64, void* split, int64_t split_ld, int64_t split_plane_stride, int32_t split_row,
                  float split_scale, int32_t split_bf16, uint32_t* rowmax_slot, int32_t npoints,
                  int64_t point_stride, int32_t rowmax_stride, void* stream);
+/* one Pauli term: P|j> = i^ny (-1)^popc(j & z) |j ^ x> */
+typedef struct {
+    double c;
+    uint32_t x, z;
+    int32_t ny, pad;
+} qgt_dev_pauli_term_t;
+/* out = (sum_k c_k P_k) psi * inv_hscale per point (rowmax slot as for qgt_dev_tfim) */
+int qgt_dev_pauli(const void* psi, void* out, int32_t n, const qgt_dev_pauli_term_t* terms, int32_t nterms,
+                  double inv_hscale, int fp64, uint32_t* rowmax_slot, int32_t npoints, int64_t point_stride,
+                  int32_t rowmax_stride, void* stream);
 /* complex128 -> complex64 rows */
 int qgt_dev_c128_to_c64(const double* X, int64_t count, float* Y, void* stream);
 /* rowmax[row0 + r] = max(rowmax, max_k |V[row0 + r][k]|) over complex64 rows (float bits) */

@@ -109,3 +109,25 @@ def test_berry_map_matches_full_qgt(orc):
             t[3] = 2 * math.pi * j / grid
             Q = orc.qgt(3, g, t)
             assert abs(m[i, j] - Q[0, 3].imag) < 1e-14
+
+
+def test_pauli_apply_matches_reference_expectation(orc):
+    """or_pauli_apply (the oracle's H psi for Pauli sums) against the reference's own
+    compute_pauli_expectation term by term (compiled from its sources when present)."""
+    try:
+        ref = O.Reference()
+    except FileNotFoundError:
+        pytest.skip("reference objects not built (no reference tree on this host)")
+    rng = np.random.default_rng(4)
+    n = 5
+    psi = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    psi /= np.linalg.norm(psi)
+    terms = [(float(rng.standard_normal()), "".join(rng.choice(list("IXYZxyz"), n))) for _ in range(12)]
+    terms.append((0.7, "XZ"))   # wrong length: contributes nothing
+    hp = orc.pauli_apply(n, psi, terms)
+    e = float(np.real(np.vdot(psi, hp)))
+    e_ref = sum(c * ref.pauli_expectation(psi, n, s) for c, s in terms if len(s) == n)
+    assert abs(e - e_ref) < 1e-13
+    # the TFIM ring as Pauli strings equals the dedicated TFIM apply
+    tf = [(c, s) for c, s in O.tfim_pauli_strings(n)]
+    assert np.abs(orc.pauli_apply(n, psi, tf) - orc.tfim_apply(n, psi)).max() < 1e-13
