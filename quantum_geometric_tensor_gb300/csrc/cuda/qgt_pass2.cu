@@ -87,8 +87,8 @@ __device__ __forceinline__ double2 shfl_x<double2>(double2 v, int mask)
 }
 
 // ---- butterflies on a register bit ----
-template <int RI, int NR, typename T, typename R>
-__device__ __forceinline__ void u_reg(T* v, const R* m, bool real)
+template <int RI, int NR, bool real, typename T, typename R>
+__device__ __forceinline__ void u_reg(T* v, const R* m)
 {
 #pragma unroll
     for (int j = 0; j < NR; j++) {
@@ -365,9 +365,15 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
             const bool real = op.kind == Q2_UR;
             if (op.ra >= RL_REG) {
                 const int ri = op.ra - RL_REG;
-#define U_CALL(I) u_reg<I, NR, T, R>(v, m, real)
-                RB_SWITCH(ri, U_CALL)
+                if (real) {
+#define U_CALL(I) u_reg<I, NR, true, T, R>(v, m)
+                    RB_SWITCH(ri, U_CALL)
 #undef U_CALL
+                } else {
+#define U_CALL(I) u_reg<I, NR, false, T, R>(v, m)
+                    RB_SWITCH(ri, U_CALL)
+#undef U_CALL
+                }
             } else {
                 // lane bit: v' = c_self v + c_partner w (w = the partner lane's amplitude);
                 // row 1 of the matrix for the upper lane, row 0 for the lower one
