@@ -105,7 +105,16 @@ typedef struct {
     int32_t num_pauli_terms;
     const char* pauli_strings;
     const double* pauli_coeffs;
+    /* how derivative states reach the Gram: QGT_TRANSPORT_AUTO (meet in the
+     * middle for mixed plans with >= 16 derivative slots, forward otherwise),
+     * QGT_TRANSPORT_FORWARD (every state carried to the end of the circuit),
+     * QGT_TRANSPORT_MEET (states of the first half carried forward to a cut,
+     * those of the second half carried backward to it from the end through
+     * the inverse gates; inner products are unchanged by the common unitary,
+     * so Q is the same with about half the gate work) */
+    int32_t transport;
 } qgt_plan_options_t;
+enum { QGT_TRANSPORT_AUTO = 0, QGT_TRANSPORT_FORWARD = 1, QGT_TRANSPORT_MEET = 2 };
 
 typedef struct qgt_plan qgt_plan_t;
 
@@ -118,6 +127,7 @@ typedef struct {
     int64_t gram_flops;                                    /* 4 P (P+1) N: algorithmic Gram flops per step */
     int64_t device_bytes;                                  /* device memory held by the plan */
     int32_t batch, num_deriv_params;                       /* points per step; output width Pd */
+    int32_t meet_in_middle, cut_gate;                      /* transport used; first gate of the backward half */
 } qgt_plan_info_t;
 
 /* Default options: MIXED, TFIM J = h = 1, lambda = 1e-3, device 0, graph on. */
@@ -154,7 +164,9 @@ void* qgt_plan_stream(qgt_plan_t* plan);
 int qgt_plan_get_state(qgt_plan_t* plan, double* psi);
 /* Row r of the plan's vector buffer after the last step, as 2^n complex
  * doubles: r = 0 psi, r = 1 (H psi)/hscale, r = 2 + s derivative slot s
- * (d psi / d angle of the s-th parameterised gate).  FP64 plans only.
+ * (d psi / d angle of the s-th parameterised gate).  With meet-in-the-middle
+ * transport the rows are those states carried to the cut (U_2^dagger applied,
+ * U_2 the gates from the cut on), which leaves every inner product as it is.
  * Replaces compute_quantum_gradient's state output
  * (src/quantum_geometric/core/quantum_geometric_gradient.c:1062). */
 int qgt_plan_get_row(qgt_plan_t* plan, int row, double* out);

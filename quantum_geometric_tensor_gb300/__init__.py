@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(PKG, "lib", "libqgt_gb300.so")
 I, X, Y, Z, H, S, T, RX, RY, RZ, CNOT, CZ, SWAP = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 12, 13
 FP64, MIXED, MIXED_BF16X3 = 0, 1, 2
 HAM_NONE, HAM_TFIM, HAM_PAULI = 0, 1, 2
+TRANSPORT_AUTO, TRANSPORT_FORWARD, TRANSPORT_MEET = 0, 1, 2
 
 
 class GateDesc(C.Structure):
@@ -34,7 +35,7 @@ class PlanOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("hamiltonian", C.c_int), ("tfim_J", C.c_double), ("tfim_h", C.c_double),
                 ("lambda_", C.c_double), ("device", C.c_int32), ("use_graph", C.c_int32), ("batch", C.c_int32),
                 ("num_deriv_params", C.c_int32), ("num_pauli_terms", C.c_int32), ("pauli_strings", C.c_char_p),
-                ("pauli_coeffs", C.c_void_p)]
+                ("pauli_coeffs", C.c_void_p), ("transport", C.c_int32)]
 
 
 class PlanInfo(C.Structure):
@@ -42,7 +43,7 @@ class PlanInfo(C.Structure):
                 ("num_rows", C.c_int32), ("num_passes", C.c_int32), ("num_launches", C.c_int32),
                 ("tile_bits", C.c_int32), ("vector_passes", C.c_int64), ("gate_bytes", C.c_int64),
                 ("gram_flops", C.c_int64), ("device_bytes", C.c_int64), ("batch", C.c_int32),
-                ("num_deriv_params", C.c_int32)]
+                ("num_deriv_params", C.c_int32), ("meet_in_middle", C.c_int32), ("cut_gate", C.c_int32)]
 
 
 class BatchOptions(C.Structure):
@@ -186,7 +187,7 @@ class Plan:
     """A compiled circuit plan (qgt_plan_t)."""
 
     def __init__(self, n, gates, num_params=None, precision=MIXED, hamiltonian=HAM_TFIM, J=1.0, h=1.0,
-                 lam=1e-3, device=0, use_graph=True, batch=1, deriv_params=0, pauli=None):
+                 lam=1e-3, device=0, use_graph=True, batch=1, deriv_params=0, pauli=None, transport=0):
         """pauli: [(coeff, "XZIY..."), ...] selects the Pauli-sum Hamiltonian (character n-1-q acts on qubit q)."""
         L = lib()
         self.desc = circuit_desc(n, gates, num_params)
@@ -202,7 +203,7 @@ class Plan:
             o.pauli_strings = self._pauli[0]
             o.pauli_coeffs = self._pauli[1].ctypes.data
         o.lambda_, o.device, o.use_graph = lam, device, int(use_graph)
-        o.batch, o.num_deriv_params = int(batch), int(deriv_params)
+        o.batch, o.num_deriv_params, o.transport = int(batch), int(deriv_params), int(transport)
         self.opt = o
         h_ = C.c_void_p()
         _check(L.qgt_plan_create(C.byref(self.desc), C.byref(o), C.byref(h_)), "qgt_plan_create")

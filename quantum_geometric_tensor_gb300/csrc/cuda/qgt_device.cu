@@ -119,7 +119,10 @@ __global__ void prepare_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const do
     theta += (int64_t)blockIdx.y * theta_stride;   // parameter point
     coef += (int64_t)8 * blockIdx.y * ncoef;
     qgt_dev_coef_desc_t g = d[c];
+    const int inv = (g.type & QGT_COEF_INVERSE) != 0;   // the gate's inverse (backward transport)
+    g.type &= ~QGT_COEF_INVERSE;
     double a = g.param >= 0 ? theta[g.param] : g.angle;
+    if (inv) a = -a;
     double m[8] = {1, 0, 0, 0, 0, 0, 1, 0};
     double cs, sn;
     sincos(0.5 * a, &sn, &cs);
@@ -132,8 +135,8 @@ __global__ void prepare_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const do
     case QGT_GATE_Y: m[0] = 0; m[2] = 0; m[3] = -1; m[4] = 0; m[5] = 1; m[6] = 0; break;
     case QGT_GATE_Z: m[6] = -1; break;
     case QGT_GATE_H: m[0] = r; m[2] = r; m[4] = r; m[6] = -r; break;
-    case QGT_GATE_S: m[6] = 0; m[7] = 1; break;
-    case QGT_GATE_T: m[6] = r; m[7] = r; break;
+    case QGT_GATE_S: m[6] = 0; m[7] = inv ? -1 : 1; break;
+    case QGT_GATE_T: m[6] = r; m[7] = inv ? -r : r; break;
     default: break;
     }
     for (int i = 0; i < 8; i++) coef[8 * c + i] = m[i];
@@ -263,6 +266,20 @@ __device__ __forceinline__ double2 hg(const double* HG, int rows, int i, int j)
     return make_double2(HG[2 * ((int64_t)i * rows + j)], HG[2 * ((int64_t)i * rows + j) + 1]);
 }
 
+// HG entry with the meet-in-the-middle scale correction: rows transported
+// backward (row 1 and rows >= late_row0) carry an extra factor rho
+__device__ __forceinline__ double2 hgs(const qgt_dev_post_args_t& a, int i, int j, double inv_rho)
+{
+    double2 v = hg(a.HG, a.rows, i, j);
+    if (a.late_scale) {
+        const int li = (i == 1 || (a.late_row0 > 0 && i >= a.late_row0)), lj = (j == 1 || (a.late_row0 > 0 && j >= a.late_row0));
+        const double f = (li && lj) ? inv_rho * inv_rho : ((li || lj) ? inv_rho : 1.0);
+        v.x *= f;
+        v.y *= f;
+    }
+    return v;
+}
+
 __global__ void post_qgt_kernel(qgt_dev_post_args_t a)
 {
     int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -271,19 +288,20 @@ __global__ void post_qgt_kernel(qgt_dev_post_args_t a)
     a.HG += (int64_t)2 * blockIdx.y * a.rows * a.rows;   // parameter point
     a.Q += (int64_t)2 * blockIdx.y * P * P;
     int p = (int)(idx / P), q = (int)(idx % P);
+    const double ir = a.late_scale ? 1.0 / a.late_scale[blockIdx.y] : 1.0;
     double s = a.HG[0];
     double2 B = make_double2(0, 0), vp = make_double2(0, 0), vq = make_double2(0, 0);
     for (int x = a.param_ptr[p]; x < a.param_ptr[p + 1]; x++) {
         int sa = a.param_slots[x];
-        double2 t = hg(a.HG, a.rows, sa + 2, 0);
+        double2 t = hgs(a, sa + 2, 0, ir);
         vp.x += t.x; vp.y += t.y;
         for (int y = a.param_ptr[q]; y < a.param_ptr[q + 1]; y++) {
-            double2 u = hg(a.HG, a.rows, sa + 2, a.param_slots[y] + 2);
+            double2 u = hgs(a, sa + 2, a.param_slots[y] + 2, ir);
             B.x += u.x; B.y += u.y;
         }
     }
     for (int y = a.param_ptr[q]; y < a.param_ptr[q + 1]; y++) {
-        double2 t = hg(a.HG, a.rows, a.param_slots[y] + 2, 0);
+        double2 t = hgs(a, a.param_slots[y] + 2, 0, ir);
         vq.x += t.x; vq.y += t.y;
     }
     // v_p conj(v_q)
@@ -299,15 +317,16 @@ __global__ void post_grad_kernel(qgt_dev_post_args_t a)
     a.HG += (int64_t)2 * blockIdx.y * a.rows * a.rows;   // parameter point
     a.grad += (int64_t)blockIdx.y * a.P;
     if (a.energy) a.energy += blockIdx.y;
+    const double ir = a.late_scale ? 1.0 / a.late_scale[blockIdx.y] : 1.0;
     double s = a.HG[0];
-    double E = a.hscale * hg(a.HG, a.rows, 0, 1).x / s;
+    double E = a.hscale * hgs(a, 0, 1, ir).x / s;
     if (threadIdx.x == 0 && blockIdx.x == 0 && a.energy) a.energy[0] = E;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.P; p += gridDim.x * blockDim.x) {
         double g = 0, v = 0;
         for (int x = a.param_ptr[p]; x < a.param_ptr[p + 1]; x++) {
             int sa = a.param_slots[x];
-            g += hg(a.HG, a.rows, sa + 2, 1).x;
-            v += hg(a.HG, a.rows, sa + 2, 0).x;
+            g += hgs(a, sa + 2, 1, ir).x;
+            v += hgs(a, sa + 2, 0, ir).x;
         }
         // d/dtheta <psi|H|psi>/<psi|psi> = 2 Re<d psi|H psi>/s - 2 E Re<d psi|psi>/s
         a.grad[p] = 2.0 * a.hscale * g / s - 2.0 * E * v / s;
@@ -616,9 +635,12 @@ __global__ void prepare32_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const 
     theta += (int64_t)blockIdx.y * theta_stride;   // parameter point
     coef += (int64_t)8 * blockIdx.y * ncoef;
     qgt_dev_coef_desc_t g = d[c];
+    const int inv = (g.type & QGT_COEF_INVERSE) != 0;   // the gate's inverse (backward transport)
+    g.type &= ~QGT_COEF_INVERSE;
     float m[8] = {1.f, 0.f, 0.f, 0.f, 0.f, 0.f, 1.f, 0.f};
     if (g.type == QGT_GATE_RX || g.type == QGT_GATE_RY || g.type == QGT_GATE_RZ) {
         double a = g.param >= 0 ? theta[g.param] : g.angle;
+        if (inv) a = -a;
         double s0, c0;
         sincos(0.5 * a, &s0, &c0);
         double best = 1e300;
@@ -645,12 +667,45 @@ __global__ void prepare32_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const 
         case QGT_GATE_Y: m[0] = 0; m[3] = -1; m[5] = 1; m[6] = 0; break;
         case QGT_GATE_Z: m[6] = -1; break;
         case QGT_GATE_H: m[0] = r; m[2] = r; m[4] = r; m[6] = -r; break;
-        case QGT_GATE_S: m[6] = 0; m[7] = 1; break;
-        case QGT_GATE_T: m[0] = (float)sqrt(2.0 * (double)r * (double)r); m[6] = r; m[7] = r; break;
+        case QGT_GATE_S: m[6] = 0; m[7] = inv ? -1.f : 1.f; break;
+        case QGT_GATE_T: m[0] = (float)sqrt(2.0 * (double)r * (double)r); m[6] = r; m[7] = inv ? -r : r; break;
         default: break;
         }
     }
     if (lane < 8) coef[8 * c + lane] = m[lane];
+}
+
+// rho[point] = prod over the listed coefficient entries of |first column|^2 of
+// their complex64 matrices (the entries' uniform scale factors squared... each
+// entry contributes its amplitude scale r = |column|; the product is taken in
+// FP64 from the exact FP32 values)
+__global__ void scale_product_kernel(const float* __restrict__ coef, int ncoef, const int32_t* __restrict__ list, int n,
+                                     double* __restrict__ rho)
+{
+    __shared__ double red[32];
+    coef += (int64_t)8 * blockIdx.x * ncoef;
+    double lg = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float* m = coef + 8 * list[i];
+        const double r2 = (double)m[0] * m[0] + (double)m[1] * m[1] + (double)m[4] * m[4] + (double)m[5] * m[5];
+        lg += 0.5 * log(r2);
+    }
+    for (int o = 16; o > 0; o >>= 1) lg += __shfl_xor_sync(0xffffffffu, lg, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lg;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+        rho[blockIdx.x] = exp(t);
+    }
+}
+
+extern "C" int qgt_dev_scale_product(const float* coef32, int32_t ncoef, const int32_t* list, int32_t n, double* rho,
+                                     int32_t npoints, void* s)
+{
+    if (npoints < 1 || n < 0) return qgt_set_error(QGT_EINVAL, "scale product: bad arguments");
+    scale_product_kernel<<<npoints, 256, 0, (cudaStream_t)s>>>(coef32, ncoef, list, n, rho);
+    return qgt_dev_last_error();
 }
 
 extern "C" int qgt_dev_prepare32(const qgt_dev_coef_desc_t* d, int32_t ncoef, const double* theta, float* coef,

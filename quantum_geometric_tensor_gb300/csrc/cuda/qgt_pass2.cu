@@ -73,6 +73,40 @@ __device__ __forceinline__ T rmad2(R a, T x, R b, T y)  // real a x + b y
     return o;
 }
 
+// complex64: packed FP32x2 arithmetic (one instruction per two lanes of a
+// complex number); per component the same rounding as fmaf
+template <>
+__device__ __forceinline__ float2 rmad2<float2, float>(float a, float2 x, float b, float2 y)
+{
+    return __ffma2_rn(make_float2(a, a), x, __fmul2_rn(make_float2(b, b), y));
+}
+
+template <>
+__device__ __forceinline__ float2 cmad2<float2, float>(const float* m, float2 x, float2 y)
+{
+    // (m0 + i m1) x + (m2 + i m3) y with i z = (-z.y, z.x)
+    const float2 xs = make_float2(-x.y, x.x), ys = make_float2(-y.y, y.x);
+    float2 o = __fmul2_rn(make_float2(m[3], m[3]), ys);
+    o = __ffma2_rn(make_float2(m[2], m[2]), y, o);
+    o = __ffma2_rn(make_float2(m[1], m[1]), xs, o);
+    return __ffma2_rn(make_float2(m[0], m[0]), x, o);
+}
+
+// (pr + i pi) x
+template <typename T, typename R>
+__device__ __forceinline__ T cmul_s(R pr, R pi, T x)
+{
+    T o;
+    o.x = pr * x.x - pi * x.y;
+    o.y = pr * x.y + pi * x.x;
+    return o;
+}
+template <>
+__device__ __forceinline__ float2 cmul_s<float2, float>(float pr, float pi, float2 x)
+{
+    return __ffma2_rn(make_float2(pr, pr), x, __fmul2_rn(make_float2(pi, pi), make_float2(-x.y, x.x)));
+}
+
 template <typename T>
 __device__ __forceinline__ T shfl_x(T v, int mask);
 template <>
@@ -338,9 +372,7 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
                 const R hr = thr[j >> LB], hi2 = thi[j >> LB], lr = tlr[j & ((1 << LB) - 1)], li = tli[j & ((1 << LB) - 1)];
                 R pr = lr * hr - li * hi2, pi = lr * hi2 + li * hr;
                 if ((sgn >> j) & 1u) { pr = -pr; pi = -pi; }
-                const T x = v[j];
-                v[j].x = pr * x.x - pi * x.y;
-                v[j].y = pr * x.y + pi * x.x;
+                v[j] = cmul_s<T, R>(pr, pi, v[j]);
             }
             if (e.spawn_op > pc && e.spawn_op <= pc + cnt) {
                 // (-i/2) Z of the spawning rotation, after the run (diagonal ops commute)

@@ -59,6 +59,7 @@ typedef struct {
 } sgate_t;
 
 typedef struct {
+    int part;                     /* 0 forward (with first-half slots); meet in the middle: 1 psi forward, 2 backward */
     int op_begin, op_count;
     int ent_begin, ent_count;
     int prog_begin, prog_count;   /* register-resident program (full tiles), 0 = v1 pass */
@@ -71,6 +72,16 @@ struct qgt_plan {
     qgt_plan_options_t opt;
     int n, P, nslots, rows, rows_pad;
     int B;                        /* parameter points per step (theta batch) */
+    /* meet in the middle: gates [0, cut) forward with their slots, psi alone
+     * through [cut, G), then [cut, G) backward (inverse gates) with the
+     * second-half slots; part_begin[] delimits the three parts in `gates` */
+    int mitm, cut, nparts, early_slots, row_T, orig_ngates;
+    int host_only;                /* schedule only (no device resources): qgt_plan_schedule_dump */
+    int part_begin[4];
+    int32_t* late_coef_h;
+    int nlate_coef;
+    int32_t* late_coef_d;
+    double* rho_d;
     int Pd;                       /* parameters [0, Pd) get derivative rows; Q is Pd x Pd */
     int64_t pstride;              /* amplitudes between points in V: (rows + 1) N */
     int64_t N, split_ld;
@@ -222,17 +233,20 @@ static int compile_schedule(qgt_plan_t* p)
         free(placed); free(blocked); free(order);
         return qgt_set_error(E_NOMEM, "schedule: out of memory");
     }
+    int nord = 0, np = 0;
+    for (int part = 0; part < p->nparts; part++) {
+    const int g0 = p->part_begin[part], g1 = p->part_begin[part + 1];
     int remaining = 0;
-    for (int g = 0; g < G; g++) {
+    for (int g = g0; g < g1; g++) {
         if (p->gates[g].type == QGT_GATE_I && p->gates[g].slot < 0) placed[g] = 1;
         else remaining++;
     }
-    int nord = 0, np = 0, first = 0;
+    int first = g0;
     while (remaining > 0) {
         uint32_t S = (lane >= 32) ? 0xffffffffu : ((1u << lane) - 1u);
         int nb = 0, start = nord;
-        while (first < G && placed[first]) first++;
-        for (int g = first; g < G; g++) {
+        while (first < g1 && placed[first]) first++;
+        for (int g = first; g < g1; g++) {
             if (placed[g]) continue;
             const sgate_t* cg = &p->gates[g];
             int ok = 1;
@@ -260,6 +274,7 @@ static int compile_schedule(qgt_plan_t* p)
         }
         spass_t* ps = &p->passes[np++];
         memset(ps, 0, sizeof *ps);
+        ps->part = part;
         ps->tile_mask = S;
         ps->tile_bits = popcount32(S);
         int8_t p2l[32];
@@ -298,6 +313,7 @@ static int compile_schedule(qgt_plan_t* p)
             default: op->kind = QOP_PHASE; break; /* identity never reaches here */
             }
         }
+    }
     }
     p->npasses = np;
     p->nops = nord;
@@ -381,6 +397,204 @@ static int build_entries(qgt_plan_t* p)
     p->nents = ne;
     free(live);
     return 0;
+}
+
+/* Transport choice.  Meet in the middle: with S slots numbered in gate
+ * order, the cut is the gate of slot S/2.  The gate list becomes three parts:
+ *   F  gates [0, cut) with slots 0 .. S/2-1 (carried forward to the cut),
+ *   P  gates [cut, G) on psi alone (psi(G) for H psi),
+ *   B  gates G-1 .. cut as inverses, slots S/2 .. S-1 spawned on the way
+ *      (psi(k-) = U^dagger psi(G) before gate k; (-i/2) G_k psi(k-) carried
+ *      backward to the cut), together with H psi carried backward.
+ * Every Gram entry is then taken at the cut; <U a|U b> = <a|b> leaves Q,
+ * the energy and the gradient unchanged. */
+static int setup_transport(qgt_plan_t* p)
+{
+    p->nparts = 1;
+    p->part_begin[0] = 0;
+    p->part_begin[1] = p->ngates;
+    p->orig_ngates = p->ngates;
+    p->mitm = 0;
+    const int want = p->opt.transport;
+    if (want < QGT_TRANSPORT_AUTO || want > QGT_TRANSPORT_MEET)
+        return qgt_set_error(E_INVAL, "qgt_plan_create: unknown transport %d", want);
+    if (want == QGT_TRANSPORT_MEET && p->opt.precision == QGT_PRECISION_MIXED_BF16X3)
+        return qgt_set_error(E_INVAL, "qgt_plan_create: meet-in-the-middle transport needs FP64 or MIXED precision");
+    p->mitm = (want == QGT_TRANSPORT_MEET) ||
+              (want == QGT_TRANSPORT_AUTO && p->opt.precision == QGT_PRECISION_MIXED && p->nslots >= 16);
+    if (p->nslots < 2) p->mitm = 0;
+    if (!p->mitm) return 0;
+    const int G = p->ngates, half = p->nslots / 2;
+    int c = -1;
+    for (int g = 0; g < G && c < 0; g++)
+        if (p->gates[g].slot == half) c = g;
+    if (c <= 0) { p->mitm = 0; return 0; }
+    const int L2 = G - c;
+    sgate_t* ext = (sgate_t*)calloc((size_t)(c + 2 * L2) + 1, sizeof(sgate_t));
+    qgt_dev_coef_desc_t* nc = (qgt_dev_coef_desc_t*)realloc(p->coef_h, sizeof(qgt_dev_coef_desc_t) * ((size_t)p->ncoef + L2 + 1));
+    if (nc) p->coef_h = nc;
+    p->late_coef_h = (int32_t*)malloc(sizeof(int32_t) * (2 * (size_t)L2 + 1));
+    if (!ext || !nc || !p->late_coef_h) { free(ext); return qgt_set_error(E_NOMEM, "transport: out of memory"); }
+    int nl = 0;
+    for (int g = 0; g < c; g++) ext[g] = p->gates[g];
+    for (int g = c; g < G; g++) {
+        ext[g] = p->gates[g];
+        ext[g].slot = -1;
+        if (ext[g].coef >= 0) p->late_coef_h[nl++] = ext[g].coef;
+    }
+    for (int k = 0; k < L2; k++) {
+        sgate_t e = p->gates[G - 1 - k];
+        if (e.coef >= 0) {
+            const int ni = p->ncoef++;
+            p->coef_h[ni] = p->coef_h[e.coef];
+            p->coef_h[ni].type |= QGT_COEF_INVERSE;
+            e.coef = ni;
+            p->late_coef_h[nl++] = ni;
+        }
+        ext[c + L2 + k] = e;
+    }
+    free(p->gates);
+    p->gates = ext;
+    p->ngates = c + 2 * L2;
+    p->nparts = 3;
+    p->part_begin[0] = 0;
+    p->part_begin[1] = c;
+    p->part_begin[2] = c + L2;
+    p->part_begin[3] = c + 2 * L2;
+    p->cut = c;
+    p->early_slots = half;
+    p->nlate_coef = nl;
+    p->pstride = (int64_t)(p->rows + 2) * p->N;   /* two spare psi rows */
+    return 0;
+}
+
+static int add_entry(qgt_plan_t* p, int* cap, const qgt_dev_entry_t* e)
+{
+    if (p->nents >= *cap) {
+        int nc = *cap * 2;
+        qgt_dev_entry_t* ne = (qgt_dev_entry_t*)realloc(p->ents_h, sizeof(qgt_dev_entry_t) * (size_t)nc);
+        if (!ne) return qgt_set_error(E_NOMEM, "entries: oom");
+        p->ents_h = ne;
+        *cap = nc;
+    }
+    p->ents_h[p->nents++] = *e;
+    const int64_t ab = p->fp64 ? 16 : 8;
+    p->gate_bytes += ab * p->N * ((e->flags & QENT_SRC_ZERO) ? 1 : 2);
+    return 0;
+}
+
+/* entries of the three meet-in-the-middle parts (see setup_transport):
+ * rows 0 psi(cut), 1 H psi carried to the cut, 2 + s slot s at the cut;
+ * spares rows and rows + 1 hold psi beyond the cut */
+static int build_entries_mitm(qgt_plan_t* p)
+{
+    int cap = 64, rc = 0;
+    p->nents = 0;
+    p->ents_h = (qgt_dev_entry_t*)malloc(sizeof(qgt_dev_entry_t) * (size_t)cap);
+    char* live = (char*)calloc((size_t)p->nslots + 1, 1);
+    if (!p->ents_h || !live) { free(live); return qgt_set_error(E_NOMEM, "entries: oom"); }
+    const int rmax = (p->opt.precision == QGT_PRECISION_MIXED && !p->small_nsplit) ? QENT_ROWMAX : 0;
+    const int has_h = p->opt.hamiltonian != QGT_HAMILTONIAN_NONE;
+    const int RA = p->rows, RB = p->rows + 1;
+    int nf = 0, nb = 0;
+    for (int k = 0; k < p->npasses; k++) { nf += p->passes[k].part == 0; nb += p->passes[k].part == 2; }
+    p->vector_passes = 0;
+    p->gate_bytes = 0;
+    int fi = 0, pi = 0, bi = 0, cur = 0, bsrc = 0;
+    for (int k = 0; k < p->npasses && !rc; k++) {
+        spass_t* ps = &p->passes[k];
+        ps->ent_begin = p->nents;
+        qgt_dev_entry_t e;
+        if (ps->part == 0) {
+            const int last = (fi == nf - 1);
+            const int dst = ((nf - 1 - fi) % 2 == 0) ? 0 : RA;
+            const int src = (fi == 0) ? -1 : (((nf - fi) % 2 == 0) ? 0 : RA);
+            memset(&e, 0, sizeof e);
+            e.src_row = src < 0 ? 0 : src;
+            e.dst_row = dst;
+            e.spawn_op = -1;
+            e.flags = QENT_STORE_V | (src < 0 ? QENT_SRC_ZERO : 0) | (last ? rmax : 0);
+            rc = add_entry(p, &cap, &e);
+            for (int s = 0; s < p->nslots && !rc; s++) {
+                if (!live[s]) continue;
+                memset(&e, 0, sizeof e);
+                e.src_row = e.dst_row = 2 + s;
+                e.spawn_op = -1;
+                e.flags = QENT_STORE_V | (last ? rmax : 0);
+                rc = add_entry(p, &cap, &e);
+            }
+            for (int j = 0; j < ps->op_count && !rc; j++) {
+                const qgt_dev_op_t* op = &p->ops_h[ps->op_begin + j];
+                if (op->slot < 0) continue;
+                memset(&e, 0, sizeof e);
+                e.src_row = src < 0 ? 0 : src;
+                e.dst_row = 2 + op->slot;
+                e.spawn_op = j;
+                e.flags = QENT_STORE_V | (src < 0 ? QENT_SRC_ZERO : 0) | (last ? rmax : 0);
+                rc = add_entry(p, &cap, &e);
+            }
+            fi++;
+        } else if (ps->part == 1) {
+            const int dst = (pi % 2 == 0) ? RA : RB;
+            memset(&e, 0, sizeof e);
+            e.src_row = (pi == 0) ? 0 : cur;
+            e.dst_row = dst;
+            e.spawn_op = -1;
+            e.flags = QENT_STORE_V;
+            rc = add_entry(p, &cap, &e);
+            cur = dst;
+            pi++;
+            p->row_T = cur;
+            bsrc = cur;
+        } else {
+            const int last = (bi == nb - 1);
+            int bdst = (bsrc == RA) ? RB : RA;
+            if (!last) {
+                memset(&e, 0, sizeof e);
+                e.src_row = bsrc;
+                e.dst_row = bdst;
+                e.spawn_op = -1;
+                e.flags = QENT_STORE_V;
+                rc = add_entry(p, &cap, &e);
+            }
+            if (has_h && !rc) {
+                memset(&e, 0, sizeof e);
+                e.src_row = e.dst_row = 1;
+                e.spawn_op = -1;
+                e.flags = QENT_STORE_V | (last ? rmax : 0);
+                rc = add_entry(p, &cap, &e);
+            }
+            for (int s = p->early_slots; s < p->nslots && !rc; s++) {   /* first-half slots stay at the cut */
+                if (!live[s]) continue;
+                memset(&e, 0, sizeof e);
+                e.src_row = e.dst_row = 2 + s;
+                e.spawn_op = -1;
+                e.flags = QENT_STORE_V | (last ? rmax : 0);
+                rc = add_entry(p, &cap, &e);
+            }
+            for (int j = 0; j < ps->op_count && !rc; j++) {
+                const qgt_dev_op_t* op = &p->ops_h[ps->op_begin + j];
+                if (op->slot < 0) continue;
+                memset(&e, 0, sizeof e);
+                e.src_row = bsrc;
+                e.dst_row = 2 + op->slot;
+                e.spawn_op = j;
+                e.flags = QENT_STORE_V | (last ? rmax : 0);
+                rc = add_entry(p, &cap, &e);
+            }
+            if (!last) bsrc = bdst;
+            bi++;
+        }
+        for (int j = 0; j < ps->op_count; j++) {
+            const qgt_dev_op_t* op = &p->ops_h[ps->op_begin + j];
+            if (op->slot >= 0) live[op->slot] = 1;
+        }
+        ps->ent_count = p->nents - ps->ent_begin;
+        if (!rc && ps->ent_count > 65535) rc = qgt_set_error(E_INVAL, "pass has more than 65535 vectors");
+        p->vector_passes += ps->ent_count;
+    }
+    free(live);
+    return rc;
 }
 
 /* Register-resident programs for passes whose tile has the full width
@@ -581,7 +795,14 @@ static int fold_diagonal_runs(qgt_plan_t* p)
 
 static int run_step(qgt_plan_t* p);
 
+static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, qgt_plan_t** out, int host_only);
+
 int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, qgt_plan_t** out)
+{
+    return plan_create(c, opt, out, 0);
+}
+
+static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, qgt_plan_t** out, int host_only)
 {
     int rc = 0;
     if (!out) return qgt_set_error(E_INVAL, "qgt_plan_create: plan pointer is NULL");
@@ -658,8 +879,9 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
         }
         free(fill);
     }
+    if ((rc = setup_transport(p)) != 0) goto fail;
     if ((rc = compile_schedule(p)) != 0) goto fail;
-    if ((rc = build_entries(p)) != 0) goto fail;
+    if ((rc = (p->mitm ? build_entries_mitm(p) : build_entries(p))) != 0) goto fail;
     if ((rc = build_programs(p)) != 0) goto fail;
     if ((rc = fold_diagonal_runs(p)) != 0) goto fail;
     if (p->opt.hamiltonian == QGT_HAMILTONIAN_PAULI) {
@@ -697,6 +919,8 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
     p->split_scale = 16384.0f; /* 2^14: |amplitude| <= 1 stays below the FP16 maximum */
 
     /* ---- device resources ---- */
+    p->host_only = host_only;
+    if (host_only) { *out = p; return 0; }
     if ((rc = qgt_dev_set_device(p->opt.device)) != 0) goto fail;
     if ((rc = qgt_dev_stream_create(&p->stream)) != 0) goto fail;
     {
@@ -733,6 +957,13 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
                                      p->stream)) != 0)
             goto fail;
     }
+    if (p->mitm && !p->fp64 && p->nprog > 0) {
+        DALLOC(p->late_coef_d, sizeof(int32_t) * (size_t)(p->nlate_coef + 1));
+        DALLOC(p->rho_d, sizeof(double) * (size_t)p->B);
+        if (p->nlate_coef && (rc = qgt_dev_memcpy_h2d(p->late_coef_d, p->late_coef_h, sizeof(int32_t) * (size_t)p->nlate_coef,
+                                                      p->stream)) != 0)
+            goto fail;
+    }
     DALLOC(p->slot_param_d, sizeof(int32_t) * (size_t)(p->nslots + 1));
     DALLOC(p->param_ptr_d, sizeof(int32_t) * (size_t)(p->Pd + 2));
     DALLOC(p->param_slots_d, sizeof(int32_t) * (size_t)(p->nslots + 1));
@@ -759,7 +990,7 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
     } else {
         if (p->n < 4) { rc = qgt_set_error(E_INVAL, "mixed precision needs at least 4 qubits (use FP64)"); goto fail; }
         DALLOC(p->rowmax_d, sizeof(uint32_t) * (size_t)p->rows * p->B);
-        if ((rc = qgt_dev_dg_gram_create(p->V, p->N, p->rows, p->rowmax_d, p->B, p->rows + 1, &p->dg)) != 0) goto fail;
+        if ((rc = qgt_dev_dg_gram_create(p->V, p->N, p->rows, p->rowmax_d, p->B, (int32_t)(p->pstride / p->N), &p->dg)) != 0) goto fail;
         p->device_bytes += qgt_dev_dg_gram_scratch_bytes(p->dg);
     }
     if ((rc = qgt_dev_memset(p->theta_d, 0, sizeof(double) * ((size_t)p->B * p->P + 1), p->stream)) != 0) goto fail;
@@ -803,13 +1034,21 @@ fail:
 void qgt_plan_destroy(qgt_plan_t* p)
 {
     if (!p) return;
+    if (p->host_only) {
+        free(p->gates); free(p->passes); free(p->ops_h); free(p->ents_h); free(p->coef_h); free(p->prog_h);
+        free(p->segs_h); free(p->slot_param_h); free(p->param_ptr_h); free(p->param_slots_h); free(p->pauli_h);
+        free(p->late_coef_h);
+        free(p);
+        return;
+    }
     if (p->stream) qgt_dev_stream_sync(p->stream);
     qgt_dev_graph_destroy(p->graph);
     qgt_dev_tc_gram_destroy(p->tc);
     qgt_dev_dg_gram_destroy(p->dg);
     qgt_dev_free(p->rowmax_d);
     free(p->pauli_h);
-    void* dev[] = {p->V, p->split, p->small_part_d, p->pauli_d, p->ops_d, p->ents_d, p->prog_d, p->segs_d, p->coef32_d, p->coef_desc_d, p->coef_d, p->theta_d, p->HG_d, p->part_d,
+    free(p->late_coef_h);
+    void* dev[] = {p->V, p->split, p->small_part_d, p->pauli_d, p->late_coef_d, p->rho_d, p->ops_d, p->ents_d, p->prog_d, p->segs_d, p->coef32_d, p->coef_desc_d, p->coef_d, p->theta_d, p->HG_d, p->part_d,
                    p->Q_d, p->grad_d, p->energy_d, p->natgrad_d, p->chol_work_d, p->status_d, p->slot_param_d,
                    p->param_ptr_d, p->param_slots_d};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++) qgt_dev_free(dev[i]);
@@ -839,6 +1078,8 @@ int qgt_plan_get_info(const qgt_plan_t* p, qgt_plan_info_t* info)
     info->gram_flops = (int64_t)4 * p->Pd * (p->Pd + 1) * p->N * p->B;
     info->batch = p->B;
     info->num_deriv_params = p->Pd;
+    info->meet_in_middle = p->mitm;
+    info->cut_gate = p->mitm ? p->cut : -1;
     info->device_bytes = p->device_bytes;
     return 0;
 }
@@ -848,6 +1089,31 @@ int qgt_plan_get_info(const qgt_plan_t* p, qgt_plan_info_t* info)
 /* ------------------------------------------------------------------------ */
 
 #define MARK(i) do { if (p->prof_ev[i] && (rc = qgt_dev_event_record(p->prof_ev[i], p->stream)) != 0) return rc; } while (0)
+
+/* row 1 = H psi / hscale; psi is row 0, or psi(G) in a spare row with
+ * meet-in-the-middle transport (whose last backward pass records row 1's
+ * maximum instead, after carrying it to the cut) */
+static int apply_hamiltonian(qgt_plan_t* p, int* launches)
+{
+    int rc = 0;
+    const size_t ab = p->fp64 ? 16 : 8;
+    const void* psi = (const char*)p->V + (size_t)(p->mitm ? p->row_T : 0) * p->N * ab;
+    void* row1 = (char*)p->V + (size_t)p->N * ab;
+    uint32_t* rmax = (p->rowmax_d && !p->mitm) ? p->rowmax_d + 1 : NULL;
+    if (p->opt.hamiltonian == QGT_HAMILTONIAN_PAULI) {
+        if ((rc = qgt_dev_pauli(psi, row1, p->n, p->pauli_d, p->npauli, 1.0 / p->hscale, p->fp64, rmax, p->B,
+                                p->pstride, p->rows, p->stream)) != 0)
+            return rc;
+        (*launches)++;
+    } else if (p->opt.hamiltonian == QGT_HAMILTONIAN_TFIM) {
+        if ((rc = qgt_dev_tfim(psi, row1, p->n, p->opt.tfim_J, p->opt.tfim_h, 1.0 / p->hscale, p->fp64, p->split,
+                               p->split_ld, (int64_t)p->rows_pad * p->split_ld, 1, p->split_scale, 1, rmax, p->B,
+                               p->pstride, p->rows, p->stream)) != 0)
+            return rc;
+        (*launches)++;
+    }
+    return 0;
+}
 
 static int run_step(qgt_plan_t* p)
 {
@@ -860,12 +1126,23 @@ static int run_step(qgt_plan_t* p)
         if ((rc = qgt_dev_prepare32(p->coef_desc_d, p->ncoef, p->theta_d, p->coef32_d, p->B, p->P, p->stream)) != 0)
             return rc;
         launches += p->ncoef > 0;
+        if (p->rho_d) {
+            if ((rc = qgt_dev_scale_product(p->coef32_d, p->ncoef, p->late_coef_d, p->nlate_coef, p->rho_d, p->B,
+                                            p->stream)) != 0)
+                return rc;
+            launches++;
+        }
     }
     if (p->dg && (rc = qgt_dev_memset(p->rowmax_d, 0, sizeof(uint32_t) * (size_t)p->rows * p->B, p->stream)) != 0)
         return rc;
     MARK(1);
+    int h_done = 0;
     for (int k = 0; k < p->npasses; k++) {
         const spass_t* ps = &p->passes[k];
+        if (ps->part == 2 && !h_done) {
+            if ((rc = apply_hamiltonian(p, &launches)) != 0) return rc;
+            h_done = 1;
+        }
         qgt_dev_pass_args_t a;
         memset(&a, 0, sizeof a);
         a.V = p->V;
@@ -935,22 +1212,7 @@ static int run_step(qgt_plan_t* p)
     }
     MARK(2);
     const int has_h = p->opt.hamiltonian != QGT_HAMILTONIAN_NONE;
-    if (p->opt.hamiltonian == QGT_HAMILTONIAN_PAULI) {
-        size_t ab = p->fp64 ? 16 : 8;
-        void* row1 = (char*)p->V + (size_t)p->N * ab;
-        if ((rc = qgt_dev_pauli(p->V, row1, p->n, p->pauli_d, p->npauli, 1.0 / p->hscale, p->fp64,
-                                p->rowmax_d ? p->rowmax_d + 1 : NULL, p->B, p->pstride, p->rows, p->stream)) != 0)
-            return rc;
-        launches++;
-    } else if (has_h) {
-        size_t ab = p->fp64 ? 16 : 8;
-        void* row1 = (char*)p->V + (size_t)p->N * ab;
-        if ((rc = qgt_dev_tfim(p->V, row1, p->n, p->opt.tfim_J, p->opt.tfim_h, 1.0 / p->hscale, p->fp64,
-                               p->split, p->split_ld, (int64_t)p->rows_pad * p->split_ld, 1, p->split_scale, 1,
-                               p->rowmax_d ? p->rowmax_d + 1 : NULL, p->B, p->pstride, p->rows, p->stream)) != 0)
-            return rc;
-        launches++;
-    }
+    if (!h_done && (rc = apply_hamiltonian(p, &launches)) != 0) return rc;
     MARK(3);
     if (p->small_nsplit) {
         if ((rc = qgt_dev_gram_small(p->V, p->N, p->rows, p->fp64, p->small_part_d, p->small_nsplit, p->HG_d, p->B,
@@ -983,6 +1245,8 @@ static int run_step(qgt_plan_t* p)
         pa.Q = p->Q_d;
         pa.grad = p->grad_d;
         pa.energy = p->energy_d;
+        pa.late_scale = p->rho_d;
+        pa.late_row0 = p->mitm ? 2 + p->early_slots : 0;
         if ((rc = qgt_dev_post(&pa, p->stream)) != 0) return rc;
         launches += 1 + has_h;
         MARK(5);
@@ -1122,13 +1386,16 @@ int qgt_plan_get_state(qgt_plan_t* p, double* psi)
     if (!p || !psi) return qgt_set_error(E_INVAL, "qgt_plan_get_state: NULL argument");
     if (!p->has_run) return qgt_set_error(E_STATE, "qgt_plan_get_state: no step has run");
     int rc;
+    const size_t row = p->mitm ? (size_t)p->row_T : 0;   /* psi after the last gate */
     if (p->fp64) {
-        if ((rc = qgt_dev_memcpy_d2h(psi, p->V, sizeof(double) * 2 * (size_t)p->N, p->stream)) != 0) return rc;
+        if ((rc = qgt_dev_memcpy_d2h(psi, (const char*)p->V + row * p->N * 16, sizeof(double) * 2 * (size_t)p->N,
+                                     p->stream)) != 0)
+            return rc;
         return qgt_dev_stream_sync(p->stream);
     }
     float* tmp = (float*)malloc(sizeof(float) * 2 * (size_t)p->N);
     if (!tmp) return qgt_set_error(E_NOMEM, "qgt_plan_get_state: oom");
-    rc = qgt_dev_memcpy_d2h(tmp, p->V, sizeof(float) * 2 * (size_t)p->N, p->stream);
+    rc = qgt_dev_memcpy_d2h(tmp, (const char*)p->V + row * p->N * 8, sizeof(float) * 2 * (size_t)p->N, p->stream);
     if (!rc) rc = qgt_dev_stream_sync(p->stream);
     if (!rc) for (int64_t i = 0; i < 2 * p->N; i++) psi[i] = tmp[i];
     free(tmp);
@@ -1247,7 +1514,8 @@ double* qgt_plan_dev_natgrad(qgt_plan_t* p) { return p->natgrad_d; }
 int qgt_plan_combine_slots(qgt_plan_t* p, const double* c, double* out)
 {
     if (!p || !c || !out) return qgt_set_error(E_INVAL, "qgt_plan_combine_slots: bad argument");
-    if (!p->fp64 || p->B != 1) return qgt_set_error(E_STATE, "qgt_plan_combine_slots: unbatched FP64 plans only");
+    if (!p->fp64 || p->B != 1 || p->mitm)
+        return qgt_set_error(E_STATE, "qgt_plan_combine_slots: unbatched FP64 plans with forward transport only");
     if (p->nslots == 0) { memset(out, 0, sizeof(double) * 2 * (size_t)p->N); return 0; }
     double *cd = NULL, *od = NULL;
     int rc = qgt_dev_malloc((void**)&cd, sizeof(double) * (size_t)p->nslots);
@@ -1259,4 +1527,46 @@ int qgt_plan_combine_slots(qgt_plan_t* p, const double* c, double* out)
     qgt_dev_free(cd);
     qgt_dev_free(od);
     return rc;
+}
+
+/* The compiled schedule as JSON (no device needed): passes with their gate
+ * ops and vector entries, coefficient sources and the row layout.  Used by
+ * the CPU tests, which replay it against the FP64 oracle. */
+int qgt_plan_schedule_dump(const void* circuit, const void* options, const char* path)
+{
+    const qgt_circuit_desc_t* c = (const qgt_circuit_desc_t*)circuit;
+    const qgt_plan_options_t* opt = (const qgt_plan_options_t*)options;
+    qgt_plan_t* p = NULL;
+    int rc = plan_create(c, opt, &p, 1);
+    if (rc) return rc;
+    FILE* f = fopen(path, "w");
+    if (!f) { qgt_plan_destroy(p); return qgt_set_error(E_INVAL, "qgt_plan_schedule_dump: cannot write %s", path); }
+    fprintf(f, "{\"n\": %d, \"rows\": %d, \"nslots\": %d, \"mitm\": %d, \"cut\": %d, \"early_slots\": %d, "
+               "\"row_T\": %d, \"hscale\": %.17g,\n", p->n, p->rows, p->nslots, p->mitm, p->cut, p->early_slots,
+            p->row_T, p->hscale);
+    fprintf(f, "\"coefs\": [");
+    for (int i = 0; i < p->ncoef; i++)
+        fprintf(f, "%s[%d, %d, %.17g]", i ? ", " : "", p->coef_h[i].type, p->coef_h[i].param, p->coef_h[i].angle);
+    fprintf(f, "],\n\"slot_param\": [");
+    for (int i = 0; i < p->nslots; i++) fprintf(f, "%s%d", i ? ", " : "", p->slot_param_h[i]);
+    fprintf(f, "],\n\"passes\": [");
+    for (int k = 0; k < p->npasses; k++) {
+        const spass_t* ps = &p->passes[k];
+        fprintf(f, "%s{\"part\": %d, \"tile_mask\": %u, \"ops\": [", k ? ",\n" : "", ps->part, ps->tile_mask);
+        for (int j = 0; j < ps->op_count; j++) {
+            const qgt_dev_op_t* o = &p->ops_h[ps->op_begin + j];
+            fprintf(f, "%s[%d, %d, %d, %d, %d, %d]", j ? ", " : "", (int)o->pad, (int)o->q, (int)o->q2, o->coef, o->slot,
+                    (int)o->kind);
+        }
+        fprintf(f, "], \"entries\": [");
+        for (int e = 0; e < ps->ent_count; e++) {
+            const qgt_dev_entry_t* en = &p->ents_h[ps->ent_begin + e];
+            fprintf(f, "%s[%d, %d, %d, %d]", e ? ", " : "", en->src_row, en->dst_row, en->spawn_op, en->flags);
+        }
+        fprintf(f, "]}");
+    }
+    fprintf(f, "]}\n");
+    fclose(f);
+    qgt_plan_destroy(p);
+    return 0;
 }

@@ -53,7 +53,9 @@ typedef struct {
     int32_t slot;   /* derivative slot of this gate, -1 if none */
 } qgt_dev_op_t;
 
-/* gate coefficient source: the prepare kernel turns theta into matrices */
+/* gate coefficient source: the prepare kernel turns theta into matrices;
+ * type | QGT_COEF_INVERSE asks for the gate's inverse */
+#define QGT_COEF_INVERSE 0x100
 typedef struct {
     int32_t type;   /* QGT_GATE_* */
     int32_t param;  /* theta index, -1 = fixed */
@@ -147,6 +149,9 @@ typedef struct {
     int32_t rowmax_stride;
 } qgt_dev_pass2_args_t;
 int qgt_dev_pass2(const qgt_dev_pass2_args_t* args, int fp64, void* stream);
+/* rho[point] = product of the amplitude scales |column 0| of the listed complex64 coefficient entries */
+int qgt_dev_scale_product(const float* coef32, int32_t ncoef, const int32_t* list, int32_t n, double* rho,
+                          int32_t npoints, void* stream);
 int qgt_dev_prepare32(const qgt_dev_coef_desc_t* descs_dev, int32_t ncoef, const double* theta_dev,
                       float* coef32_dev, int32_t npoints, int32_t theta_stride, void* stream);
 
@@ -158,6 +163,9 @@ int qgt_plan_enqueue_step(struct qgt_plan* p, void* stream);
 double* qgt_plan_dev_theta(struct qgt_plan* p);   /* batch x num_params */
 double* qgt_plan_dev_Q(struct qgt_plan* p);       /* batch x Pd x Pd complex */
 int qgt_plan_launches(const struct qgt_plan* p);
+/* the host-side schedule of a circuit as JSON, without a device (circuit /
+ * options: qgt_circuit_desc_t / qgt_plan_options_t of qgt_gb300.h) */
+int qgt_plan_schedule_dump(const void* circuit, const void* options, const char* path);
 
 /* thread-local last error (host/qgt_error.c): stores the message and returns code */
 int qgt_set_error(int code, const char* fmt, ...);
@@ -259,6 +267,10 @@ typedef struct {
     double* grad;           /* P */
     double* energy;         /* 1 */
     int32_t npoints;        /* parameter points (0 = 1): HG, Q, grad, energy blocks per point */
+    /* meet-in-the-middle: rows 1 and >= late_row0 carry the extra amplitude
+     * scale late_scale[point] of the complex64 gates they crossed twice (NULL: none) */
+    const double* late_scale;
+    int32_t late_row0;
 } qgt_dev_post_args_t;
 int qgt_dev_post(const qgt_dev_post_args_t* a, void* stream);
 /* (Re Q + lambda I) x = b, FP64 Cholesky; A taken as Re of the complex Q when
