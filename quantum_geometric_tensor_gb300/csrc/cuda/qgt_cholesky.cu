@@ -18,6 +18,7 @@
 #include "../qgt_internal.h"
 
 #define CB 32
+#define CHOL_BLOCKED_MAXP 2048   // the solve keeps y and 1 / L_ii in shared memory (32 KB)
 
 __global__ void chol_init_kernel(const double* __restrict__ A, int cplx, int P, double lambda, double* __restrict__ L,
                                  double* status)
@@ -40,16 +41,20 @@ __global__ void __launch_bounds__(CB* CB) chol_diag_kernel(double* __restrict__ 
     a[ty][tx] = (ty < nb && tx < nb) ? L[(int64_t)(j0 + ty) * P + j0 + tx] : (ty == tx ? 1.0 : 0.0);
     __syncthreads();
     __shared__ int bad;
+    __shared__ double inv;
     if (threadIdx.x == 0) bad = 0;
     __syncthreads();
+    // FP64 divisions and square roots are scarce on this part: one of each per column
     for (int k = 0; k < nb; k++) {
         if (threadIdx.x == 0) {
             double d = a[k][k];
             if (!(d > 0.0)) { bad = 1; d = 1.0; }
-            a[k][k] = sqrt(d);
+            const double l = sqrt(d);
+            a[k][k] = l;
+            inv = 1.0 / l;
         }
         __syncthreads();
-        if (tx == k && ty > k && ty < nb) a[ty][k] /= a[k][k];
+        if (tx == k && ty > k && ty < nb) a[ty][k] *= inv;
         __syncthreads();
         if (ty > k && tx > k && tx <= ty && ty < nb) a[ty][tx] -= a[ty][k] * a[tx][k];
         __syncthreads();
@@ -62,10 +67,13 @@ __global__ void __launch_bounds__(CB* CB) chol_diag_kernel(double* __restrict__ 
 __global__ void __launch_bounds__(CB* CB) chol_panel_kernel(double* __restrict__ L, int P, int jb)
 {
     __shared__ double ljj[CB][CB + 1];
+    __shared__ double rinv[CB];
     const int tx = threadIdx.x % CB, ty = threadIdx.x / CB;
     const int j0 = jb * CB, nb = min(CB, P - j0);
     const int i0 = (jb + 1 + blockIdx.x) * CB;
     ljj[ty][tx] = (ty < nb && tx < nb) ? L[(int64_t)(j0 + ty) * P + j0 + tx] : (ty == tx ? 1.0 : 0.0);
+    __syncthreads();
+    if (threadIdx.x < CB) rinv[threadIdx.x] = 1.0 / ljj[threadIdx.x][threadIdx.x];
     __syncthreads();
     const int r = i0 + ty;
     if (r >= P) return;
@@ -73,7 +81,7 @@ __global__ void __launch_bounds__(CB* CB) chol_panel_kernel(double* __restrict__
     double acur = (tx < nb) ? L[(int64_t)r * P + j0 + tx] : 0.0;
     double x = 0.0;
     for (int c = 0; c < nb; c++) {
-        double xc = __shfl_sync(0xffffffffu, acur / ljj[c][c], c);
+        double xc = __shfl_sync(0xffffffffu, acur, c) * rinv[c];
         if (tx == c) x = xc;
         if (tx > c) acur -= xc * ljj[tx][c];
     }
@@ -106,11 +114,14 @@ __global__ void __launch_bounds__(CB* CB) chol_update_kernel(double* __restrict_
 __global__ void __launch_bounds__(CB* CB) chol_solve_kernel(const double* __restrict__ L, const double* __restrict__ b,
                                                             double* __restrict__ x, int P)
 {
-    __shared__ double y[4096];
-    __shared__ double part[CB][CB + 1];
+    __shared__ double y[CHOL_BLOCKED_MAXP];
+    __shared__ double rd[CHOL_BLOCKED_MAXP];   // 1 / L_ii
     const int tx = threadIdx.x % CB, ty = threadIdx.x / CB;
     const int nt = (P + CB - 1) / CB;
-    for (int i = threadIdx.x; i < P; i += blockDim.x) y[i] = b[i];
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        y[i] = b[i];
+        rd[i] = 1.0 / L[(int64_t)i * P + i];
+    }
     __syncthreads();
     // forward
     for (int bb = 0; bb < nt; bb++) {
@@ -126,7 +137,7 @@ __global__ void __launch_bounds__(CB* CB) chol_solve_kernel(const double* __rest
         if (ty == 0) {  // one warp: triangular solve of the diagonal block
             double acur = (tx < nb) ? y[r0 + tx] : 0.0, xv = 0.0;
             for (int c = 0; c < nb; c++) {
-                double xc = __shfl_sync(0xffffffffu, acur / L[(int64_t)(r0 + c) * P + r0 + c], c);
+                double xc = __shfl_sync(0xffffffffu, acur, c) * rd[r0 + c];
                 if (tx == c) xv = xc;
                 if (tx > c && tx < nb) acur -= xc * L[(int64_t)(r0 + tx) * P + r0 + c];
             }
@@ -147,7 +158,7 @@ __global__ void __launch_bounds__(CB* CB) chol_solve_kernel(const double* __rest
         if (ty == 0) {
             double acur = (tx < nb) ? y[r0 + tx] : 0.0, xv = 0.0;
             for (int c = nb - 1; c >= 0; c--) {
-                double xc = __shfl_sync(0xffffffffu, acur / L[(int64_t)(r0 + c) * P + r0 + c], c);
+                double xc = __shfl_sync(0xffffffffu, acur, c) * rd[r0 + c];
                 if (tx == c) xv = xc;
                 if (tx < c) acur -= xc * L[(int64_t)(r0 + c) * P + r0 + tx];
             }
@@ -155,14 +166,14 @@ __global__ void __launch_bounds__(CB* CB) chol_solve_kernel(const double* __rest
         }
         __syncthreads();
     }
-    (void)part;
     for (int i = threadIdx.x; i < P; i += blockDim.x) x[i] = y[i];
 }
 
 extern "C" int qgt_dev_cholesky_blocked(const double* A, int cplx, const double* b, int32_t P, double lambda,
                                         double* L, double* x, double* status, void* stream)
 {
-    if (P <= 0 || P > 4096) return qgt_set_error(-1, "blocked cholesky: P = %d outside [1, 4096]", P);
+    if (P <= 0 || P > CHOL_BLOCKED_MAXP)
+        return qgt_set_error(-1, "blocked cholesky: P = %d outside [1, %d]", P, CHOL_BLOCKED_MAXP);
     cudaStream_t s = (cudaStream_t)stream;
     int64_t PP = (int64_t)P * P;
     chol_init_kernel<<<(unsigned)((PP + 255) / 256), 256, 0, s>>>(A, cplx, P, lambda, L, status);

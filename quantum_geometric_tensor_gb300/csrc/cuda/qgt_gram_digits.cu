@@ -306,8 +306,10 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
         mma_done_commit = true;
     } else if (warp >= 2) {
         // ---------- converters: complex64 -> {Re D, Re l1, Re l2, Im D, Im l1, Im l2} ----------
-        const int cw = warp - 2;  // rows r = cw, cw + DG_CONV_WARPS, ...
-        const int comp = lane & 1, k = lane >> 1;
+        const int cw = warp - 2;
+        // lane -> (row r = 4 cw + 32 i + lane / 8, amplitude pair kp, kp + 1): one 16-byte load of
+        // (re, im, re, im), then 32-bit stores of half2 pairs into the six planes
+        const int sub = lane >> 3, kp = (lane & 7) * 2;
         for (int kt = 0; kt < nk; kt++) {
             const int rs = kt % DG_RAW_STAGES, ps = kt % DG_PL_STAGES;
             bool ok = bar_wait(smem_u32(&raw_full[rs]), (kt / DG_RAW_STAGES) & 1, deadline);
@@ -322,19 +324,26 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
             for (int b = 0; b < nblk; b++) {
                 const float* raw = reinterpret_cast<const float*>(rawst + b * DG_RAW_BYTES);
                 uint8_t* planes = plst + b * 6 * DG_PLANE_BYTES;
-                uint8_t* pD = planes + (comp ? 3 : 0) * DG_PLANE_BYTES;
 #pragma unroll 4
-                for (int r = cw; r < 128; r += DG_CONV_WARPS) {
-                    const float x = raw[r * 32 + lane] * inv_u[b][r];
-                    const float d = rintf(x);
-                    const float l = x - d;
-                    const __half h1 = __float2half_rn(l);
-                    const __half h2 = __float2half_rn(l - __half2float(h1));
-                    // SWIZZLE_32B: 16-byte chunk (k / 8) xor bit 2 of the row
-                    const int off = r * 32 + ((((k >> 3) ^ (r >> 2)) & 1) << 4) + (k & 7) * 2;
-                    *reinterpret_cast<__half*>(pD + off) = __float2half_rn(d);
-                    *reinterpret_cast<__half*>(pD + DG_PLANE_BYTES + off) = h1;
-                    *reinterpret_cast<__half*>(pD + 2 * DG_PLANE_BYTES + off) = h2;
+                for (int rr = 4 * cw; rr < 128; rr += 4 * DG_CONV_WARPS) {
+                    const int r = rr + sub;
+                    const float4 q = *reinterpret_cast<const float4*>(raw + r * 32 + 2 * kp);
+                    const float iu = inv_u[b][r];
+                    // SWIZZLE_32B: 16-byte chunk (k / 8) xor bit 2 of the row; kp, kp + 1 share a chunk
+                    const int off = r * 32 + ((((kp >> 3) ^ (r >> 2)) & 1) << 4) + (kp & 7) * 2;
+#pragma unroll
+                    for (int c = 0; c < 2; c++) {   // 0: real parts, 1: imaginary parts
+                        const float x0 = (c ? q.y : q.x) * iu, x1 = (c ? q.w : q.z) * iu;
+                        const float d0 = rintf(x0), d1 = rintf(x1);
+                        const float l0 = x0 - d0, l1 = x1 - d1;
+                        const __half2 h1 = __floats2half2_rn(l0, l1);
+                        const float2 f1 = __half22float2(h1);
+                        const __half2 h2 = __floats2half2_rn(l0 - f1.x, l1 - f1.y);
+                        uint8_t* pD = planes + (c ? 3 : 0) * DG_PLANE_BYTES + off;
+                        *reinterpret_cast<__half2*>(pD) = __floats2half2_rn(d0, d1);
+                        *reinterpret_cast<__half2*>(pD + DG_PLANE_BYTES) = h1;
+                        *reinterpret_cast<__half2*>(pD + 2 * DG_PLANE_BYTES) = h2;
+                    }
                 }
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -395,12 +404,28 @@ __global__ void dg_reduce_kernel(const float* __restrict__ part, const uint32_t*
     int ti = i >> 7, tj = j >> 7;
     int tp = ti * nbk - ti * (ti - 1) / 2 + (tj - ti);
     int64_t off = (int64_t)(i & 127) * 128 + (j & 127);
-    double re = 0, im = 0;
-    for (int s = 0; s < nsplit; s++) {
-        const float* b = part + ((int64_t)s * ntp + tp) * (2 * 128 * 128);
-        re += (double)b[off];
-        im += (double)b[128 * 128 + off];
+    // 8 independent sums keep 16 loads in flight per thread (the reduction is
+    // bound by memory-level parallelism, not by its FP64 adds)
+    double re8[8] = {0, 0, 0, 0, 0, 0, 0, 0}, im8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int64_t sstride = (int64_t)ntp * (2 * 128 * 128);
+    const float* b0 = part + (int64_t)tp * (2 * 128 * 128) + off;
+    int s = 0;
+    for (; s + 8 <= nsplit; s += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const float* b = b0 + (int64_t)(s + u) * sstride;
+            re8[u] += (double)__ldg(b);
+            im8[u] += (double)__ldg(b + 128 * 128);
+        }
     }
+    for (; s < nsplit; s++) {
+        const float* b = b0 + (int64_t)s * sstride;
+        re8[0] += (double)__ldg(b);
+        im8[0] += (double)__ldg(b + 128 * 128);
+    }
+    double re = 0, im = 0;
+#pragma unroll
+    for (int u = 0; u < 8; u++) { re += re8[u]; im += im8[u]; }
     double uu = ldexp(1.0, unit_exp(rowmax[i], mbits) + unit_exp(rowmax[j], mbits));
     HG[(int64_t)i * rows + j] = make_double2(re * uu, im * uu);
     HG[(int64_t)j * rows + i] = make_double2(re * uu, -im * uu);

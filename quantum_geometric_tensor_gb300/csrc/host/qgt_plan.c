@@ -1257,7 +1257,7 @@ static int run_step(qgt_plan_t* p)
                                                  p->natgrad_d, p->status_d, p->B, p->stream)) != 0)
                     return rc;
                 launches++;
-            } else if (p->Pd <= 4096) {
+            } else if (p->Pd <= 2048) {
                 if ((rc = qgt_dev_cholesky_blocked(p->Q_d, 1, p->grad_d, p->Pd, p->opt.lambda, p->chol_work_d,
                                                    p->natgrad_d, p->status_d, p->stream)) != 0)
                     return rc;

@@ -279,7 +279,7 @@ int qgt_dev_post(const qgt_dev_post_args_t* a, void* stream);
 int qgt_dev_cholesky(const double* A, int complex_input, const double* b, int32_t P,
                      double lambda, double* work, double* x, double* status, void* stream);
 /* the same solve, blocked over many CTAs, without retries (status[0] =
- * QGT_ERROR_NOT_POSITIVE_DEFINITE on a non-positive pivot); P <= 4096 */
+ * QGT_ERROR_NOT_POSITIVE_DEFINITE on a non-positive pivot); P <= 2048 */
 int qgt_dev_cholesky_blocked(const double* A, int complex_input, const double* b, int32_t P,
                              double lambda, double* work, double* x, double* status, void* stream);
 int qgt_dev_cholesky_launches(int32_t P);
