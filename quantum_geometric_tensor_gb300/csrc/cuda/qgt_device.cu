@@ -112,12 +112,12 @@ const char* qgt_dev_error_string(void) { return cudaGetErrorString(cudaPeekAtLas
 // hybrid/quantum_classical_algorithms.c:228-276.
 // ---------------------------------------------------------------------------
 __global__ void prepare_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const double* theta, double* coef,
-                               int theta_stride)
+                               int theta_stride, int coef_stride)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncoef) return;
     theta += (int64_t)blockIdx.y * theta_stride;   // parameter point
-    coef += (int64_t)8 * blockIdx.y * ncoef;
+    coef += (int64_t)8 * blockIdx.y * coef_stride;
     qgt_dev_coef_desc_t g = d[c];
     const int inv = (g.type & QGT_COEF_INVERSE) != 0;   // the gate's inverse (backward transport)
     g.type &= ~QGT_COEF_INVERSE;
@@ -266,14 +266,14 @@ __device__ __forceinline__ double2 hg(const double* HG, int rows, int i, int j)
     return make_double2(HG[2 * ((int64_t)i * rows + j)], HG[2 * ((int64_t)i * rows + j) + 1]);
 }
 
-// HG entry with the meet-in-the-middle scale correction: rows transported
-// backward (row 1 and rows >= late_row0) carry an extra factor rho
-__device__ __forceinline__ double2 hgs(const qgt_dev_post_args_t& a, int i, int j, double inv_rho)
+// HG entry with the meet-in-the-middle scale correction: row r carries the
+// extra amplitude scale rho[row_group[r]] of the complex64 gates it crossed twice
+__device__ __forceinline__ double2 hgs(const qgt_dev_post_args_t& a, int i, int j, const double* rho)
 {
     double2 v = hg(a.HG, a.rows, i, j);
-    if (a.late_scale) {
-        const int li = (i == 1 || (a.late_row0 > 0 && i >= a.late_row0)), lj = (j == 1 || (a.late_row0 > 0 && j >= a.late_row0));
-        const double f = (li && lj) ? inv_rho * inv_rho : ((li || lj) ? inv_rho : 1.0);
+    if (rho) {
+        const int gi = a.row_group[i], gj = a.row_group[j];
+        const double f = (gi >= 0 ? 1.0 / rho[gi] : 1.0) * (gj >= 0 ? 1.0 / rho[gj] : 1.0);
         v.x *= f;
         v.y *= f;
     }
@@ -288,7 +288,7 @@ __global__ void post_qgt_kernel(qgt_dev_post_args_t a)
     a.HG += (int64_t)2 * blockIdx.y * a.rows * a.rows;   // parameter point
     a.Q += (int64_t)2 * blockIdx.y * P * P;
     int p = (int)(idx / P), q = (int)(idx % P);
-    const double ir = a.late_scale ? 1.0 / a.late_scale[blockIdx.y] : 1.0;
+    const double* ir = a.rho ? a.rho + (int64_t)blockIdx.y * a.ngroups : NULL;
     double s = a.HG[0];
     double2 B = make_double2(0, 0), vp = make_double2(0, 0), vq = make_double2(0, 0);
     for (int x = a.param_ptr[p]; x < a.param_ptr[p + 1]; x++) {
@@ -317,7 +317,7 @@ __global__ void post_grad_kernel(qgt_dev_post_args_t a)
     a.HG += (int64_t)2 * blockIdx.y * a.rows * a.rows;   // parameter point
     a.grad += (int64_t)blockIdx.y * a.P;
     if (a.energy) a.energy += blockIdx.y;
-    const double ir = a.late_scale ? 1.0 / a.late_scale[blockIdx.y] : 1.0;
+    const double* ir = a.rho ? a.rho + (int64_t)blockIdx.y * a.ngroups : NULL;
     double s = a.HG[0];
     double E = a.hscale * hgs(a, 0, 1, ir).x / s;
     if (threadIdx.x == 0 && blockIdx.x == 0 && a.energy) a.energy[0] = E;
@@ -425,11 +425,12 @@ __global__ void __launch_bounds__(1024) cholesky_kernel(const double* A, int cpl
 extern "C" {
 
 int qgt_dev_prepare(const qgt_dev_coef_desc_t* d, int32_t ncoef, const double* theta, double* coef, int32_t npoints,
-                    int32_t theta_stride, void* s)
+                    int32_t theta_stride, int32_t coef_stride, void* s)
 {
     if (ncoef <= 0) return QGT_OK;
     if (npoints < 1 || npoints > 65535) return qgt_set_error(QGT_EINVAL, "prepare: %d points", npoints);
-    prepare_kernel<<<dim3((ncoef + 127) / 128, npoints), 128, 0, (cudaStream_t)s>>>(d, ncoef, theta, coef, theta_stride);
+    prepare_kernel<<<dim3((ncoef + 127) / 128, npoints), 128, 0, (cudaStream_t)s>>>(d, ncoef, theta, coef, theta_stride,
+                                                                                      coef_stride);
     return qgt_dev_last_error();
 }
 
@@ -627,13 +628,13 @@ int qgt_dev_event_elapsed(void* a, void* b, float* ms)
 // One warp per coefficient; 8 floats per coefficient (2x2 complex, row-major).
 // ---------------------------------------------------------------------------
 __global__ void prepare32_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const double* theta, float* coef,
-                                 int theta_stride)
+                                 int theta_stride, int coef_stride)
 {
     const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (c >= ncoef) return;
     theta += (int64_t)blockIdx.y * theta_stride;   // parameter point
-    coef += (int64_t)8 * blockIdx.y * ncoef;
+    coef += (int64_t)8 * blockIdx.y * coef_stride;
     qgt_dev_coef_desc_t g = d[c];
     const int inv = (g.type & QGT_COEF_INVERSE) != 0;   // the gate's inverse (backward transport)
     g.type &= ~QGT_COEF_INVERSE;
@@ -675,44 +676,89 @@ __global__ void prepare32_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const 
     if (lane < 8) coef[8 * c + lane] = m[lane];
 }
 
-// rho[point] = prod over the listed coefficient entries of |first column|^2 of
-// their complex64 matrices (the entries' uniform scale factors squared... each
-// entry contributes its amplitude scale r = |column|; the product is taken in
-// FP64 from the exact FP32 values)
-__global__ void scale_product_kernel(const float* __restrict__ coef, int ncoef, const int32_t* __restrict__ list, int n,
-                                     double* __restrict__ rho)
+// rho[point][m] = prod over groups 0..m of the amplitude scales r = |column 0|
+// of the groups' complex64 coefficient entries (FP64 from the exact FP32 values)
+__global__ void scale_product_kernel(const float* __restrict__ coef, int coef_stride, const int32_t* __restrict__ ptr,
+                                     const int32_t* __restrict__ src, int ngroups, double* __restrict__ rho)
 {
     __shared__ double red[32];
-    coef += (int64_t)8 * blockIdx.x * ncoef;
-    double lg = 0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const float* m = coef + 8 * list[i];
-        const double r2 = (double)m[0] * m[0] + (double)m[1] * m[1] + (double)m[4] * m[4] + (double)m[5] * m[5];
-        lg += 0.5 * log(r2);
-    }
-    for (int o = 16; o > 0; o >>= 1) lg += __shfl_xor_sync(0xffffffffu, lg, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lg;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
-        rho[blockIdx.x] = exp(t);
+    __shared__ double acc;
+    coef += (int64_t)8 * blockIdx.x * coef_stride;
+    if (threadIdx.x == 0) acc = 0;
+    for (int g = 0; g < ngroups; g++) {
+        double lg = 0;
+        for (int i = ptr[g] + threadIdx.x; i < ptr[g + 1]; i += blockDim.x) {
+            const float* m = coef + 8 * src[i];
+            const double r2 = (double)m[0] * m[0] + (double)m[1] * m[1] + (double)m[4] * m[4] + (double)m[5] * m[5];
+            lg += 0.5 * log(r2);
+        }
+        for (int o = 16; o > 0; o >>= 1) lg += __shfl_xor_sync(0xffffffffu, lg, o);
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lg;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) acc += red[w];
+            rho[(int64_t)blockIdx.x * ngroups + g] = exp(acc);
+        }
     }
 }
 
-extern "C" int qgt_dev_scale_product(const float* coef32, int32_t ncoef, const int32_t* list, int32_t n, double* rho,
-                                     int32_t npoints, void* s)
+extern "C" int qgt_dev_scale_product(const float* coef32, int32_t coef_stride, const int32_t* ptr, const int32_t* src,
+                                     int32_t ngroups, double* rho, int32_t npoints, void* s)
 {
-    if (npoints < 1 || n < 0) return qgt_set_error(QGT_EINVAL, "scale product: bad arguments");
-    scale_product_kernel<<<npoints, 256, 0, (cudaStream_t)s>>>(coef32, ncoef, list, n, rho);
+    if (npoints < 1 || ngroups < 0) return qgt_set_error(QGT_EINVAL, "scale product: bad arguments");
+    if (ngroups == 0) return 0;
+    scale_product_kernel<<<npoints, 256, 0, (cudaStream_t)s>>>(coef32, coef_stride, ptr, src, ngroups, rho);
+    return qgt_dev_last_error();
+}
+
+// combined phase entries of diagonal runs (products formed in FP64)
+__global__ void combine_diag_kernel(double* __restrict__ coef, float* __restrict__ coef32, int stride, int base,
+                                    const int32_t* __restrict__ ptr, const int32_t* __restrict__ src, int ncomb)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ncomb) return;
+    const int64_t off = (int64_t)8 * blockIdx.y * stride;
+    for (int t = 0; t < 2; t++) {
+        double a0r = 1, a0i = 0, a1r = 1, a1i = 0;
+        if (t == 0 && !coef) continue;
+        if (t == 1 && !coef32) continue;
+        for (int i = ptr[k]; i < ptr[k + 1]; i++) {
+            const int64_t e = off + (int64_t)8 * src[i];
+            const double p0r = t ? coef32[e] : coef[e], p0i = t ? coef32[e + 1] : coef[e + 1];
+            const double p1r = t ? coef32[e + 6] : coef[e + 6], p1i = t ? coef32[e + 7] : coef[e + 7];
+            double x = a0r * p0r - a0i * p0i;
+            a0i = a0r * p0i + a0i * p0r;
+            a0r = x;
+            x = a1r * p1r - a1i * p1i;
+            a1i = a1r * p1i + a1i * p1r;
+            a1r = x;
+        }
+        const int64_t d = off + (int64_t)8 * (base + k);
+        const double m[8] = {a0r, a0i, 0, 0, 0, 0, a1r, a1i};
+        for (int i = 0; i < 8; i++) {
+            if (t) coef32[d + i] = (float)m[i];
+            else coef[d + i] = m[i];
+        }
+    }
+}
+
+extern "C" int qgt_dev_combine_diag(double* coef, float* coef32, int32_t stride, int32_t base, const int32_t* ptr,
+                                    const int32_t* src, int32_t ncomb, int32_t npoints, void* s)
+{
+    if (ncomb <= 0) return 0;
+    if (npoints < 1 || npoints > 65535) return qgt_set_error(QGT_EINVAL, "combine: %d points", npoints);
+    combine_diag_kernel<<<dim3((ncomb + 127) / 128, npoints), 128, 0, (cudaStream_t)s>>>(coef, coef32, stride, base, ptr,
+                                                                                           src, ncomb);
     return qgt_dev_last_error();
 }
 
 extern "C" int qgt_dev_prepare32(const qgt_dev_coef_desc_t* d, int32_t ncoef, const double* theta, float* coef,
-                                 int32_t npoints, int32_t theta_stride, void* s)
+                                 int32_t npoints, int32_t theta_stride, int32_t coef_stride, void* s)
 {
     if (ncoef <= 0) return QGT_OK;
     if (npoints < 1 || npoints > 65535) return qgt_set_error(QGT_EINVAL, "prepare32: %d points", npoints);
-    prepare32_kernel<<<dim3((ncoef + 7) / 8, npoints), 256, 0, (cudaStream_t)s>>>(d, ncoef, theta, coef, theta_stride);
+    prepare32_kernel<<<dim3((ncoef + 7) / 8, npoints), 256, 0, (cudaStream_t)s>>>(d, ncoef, theta, coef, theta_stride,
+                                                                                    coef_stride);
     return qgt_dev_last_error();
 }

@@ -322,6 +322,22 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
                         ci = cr * pi + ci * pr;
                         cr = t;
                     }
+                } else if (so.kind == Q2_CZM) {
+                    // register bit ra against the thread qubits in slot: sign of its |1> factor
+                    if (__popc(pthr & (uint32_t)so.slot) & 1) {
+                        const int ri = so.ra - RL_REG;
+#pragma unroll
+                        for (int i = 0; i < RB; i++)
+                            if (i == ri) { f1r[i] = -f1r[i]; f1i[i] = -f1i[i]; }
+                    }
+                } else if (so.kind == Q2_CZT) {
+                    // thread qubit q against the thread qubits in slot
+                    if (((pthr >> so.q) & 1u) && (__popc(pthr & (uint32_t)so.slot) & 1)) {
+                        cr = -cr;
+                        ci = -ci;
+                    }
+                } else if (so.kind == Q2_ZGEN) {
+                    // marker of a derivative spawned in the run (applied after it)
                 } else {  // Q2_CZ
                     const bool rb_reg = so.rb >= RL_REG && so.rb < RL_WARP;
                     if (ra_reg && rb_reg) continue;  // in the static mask

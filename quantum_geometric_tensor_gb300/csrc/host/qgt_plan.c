@@ -76,11 +76,20 @@ struct qgt_plan {
      * through [cut, G), then [cut, G) backward (inverse gates) with the
      * second-half slots; part_begin[] delimits the three parts in `gates` */
     int mitm, cut, nparts, early_slots, row_T, orig_ngates;
+    int* op_gate;                 /* gate (index into gates) of each op */
+    /* combined phase entries of diagonal runs: entry ncoef + k = product of
+     * comb_src[comb_ptr[k] .. comb_ptr[k+1]) (formed per step on the device) */
+    int ncomb, comb_nsrc;
+    int32_t *comb_ptr_h, *comb_src_h, *comb_ptr_d, *comb_src_d;
     int host_only;                /* schedule only (no device resources): qgt_plan_schedule_dump */
     int part_begin[4];
-    int32_t* late_coef_h;
-    int nlate_coef;
-    int32_t* late_coef_d;
+    /* amplitude-scale bookkeeping of meet in the middle (complex64 gates are
+     * not exactly unitary): group m = the coefficient entries of psi-forward
+     * pass m and of its mirror; rho[m] = product of their scales over groups
+     * 0..m; a row carried through groups 0..m (row_group = m) is divided by it */
+    int nscale_groups;
+    int32_t *scale_ptr_h, *scale_src_h, *row_group_h;
+    int32_t *scale_ptr_d, *scale_src_d, *row_group_d;
     double* rho_d;
     int Pd;                       /* parameters [0, Pd) get derivative rows; Q is Pd x Pd */
     int64_t pstride;              /* amplitudes between points in V: (rows + 1) N */
@@ -218,6 +227,54 @@ static int commute(const sgate_t* a, const sgate_t* b)
 /* schedule                                                                  */
 /* ------------------------------------------------------------------------ */
 
+/* Backward part of meet in the middle: the psi-forward passes (part 1) in
+ * reverse order, each with its ops reversed and every gate replaced by its
+ * inverse (the coefficient entry of the matching part-2 gate, which also
+ * carries the gate's derivative slot).  A pass and its mirror share the tile
+ * set, so backward pass j starts exactly where forward pass nP-1-j ended and
+ * can spawn from psi as the forward pass left it. */
+static int mirror_backward_passes(qgt_plan_t* p)
+{
+    const int c = p->cut, G = p->orig_ngates, L2 = G - c;
+    int nP = 0;
+    for (int k = 0; k < p->npasses; k++) nP += p->passes[k].part == 1;
+    spass_t* np2 = (spass_t*)realloc(p->passes, sizeof(spass_t) * (size_t)(p->npasses + nP + 1));
+    if (!np2) return qgt_set_error(E_NOMEM, "schedule: oom");
+    p->passes = np2;
+    int extra = 0;
+    for (int k = 0; k < p->npasses; k++) if (p->passes[k].part == 1) extra += p->passes[k].op_count;
+    qgt_dev_op_t* nops = (qgt_dev_op_t*)realloc(p->ops_h, sizeof(qgt_dev_op_t) * (size_t)(p->nops + extra + 1));
+    int* ng = (int*)realloc(p->op_gate, sizeof(int) * (size_t)(p->nops + extra + 1));
+    if (nops) p->ops_h = nops;
+    if (ng) p->op_gate = ng;
+    if (!nops || !ng) return qgt_set_error(E_NOMEM, "schedule: oom");
+    const int np = p->npasses;
+    for (int k = np - 1; k >= 0; k--) {
+        const spass_t* src = &p->passes[k];
+        if (src->part != 1) continue;
+        spass_t* ps = &p->passes[p->npasses++];
+        *ps = *src;
+        ps->part = 2;
+        ps->op_begin = p->nops;
+        for (int j = src->op_count - 1; j >= 0; j--) {
+            const int si = src->op_begin + j;
+            const int g = p->op_gate[si];                 /* forward copy of original gate g, c <= g < G */
+            const int bg = c + L2 + (G - 1 - g);          /* its inverse in part 2 */
+            const sgate_t* bgate = &p->gates[bg];
+            qgt_dev_op_t op = p->ops_h[si];
+            op.coef = bgate->coef;
+            op.slot = bgate->slot;
+            op.gen = QGEN_NONE;
+            if (bgate->slot >= 0)
+                op.gen = bgate->type == QGT_GATE_RX ? QGEN_X : (bgate->type == QGT_GATE_RY ? QGEN_Y : QGEN_Z);
+            p->op_gate[p->nops] = bg;
+            p->ops_h[p->nops++] = op;
+        }
+        ps->op_count = p->nops - ps->op_begin;
+    }
+    return 0;
+}
+
 static int compile_schedule(qgt_plan_t* p)
 {
     const int n = p->n, G = p->ngates;
@@ -234,7 +291,13 @@ static int compile_schedule(qgt_plan_t* p)
         return qgt_set_error(E_NOMEM, "schedule: out of memory");
     }
     int nord = 0, np = 0;
-    for (int part = 0; part < p->nparts; part++) {
+    /* with meet in the middle the backward part mirrors the psi-forward passes
+     * (mirror_backward_passes), so only the first two parts are scheduled here */
+    const int sched_parts = p->mitm ? 2 : p->nparts;
+    free(p->op_gate);
+    p->op_gate = (int*)calloc((size_t)G + 1, sizeof(int));
+    if (!p->op_gate) { free(placed); free(blocked); free(order); return qgt_set_error(E_NOMEM, "schedule: oom"); }
+    for (int part = 0; part < sched_parts; part++) {
     const int g0 = p->part_begin[part], g1 = p->part_begin[part + 1];
     int remaining = 0;
     for (int g = g0; g < g1; g++) {
@@ -287,6 +350,7 @@ static int compile_schedule(qgt_plan_t* p)
         for (int k = start; k < nord; k++) {
             const sgate_t* g = &p->gates[order[k]];
             qgt_dev_op_t* op = &p->ops_h[k];
+            p->op_gate[k] = order[k];
             memset(op, 0, sizeof *op);
             op->q = (int8_t)g->q0;
             op->q2 = (int8_t)(g->q1 >= 0 ? g->q1 : 0);
@@ -320,7 +384,7 @@ static int compile_schedule(qgt_plan_t* p)
     free(placed);
     free(blocked);
     free(order);
-    return 0;
+    return p->mitm ? mirror_backward_passes(p) : 0;
 }
 
 /* entries: psi ping-pongs between row 0 and row `rows`, ending in row 0 */
@@ -433,14 +497,12 @@ static int setup_transport(qgt_plan_t* p)
     sgate_t* ext = (sgate_t*)calloc((size_t)(c + 2 * L2) + 1, sizeof(sgate_t));
     qgt_dev_coef_desc_t* nc = (qgt_dev_coef_desc_t*)realloc(p->coef_h, sizeof(qgt_dev_coef_desc_t) * ((size_t)p->ncoef + L2 + 1));
     if (nc) p->coef_h = nc;
-    p->late_coef_h = (int32_t*)malloc(sizeof(int32_t) * (2 * (size_t)L2 + 1));
-    if (!ext || !nc || !p->late_coef_h) { free(ext); return qgt_set_error(E_NOMEM, "transport: out of memory"); }
+    if (!ext || !nc) { free(ext); return qgt_set_error(E_NOMEM, "transport: out of memory"); }
     int nl = 0;
     for (int g = 0; g < c; g++) ext[g] = p->gates[g];
     for (int g = c; g < G; g++) {
         ext[g] = p->gates[g];
         ext[g].slot = -1;
-        if (ext[g].coef >= 0) p->late_coef_h[nl++] = ext[g].coef;
     }
     for (int k = 0; k < L2; k++) {
         sgate_t e = p->gates[G - 1 - k];
@@ -449,7 +511,6 @@ static int setup_transport(qgt_plan_t* p)
             p->coef_h[ni] = p->coef_h[e.coef];
             p->coef_h[ni].type |= QGT_COEF_INVERSE;
             e.coef = ni;
-            p->late_coef_h[nl++] = ni;
         }
         ext[c + L2 + k] = e;
     }
@@ -463,8 +524,8 @@ static int setup_transport(qgt_plan_t* p)
     p->part_begin[3] = c + 2 * L2;
     p->cut = c;
     p->early_slots = half;
-    p->nlate_coef = nl;
-    p->pstride = (int64_t)(p->rows + 2) * p->N;   /* two spare psi rows */
+    (void)nl;
+    p->pstride = (int64_t)(p->rows + 2) * p->N;   /* final value set with the entries (psi checkpoints) */
     return 0;
 }
 
@@ -485,7 +546,8 @@ static int add_entry(qgt_plan_t* p, int* cap, const qgt_dev_entry_t* e)
 
 /* entries of the three meet-in-the-middle parts (see setup_transport):
  * rows 0 psi(cut), 1 H psi carried to the cut, 2 + s slot s at the cut;
- * spares rows and rows + 1 hold psi beyond the cut */
+ * row `rows` is psi's second buffer in the forward part, rows + 1 + m holds
+ * psi after psi-forward pass m (the start of its mirrored backward pass) */
 static int build_entries_mitm(qgt_plan_t* p)
 {
     int cap = 64, rc = 0;
@@ -495,12 +557,17 @@ static int build_entries_mitm(qgt_plan_t* p)
     if (!p->ents_h || !live) { free(live); return qgt_set_error(E_NOMEM, "entries: oom"); }
     const int rmax = (p->opt.precision == QGT_PRECISION_MIXED && !p->small_nsplit) ? QENT_ROWMAX : 0;
     const int has_h = p->opt.hamiltonian != QGT_HAMILTONIAN_NONE;
-    const int RA = p->rows, RB = p->rows + 1;
-    int nf = 0, nb = 0;
-    for (int k = 0; k < p->npasses; k++) { nf += p->passes[k].part == 0; nb += p->passes[k].part == 2; }
+    const int RA = p->rows;
+    int nf = 0, nP = 0, nb = 0;
+    for (int k = 0; k < p->npasses; k++) {
+        nf += p->passes[k].part == 0;
+        nP += p->passes[k].part == 1;
+        nb += p->passes[k].part == 2;
+    }
+    p->pstride = (int64_t)(p->rows + 1 + nP) * p->N;
     p->vector_passes = 0;
     p->gate_bytes = 0;
-    int fi = 0, pi = 0, bi = 0, cur = 0, bsrc = 0;
+    int fi = 0, pi = 0, bi = 0;
     for (int k = 0; k < p->npasses && !rc; k++) {
         spass_t* ps = &p->passes[k];
         ps->ent_begin = p->nents;
@@ -535,29 +602,18 @@ static int build_entries_mitm(qgt_plan_t* p)
             }
             fi++;
         } else if (ps->part == 1) {
-            const int dst = (pi % 2 == 0) ? RA : RB;
             memset(&e, 0, sizeof e);
-            e.src_row = (pi == 0) ? 0 : cur;
-            e.dst_row = dst;
+            e.src_row = (pi == 0) ? 0 : p->rows + pi;
+            e.dst_row = p->rows + 1 + pi;
             e.spawn_op = -1;
             e.flags = QENT_STORE_V;
             rc = add_entry(p, &cap, &e);
-            cur = dst;
+            p->row_T = e.dst_row;
             pi++;
-            p->row_T = cur;
-            bsrc = cur;
         } else {
             const int last = (bi == nb - 1);
-            int bdst = (bsrc == RA) ? RB : RA;
-            if (!last) {
-                memset(&e, 0, sizeof e);
-                e.src_row = bsrc;
-                e.dst_row = bdst;
-                e.spawn_op = -1;
-                e.flags = QENT_STORE_V;
-                rc = add_entry(p, &cap, &e);
-            }
-            if (has_h && !rc) {
+            const int src = p->rows + 1 + (nP - 1 - bi);   /* psi where the mirrored forward pass ended */
+            if (has_h) {
                 memset(&e, 0, sizeof e);
                 e.src_row = e.dst_row = 1;
                 e.spawn_op = -1;
@@ -576,13 +632,12 @@ static int build_entries_mitm(qgt_plan_t* p)
                 const qgt_dev_op_t* op = &p->ops_h[ps->op_begin + j];
                 if (op->slot < 0) continue;
                 memset(&e, 0, sizeof e);
-                e.src_row = bsrc;
+                e.src_row = src;
                 e.dst_row = 2 + op->slot;
                 e.spawn_op = j;
                 e.flags = QENT_STORE_V | (last ? rmax : 0);
                 rc = add_entry(p, &cap, &e);
             }
-            if (!last) bsrc = bdst;
             bi++;
         }
         for (int j = 0; j < ps->op_count; j++) {
@@ -594,7 +649,44 @@ static int build_entries_mitm(qgt_plan_t* p)
         p->vector_passes += ps->ent_count;
     }
     free(live);
-    return rc;
+    if (rc) return rc;
+    /* scale groups: psi-forward pass m and backward pass nP-1-m (its mirror) */
+    p->nscale_groups = nP;
+    p->scale_ptr_h = (int32_t*)calloc((size_t)nP + 1, sizeof(int32_t));
+    p->scale_src_h = (int32_t*)malloc(sizeof(int32_t) * ((size_t)p->nops + 1));
+    p->row_group_h = (int32_t*)malloc(sizeof(int32_t) * ((size_t)p->rows + 1));
+    if (!p->scale_ptr_h || !p->scale_src_h || !p->row_group_h) return qgt_set_error(E_NOMEM, "entries: oom");
+    int ns = 0, m = 0, bj = 0;
+    int* pk = (int*)malloc(sizeof(int) * ((size_t)nP + 1));
+    int* bk = (int*)malloc(sizeof(int) * ((size_t)nP + 1));
+    if (!pk || !bk) { free(pk); free(bk); return qgt_set_error(E_NOMEM, "entries: oom"); }
+    for (int k = 0; k < p->npasses; k++) {
+        if (p->passes[k].part == 1) pk[m++] = k;
+        if (p->passes[k].part == 2) bk[bj++] = k;
+    }
+    for (m = 0; m < nP; m++) {
+        const spass_t* a = &p->passes[pk[m]];
+        const spass_t* bpass = &p->passes[bk[nP - 1 - m]];
+        for (int j = 0; j < a->op_count; j++)
+            if (p->ops_h[a->op_begin + j].coef >= 0) p->scale_src_h[ns++] = p->ops_h[a->op_begin + j].coef;
+        for (int j = 0; j < bpass->op_count; j++)
+            if (p->ops_h[bpass->op_begin + j].coef >= 0) p->scale_src_h[ns++] = p->ops_h[bpass->op_begin + j].coef;
+        p->scale_ptr_h[m + 1] = ns;
+    }
+    /* rows: psi(cut) and first-half slots none; H psi all groups; a second-half
+     * slot spawned in backward pass j crosses groups 0 .. nP-1-j */
+    for (int r = 0; r < p->rows; r++) p->row_group_h[r] = -1;
+    if (has_h) p->row_group_h[1] = nP - 1;
+    for (int j = 0; j < nb; j++) {
+        const spass_t* ps = &p->passes[bk[j]];
+        for (int t = 0; t < ps->op_count; t++) {
+            const int sl = p->ops_h[ps->op_begin + t].slot;
+            if (sl >= 0) p->row_group_h[2 + sl] = nP - 1 - j;
+        }
+    }
+    free(pk);
+    free(bk);
+    return 0;
 }
 
 /* Register-resident programs for passes whose tile has the full width
@@ -728,9 +820,123 @@ static int build_programs(qgt_plan_t* p)
  * each amplitude once by the run's combined phase instead of once per gate.
  * Diagonal ops commute, so a derivative generator (-i/2) Z spawned inside the
  * run is applied after it. */
+/* add a combined phase entry (product of the listed coefficient entries'
+ * diagonals), or return the entry itself for a single factor */
+static int comb_entry(qgt_plan_t* p, const int* list, int n)
+{
+    if (n == 1) return list[0];
+    int32_t* ns = (int32_t*)realloc(p->comb_src_h, sizeof(int32_t) * ((size_t)p->comb_nsrc + n + 1));
+    int32_t* np = (int32_t*)realloc(p->comb_ptr_h, sizeof(int32_t) * ((size_t)p->ncomb + 2));
+    if (ns) p->comb_src_h = ns;
+    if (np) p->comb_ptr_h = np;
+    if (!ns || !np) return -1;
+    if (p->ncomb == 0) p->comb_ptr_h[0] = 0;
+    for (int i = 0; i < n; i++) p->comb_src_h[p->comb_nsrc++] = list[i];
+    p->comb_ptr_h[p->ncomb + 1] = p->comb_nsrc;
+    return p->ncoef + p->ncomb++;
+}
+
+/* One run of diagonal ops src[j, e) as a compact Q2_DIAG block: one phase
+ * factor per register bit and per thread qubit (products of the run's
+ * coefficients, formed once per step by the combine kernel), the CZs as
+ * parity masks (register-register pairs in the header's static sign mask,
+ * register-thread pairs per register bit, thread-thread pairs per qubit),
+ * and a Q2_ZGEN marker for each derivative spawned inside the run. */
+static int emit_diag_run(qgt_plan_t* p, const qgt_dev_op2_t* src, int j, int e, qgt_dev_op2_t* out_ops, int* out,
+                         int nb, int* remap)
+{
+    int lists[40][64];
+    int nl[40];
+    int8_t role[40];
+    memset(nl, 0, sizeof nl);
+    memset(role, 0, sizeof role);
+    uint32_t regmask = 0, czm[8] = {0}, czt[32] = {0};
+    for (int t = j; t < e; t++) {
+        const qgt_dev_op2_t* o = &src[t];
+        const int ra_reg = o->ra >= RL_REG_ && o->ra < RL_WARP_;
+        if (o->kind == Q2_PHASE) {
+            /* slot index 0..7: register bits, 8 + q: thread qubit q */
+            const int key = ra_reg ? (o->ra - RL_REG_) : 8 + o->q;
+            if (key >= 40 || nl[key] >= 64) return qgt_set_error(E_STATE, "programs: diagonal run too long");
+            role[key] = (int8_t)o->ra;
+            lists[key][nl[key]++] = o->coef;
+        } else {
+            const int rb_reg = o->rb >= RL_REG_ && o->rb < RL_WARP_;
+            if (ra_reg && rb_reg) {
+                const int a = o->ra - RL_REG_, b = o->rb - RL_REG_;
+                for (int r = 0; r < 32; r++)
+                    if (((r >> a) & 1) && ((r >> b) & 1)) regmask ^= 1u << r;
+            } else if (ra_reg || rb_reg) {
+                const int i = (ra_reg ? o->ra : o->rb) - RL_REG_;
+                const int q = ra_reg ? o->q2 : o->q;
+                czm[i] ^= 1u << q;
+            } else {
+                const int a = o->q < o->q2 ? o->q : o->q2, b = o->q < o->q2 ? o->q2 : o->q;
+                czt[a] ^= 1u << b;
+            }
+        }
+    }
+    int cnt = 0;
+    for (int k = 0; k < 40; k++) cnt += nl[k] > 0;
+    for (int i = 0; i < 8; i++) cnt += czm[i] != 0;
+    for (int a = 0; a < 32; a++) cnt += czt[a] != 0;
+    for (int t = j; t < e; t++) cnt += src[t].slot >= 0;
+    qgt_dev_op2_t h;
+    memset(&h, 0, sizeof h);
+    h.kind = Q2_DIAG;
+    h.seg = (int16_t)cnt;
+    h.coef = -1;
+    h.slot = (int32_t)regmask;
+    out_ops[(*out)++] = h;
+    for (int k = 0; k < 40; k++) {
+        if (!nl[k]) continue;
+        qgt_dev_op2_t x;
+        memset(&x, 0, sizeof x);
+        x.kind = Q2_PHASE;
+        x.ra = (uint8_t)role[k];
+        x.q = (int8_t)(k >= 8 ? k - 8 : 0);
+        x.slot = -1;
+        x.coef = comb_entry(p, lists[k], nl[k]);
+        if (x.coef < 0) return qgt_set_error(E_NOMEM, "programs: oom");
+        out_ops[(*out)++] = x;
+    }
+    for (int i = 0; i < 8; i++) {
+        if (!czm[i]) continue;
+        qgt_dev_op2_t x;
+        memset(&x, 0, sizeof x);
+        x.kind = Q2_CZM;
+        x.ra = (uint8_t)(RL_REG_ + i);
+        x.coef = -1;
+        x.slot = (int32_t)czm[i];
+        out_ops[(*out)++] = x;
+    }
+    for (int a = 0; a < 32; a++) {
+        if (!czt[a]) continue;
+        qgt_dev_op2_t x;
+        memset(&x, 0, sizeof x);
+        x.kind = Q2_CZT;
+        x.q = (int8_t)a;
+        x.coef = -1;
+        x.slot = (int32_t)czt[a];
+        out_ops[(*out)++] = x;
+    }
+    for (int t = j; t < e; t++) {
+        if (src[t].slot < 0) continue;
+        qgt_dev_op2_t x = src[t];
+        x.kind = Q2_ZGEN;
+        x.coef = -1;
+        remap[t] = *out - nb;
+        out_ops[(*out)++] = x;
+    }
+    for (int t = j; t < e; t++)
+        if (src[t].slot < 0) remap[t] = -1;   /* no entry spawns at a plain op */
+    return 0;
+}
+
 static int fold_diagonal_runs(qgt_plan_t* p)
 {
     if (p->nprog == 0) return 0;
+    int rc = 0;
     const int cap = p->nprog + p->nprog / 2 + 16;
     qgt_dev_op2_t* np2 = (qgt_dev_op2_t*)calloc((size_t)cap, sizeof(qgt_dev_op2_t));
     int* remap = (int*)malloc(sizeof(int) * ((size_t)p->nprog + 1));
@@ -745,23 +951,7 @@ static int fold_diagonal_runs(qgt_plan_t* p)
             int e = j;
             while (e < n && (src[e].kind == Q2_PHASE || src[e].kind == Q2_CZ)) e++;
             if (e - j >= 2 && out + (e - j) + 1 < cap) {
-                qgt_dev_op2_t h;
-                memset(&h, 0, sizeof h);
-                h.kind = Q2_DIAG;
-                h.seg = (int16_t)(e - j);
-                h.coef = -1;
-                uint32_t mask = 0;
-                for (int t = j; t < e; t++) {
-                    const qgt_dev_op2_t* o = &src[t];
-                    if (o->kind == Q2_CZ && o->ra >= RL_REG_ && o->ra < RL_WARP_ && o->rb >= RL_REG_ && o->rb < RL_WARP_) {
-                        const int a = o->ra - RL_REG_, b = o->rb - RL_REG_;
-                        for (int r = 0; r < 32; r++)
-                            if (((r >> a) & 1) && ((r >> b) & 1)) mask ^= 1u << r;
-                    }
-                }
-                h.slot = (int32_t)mask;
-                np2[out++] = h;
-                for (int t = j; t < e; t++) { remap[t] = out - nb; np2[out++] = src[t]; }
+                if ((rc = emit_diag_run(p, src, j, e, np2, &out, nb, remap)) != 0) { free(np2); free(remap); return rc; }
                 j = e;
             } else {
                 if (e == j) e = j + 1;
@@ -936,8 +1126,16 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
     DALLOC(p->ops_d, sizeof(qgt_dev_op_t) * (size_t)(p->nops + 1));
     DALLOC(p->ents_d, sizeof(qgt_dev_entry_t) * (size_t)(p->nents + 1));
     DALLOC(p->coef_desc_d, sizeof(qgt_dev_coef_desc_t) * (size_t)(p->ncoef + 1));
-    DALLOC(p->coef_d, sizeof(double) * 8 * (size_t)p->B * (size_t)(p->ncoef + 1));
-    DALLOC(p->coef32_d, sizeof(float) * 8 * (size_t)p->B * (size_t)(p->ncoef + 1));
+    DALLOC(p->coef_d, sizeof(double) * 8 * (size_t)p->B * (size_t)(p->ncoef + p->ncomb + 1));
+    DALLOC(p->coef32_d, sizeof(float) * 8 * (size_t)p->B * (size_t)(p->ncoef + p->ncomb + 1));
+    if (p->ncomb) {
+        DALLOC(p->comb_ptr_d, sizeof(int32_t) * (size_t)(p->ncomb + 1));
+        DALLOC(p->comb_src_d, sizeof(int32_t) * (size_t)(p->comb_nsrc + 1));
+        if ((rc = qgt_dev_memcpy_h2d(p->comb_ptr_d, p->comb_ptr_h, sizeof(int32_t) * (size_t)(p->ncomb + 1), p->stream)) != 0)
+            goto fail;
+        if ((rc = qgt_dev_memcpy_h2d(p->comb_src_d, p->comb_src_h, sizeof(int32_t) * (size_t)p->comb_nsrc, p->stream)) != 0)
+            goto fail;
+    }
     DALLOC(p->prog_d, sizeof(qgt_dev_op2_t) * (size_t)(p->nprog + 1));
     DALLOC(p->segs_d, (size_t)16 * (p->nsegs + 1));
     {
@@ -958,9 +1156,16 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
             goto fail;
     }
     if (p->mitm && !p->fp64 && p->nprog > 0) {
-        DALLOC(p->late_coef_d, sizeof(int32_t) * (size_t)(p->nlate_coef + 1));
-        DALLOC(p->rho_d, sizeof(double) * (size_t)p->B);
-        if (p->nlate_coef && (rc = qgt_dev_memcpy_h2d(p->late_coef_d, p->late_coef_h, sizeof(int32_t) * (size_t)p->nlate_coef,
+        const int ng = p->nscale_groups;
+        DALLOC(p->scale_ptr_d, sizeof(int32_t) * (size_t)(ng + 1));
+        DALLOC(p->scale_src_d, sizeof(int32_t) * (size_t)(p->scale_ptr_h[ng] + 1));
+        DALLOC(p->row_group_d, sizeof(int32_t) * (size_t)p->rows);
+        DALLOC(p->rho_d, sizeof(double) * (size_t)p->B * ng);
+        if ((rc = qgt_dev_memcpy_h2d(p->scale_ptr_d, p->scale_ptr_h, sizeof(int32_t) * (size_t)(ng + 1), p->stream)) != 0)
+            goto fail;
+        if ((rc = qgt_dev_memcpy_h2d(p->row_group_d, p->row_group_h, sizeof(int32_t) * (size_t)p->rows, p->stream)) != 0)
+            goto fail;
+        if (p->scale_ptr_h[ng] && (rc = qgt_dev_memcpy_h2d(p->scale_src_d, p->scale_src_h, sizeof(int32_t) * (size_t)p->scale_ptr_h[ng],
                                                       p->stream)) != 0)
             goto fail;
     }
@@ -1037,7 +1242,10 @@ void qgt_plan_destroy(qgt_plan_t* p)
     if (p->host_only) {
         free(p->gates); free(p->passes); free(p->ops_h); free(p->ents_h); free(p->coef_h); free(p->prog_h);
         free(p->segs_h); free(p->slot_param_h); free(p->param_ptr_h); free(p->param_slots_h); free(p->pauli_h);
-        free(p->late_coef_h);
+        free(p->scale_ptr_h); free(p->scale_src_h); free(p->row_group_h);
+        free(p->op_gate);
+        free(p->comb_ptr_h);
+        free(p->comb_src_h);
         free(p);
         return;
     }
@@ -1047,8 +1255,13 @@ void qgt_plan_destroy(qgt_plan_t* p)
     qgt_dev_dg_gram_destroy(p->dg);
     qgt_dev_free(p->rowmax_d);
     free(p->pauli_h);
-    free(p->late_coef_h);
-    void* dev[] = {p->V, p->split, p->small_part_d, p->pauli_d, p->late_coef_d, p->rho_d, p->ops_d, p->ents_d, p->prog_d, p->segs_d, p->coef32_d, p->coef_desc_d, p->coef_d, p->theta_d, p->HG_d, p->part_d,
+    free(p->scale_ptr_h); free(p->scale_src_h); free(p->row_group_h);
+    free(p->op_gate);
+    free(p->comb_ptr_h);
+    free(p->comb_src_h);
+    void* dev[] = {p->V, p->split, p->small_part_d, p->pauli_d, p->scale_ptr_d, p->scale_src_d, p->row_group_d,
+                   p->rho_d, p->comb_ptr_d, p->comb_src_d,
+                   p->ops_d, p->ents_d, p->prog_d, p->segs_d, p->coef32_d, p->coef_desc_d, p->coef_d, p->theta_d, p->HG_d, p->part_d,
                    p->Q_d, p->grad_d, p->energy_d, p->natgrad_d, p->chol_work_d, p->status_d, p->slot_param_d,
                    p->param_ptr_d, p->param_slots_d};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++) qgt_dev_free(dev[i]);
@@ -1120,18 +1333,26 @@ static int run_step(qgt_plan_t* p)
     int rc;
     int launches = 0;
     MARK(0);
-    if ((rc = qgt_dev_prepare(p->coef_desc_d, p->ncoef, p->theta_d, p->coef_d, p->B, p->P, p->stream)) != 0) return rc;
+    const int cstride = p->ncoef + p->ncomb;
+    if ((rc = qgt_dev_prepare(p->coef_desc_d, p->ncoef, p->theta_d, p->coef_d, p->B, p->P, cstride, p->stream)) != 0)
+        return rc;
     launches += p->ncoef > 0;
     if (!p->fp64 && p->nprog > 0) {
-        if ((rc = qgt_dev_prepare32(p->coef_desc_d, p->ncoef, p->theta_d, p->coef32_d, p->B, p->P, p->stream)) != 0)
+        if ((rc = qgt_dev_prepare32(p->coef_desc_d, p->ncoef, p->theta_d, p->coef32_d, p->B, p->P, cstride, p->stream)) != 0)
             return rc;
         launches += p->ncoef > 0;
         if (p->rho_d) {
-            if ((rc = qgt_dev_scale_product(p->coef32_d, p->ncoef, p->late_coef_d, p->nlate_coef, p->rho_d, p->B,
-                                            p->stream)) != 0)
+            if ((rc = qgt_dev_scale_product(p->coef32_d, cstride, p->scale_ptr_d, p->scale_src_d, p->nscale_groups,
+                                            p->rho_d, p->B, p->stream)) != 0)
                 return rc;
             launches++;
         }
+    }
+    if (p->ncomb) {
+        if ((rc = qgt_dev_combine_diag(p->fp64 ? p->coef_d : NULL, p->fp64 ? NULL : p->coef32_d, cstride, p->ncoef,
+                                       p->comb_ptr_d, p->comb_src_d, p->ncomb, p->B, p->stream)) != 0)
+            return rc;
+        launches++;
     }
     if (p->dg && (rc = qgt_dev_memset(p->rowmax_d, 0, sizeof(uint32_t) * (size_t)p->rows * p->B, p->stream)) != 0)
         return rc;
@@ -1163,7 +1384,7 @@ static int run_step(qgt_plan_t* p)
         memcpy(a.local_to_phys, ps->l2p, sizeof a.local_to_phys);
         a.rowmax = p->rowmax_d;
         a.npoints = p->B;
-        a.coef_stride = p->ncoef;
+        a.coef_stride = p->ncoef + p->ncomb;
         a.point_stride = p->pstride;
         a.rowmax_stride = p->rows;
         if (ps->prog_count > 0) {
@@ -1245,8 +1466,9 @@ static int run_step(qgt_plan_t* p)
         pa.Q = p->Q_d;
         pa.grad = p->grad_d;
         pa.energy = p->energy_d;
-        pa.late_scale = p->rho_d;
-        pa.late_row0 = p->mitm ? 2 + p->early_slots : 0;
+        pa.rho = p->rho_d;
+        pa.row_group = p->row_group_d;
+        pa.ngroups = p->nscale_groups;
         if ((rc = qgt_dev_post(&pa, p->stream)) != 0) return rc;
         launches += 1 + has_h;
         MARK(5);

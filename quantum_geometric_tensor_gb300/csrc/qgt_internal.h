@@ -110,7 +110,10 @@ typedef struct {
  * bits are register bits / warp bits) through shared memory.  Bits are
  * role-encoded: 0..4 lane bit, 8 + i register bit i, 16 + w warp bit w,
  * 32 outside the tile (physical qubit in q / q2). */
-enum { Q2_SEG = 1, Q2_U = 2, Q2_UR = 3, Q2_PHASE = 4, Q2_CZ = 5, Q2_CNOT = 6, Q2_DIAG = 7 };
+enum { Q2_SEG = 1, Q2_U = 2, Q2_UR = 3, Q2_PHASE = 4, Q2_CZ = 5, Q2_CNOT = 6, Q2_DIAG = 7,
+       Q2_CZM = 8,    /* in a diagonal run: register bit ra's |1> factor flips sign when popc(thread bits & slot) is odd */
+       Q2_CZT = 9,    /* in a diagonal run: the thread factor flips when thread bit q and popc(thread bits & slot) are odd */
+       Q2_ZGEN = 10 };/* in a diagonal run: marks a derivative spawned by the rotation on (ra, q) */
 /* Q2_DIAG: header of a run of `seg` diagonal ops (Q2_PHASE / Q2_CZ) that
  * follow it; the run is applied as one per-thread phase table.  `slot` holds
  * the sign mask over the register index of the run's CZs between two register
@@ -149,11 +152,12 @@ typedef struct {
     int32_t rowmax_stride;
 } qgt_dev_pass2_args_t;
 int qgt_dev_pass2(const qgt_dev_pass2_args_t* args, int fp64, void* stream);
-/* rho[point] = product of the amplitude scales |column 0| of the listed complex64 coefficient entries */
-int qgt_dev_scale_product(const float* coef32, int32_t ncoef, const int32_t* list, int32_t n, double* rho,
-                          int32_t npoints, void* stream);
+/* rho[point][m] = product over groups 0..m of the amplitude scales |column 0|
+ * of the complex64 coefficient entries src[ptr[g] .. ptr[g+1]) */
+int qgt_dev_scale_product(const float* coef32, int32_t coef_stride, const int32_t* ptr, const int32_t* src,
+                          int32_t ngroups, double* rho, int32_t npoints, void* stream);
 int qgt_dev_prepare32(const qgt_dev_coef_desc_t* descs_dev, int32_t ncoef, const double* theta_dev,
-                      float* coef32_dev, int32_t npoints, int32_t theta_stride, void* stream);
+                      float* coef32_dev, int32_t npoints, int32_t theta_stride, int32_t coef_stride, void* stream);
 
 /* internal plan helpers used by the reference API layer and the batch driver */
 struct qgt_plan;
@@ -200,7 +204,12 @@ int qgt_dev_event_elapsed(void* start, void* end, float* ms);
 /* ---- kernels ---- */
 /* gate matrices for npoints parameter points: theta + p theta_stride -> coef + 8 p ncoef */
 int qgt_dev_prepare(const qgt_dev_coef_desc_t* descs_dev, int32_t ncoef, const double* theta_dev,
-                    double* coef_dev, int32_t npoints, int32_t theta_stride, void* stream);
+                    double* coef_dev, int32_t npoints, int32_t theta_stride, int32_t coef_stride, void* stream);
+/* combined diagonal entries: entry base + k of each point = product of the
+ * diagonals (m0 + i m1, m6 + i m7) of entries src[ptr[k] .. ptr[k+1]), in the
+ * FP64 table and / or the complex64 table (either may be NULL) */
+int qgt_dev_combine_diag(double* coef, float* coef32, int32_t coef_stride, int32_t base, const int32_t* ptr,
+                         const int32_t* src, int32_t ncomb, int32_t npoints, void* stream);
 int qgt_dev_pass(const qgt_dev_pass_args_t* args, int fp64, void* stream);
 /* out (row 1 of V, and split row 1 when split != NULL) = H psi / hscale, for
  * npoints points point_stride amplitudes apart (rowmax slots rowmax_stride apart) */
@@ -267,10 +276,11 @@ typedef struct {
     double* grad;           /* P */
     double* energy;         /* 1 */
     int32_t npoints;        /* parameter points (0 = 1): HG, Q, grad, energy blocks per point */
-    /* meet-in-the-middle: rows 1 and >= late_row0 carry the extra amplitude
-     * scale late_scale[point] of the complex64 gates they crossed twice (NULL: none) */
-    const double* late_scale;
-    int32_t late_row0;
+    /* meet in the middle with complex64 gates: row r carries the extra
+     * amplitude scale rho[point][row_group[r]] (row_group < 0: none; rho NULL: no rows) */
+    const double* rho;
+    const int32_t* row_group;
+    int32_t ngroups;
 } qgt_dev_post_args_t;
 int qgt_dev_post(const qgt_dev_post_args_t* a, void* stream);
 /* (Re Q + lambda I) x = b, FP64 Cholesky; A taken as Re of the complex Q when
