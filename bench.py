@@ -117,6 +117,22 @@ def init_dist(ws, local):
     return dist
 
 
+def max_over_ranks(x: float, dist, device=None) -> float:
+    """Max of a per-rank scalar over the ranks (timing of replicas; the only
+    collective of the benchmark, none on the data path)."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(ms_max: float, ws: int) -> float:
+    """Whole-job QGT/s of ws independent replicas, each one QGT per step."""
+    return ws * 1000.0 / ms_max
+
+
 def cpu_baseline(threads: int | None = None, S: int = 16):
     """The FP64 oracle on the host cores on a bounded sample of the workload,
     extrapolated to one full QGT step:
@@ -242,11 +258,8 @@ def run_gb300(args, ws, rank, local):
     st, lam_used = plan.status()
     if st != 0:
         raise RuntimeError(f"device status {st} after the timed steps")
-    if dist:
-        t = torch.tensor([ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * 1000.0 / ms
+    ms = max_over_ranks(ms, dist, f"cuda:{dev}")
+    value = replica_value(ms, ws)
 
     # e2e: host theta in, host Q / grad / energy / natgrad out, through the public C ABI
     e2e_steps = max(2, min(args.steps, 10))
@@ -255,10 +268,7 @@ def run_gb300(args, ws, rank, local):
     for _ in range(e2e_steps):
         out = plan.run(theta)
     e2e_ms = (time.perf_counter() - t0) * 1000.0 / e2e_steps
-    if dist:
-        t = torch.tensor([e2e_ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e2e_ms, dist, f"cuda:{dev}")
     h2d = P * 8
     d2h = P * P * 16 + 2 * P * 8 + 8
 
