@@ -391,6 +391,16 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
     }
 }
 
+// hi + lo += x with the exact rounding error of hi + x kept in lo (Knuth's TwoSum)
+static __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x)
+{
+    const float sum = __fadd_rn(hi, x);
+    const float bp = __fsub_rn(sum, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bp)), __fsub_rn(x, bp));
+    hi = sum;
+    lo = __fadd_rn(lo, err);
+}
+
 __global__ void dg_reduce_kernel(const float* __restrict__ part, const uint32_t* __restrict__ rowmax, int rows, int nbk,
                                  int ntp, int nsplit, int mbits, double2* __restrict__ HG)
 {
@@ -404,28 +414,32 @@ __global__ void dg_reduce_kernel(const float* __restrict__ part, const uint32_t*
     int ti = i >> 7, tj = j >> 7;
     int tp = ti * nbk - ti * (ti - 1) / 2 + (tj - ti);
     int64_t off = (int64_t)(i & 127) * 128 + (j & 127);
-    // 8 independent sums keep 16 loads in flight per thread (the reduction is
-    // bound by memory-level parallelism, not by its FP64 adds)
-    double re8[8] = {0, 0, 0, 0, 0, 0, 0, 0}, im8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // double-float sums in FP32 (TwoSum: the high part and the accumulated
+    // rounding errors), four of them for independent loads; FP64 conversions
+    // and adds are scarce on this part, so only the final pairs go to FP64
+    float rh[4] = {0, 0, 0, 0}, rl[4] = {0, 0, 0, 0}, ih[4] = {0, 0, 0, 0}, il[4] = {0, 0, 0, 0};
     const int64_t sstride = (int64_t)ntp * (2 * 128 * 128);
     const float* b0 = part + (int64_t)tp * (2 * 128 * 128) + off;
     int s = 0;
-    for (; s + 8 <= nsplit; s += 8) {
+    for (; s + 4 <= nsplit; s += 4) {
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
+        for (int u = 0; u < 4; u++) {
             const float* b = b0 + (int64_t)(s + u) * sstride;
-            re8[u] += (double)__ldg(b);
-            im8[u] += (double)__ldg(b + 128 * 128);
+            two_sum_acc(rh[u], rl[u], __ldg(b));
+            two_sum_acc(ih[u], il[u], __ldg(b + 128 * 128));
         }
     }
     for (; s < nsplit; s++) {
         const float* b = b0 + (int64_t)s * sstride;
-        re8[0] += (double)__ldg(b);
-        im8[0] += (double)__ldg(b + 128 * 128);
+        two_sum_acc(rh[0], rl[0], __ldg(b));
+        two_sum_acc(ih[0], il[0], __ldg(b + 128 * 128));
     }
     double re = 0, im = 0;
 #pragma unroll
-    for (int u = 0; u < 8; u++) { re += re8[u]; im += im8[u]; }
+    for (int u = 0; u < 4; u++) {
+        re += (double)rh[u] + (double)rl[u];
+        im += (double)ih[u] + (double)il[u];
+    }
     double uu = ldexp(1.0, unit_exp(rowmax[i], mbits) + unit_exp(rowmax[j], mbits));
     HG[(int64_t)i * rows + j] = make_double2(re * uu, im * uu);
     HG[(int64_t)j * rows + i] = make_double2(re * uu, -im * uu);
