@@ -226,6 +226,35 @@ int qgt_batch_execute_host(qgt_batch_t* batch, const double* theta, double* Q, d
 int qgt_batch_get_info(const qgt_batch_t* batch, qgt_batch_info_t* info);
 void qgt_batch_destroy(qgt_batch_t* batch);
 
+/* ---- plaquette Berry flux over a two-parameter lattice ------------------
+ * The Wilson-loop curvature of the reference's berry_curvature_kernel
+ * (src/cuda/quantum_phase_cuda.cu:245-313): for the plaquette at site (i, j)
+ * W = <p00|p10> <p10|p11> <p11|p01> <p01|p00> and flux = arg W (0 when
+ * |W| <= 1e-15), with p_kl the site (i + k, j + l).  There a site holds one
+ * complex number; here it holds the circuit's full state at
+ * (theta_a, theta_b) = (a0 + i da, b0 + j db), the other parameters at theta,
+ * and each link is a 2^n-amplitude inner product on the GPU.  For small
+ * spacings flux ~ 2 Im Q_ab da db at the plaquette centre.  The states of a
+ * block of lattice rows are made by one theta-batched plan; with periodic = 1
+ * site rows and columns wrap (a torus: the fluxes of all rows x cols
+ * plaquettes sum to 2 pi times an integer), with periodic = 0 the last row and
+ * column of flux are 0 as in the reference kernel. */
+typedef struct {
+    int32_t param_a, param_b;   /* distinct indices into theta */
+    int32_t rows, cols;         /* sites along theta_a and theta_b, each in [2, 4096] */
+    double a0, da, b0, db;      /* site (i, j) at theta_a = a0 + i da, theta_b = b0 + j db */
+    int32_t periodic;
+    qgt_precision_t precision;  /* QGT_PRECISION_FP64 or QGT_PRECISION_MIXED (complex64 states) */
+    int32_t device;
+} qgt_flux_options_t;
+
+/* Defaults: params 0 and 1, 32 x 32 sites on [0, 2 pi)^2, periodic, MIXED, device 0. */
+void qgt_flux_default_options(qgt_flux_options_t* opt);
+/* flux: rows x cols doubles (row-major, flux[i * cols + j]); total (NULL
+ * allowed): their sum. */
+int qgt_berry_flux_grid(const qgt_circuit_desc_t* circuit, const double* theta, const qgt_flux_options_t* opt,
+                        double* flux, double* total);
+
 /* ---- learned metric preconditioner -------------------------------------
  * No reference counterpart.  A 3-layer MLP (hidden width W, BF16 weights,
  * FP32 accumulation) maps theta (P) to M = diag(d) + U U^T (U: P x r)

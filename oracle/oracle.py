@@ -111,6 +111,8 @@ class Oracle:
         L.or_pcg_solve.argtypes = [i32, vp, vp, vp, i32, f64, vp, vp, i32]
         L.or_berry_map.argtypes = [i32, vp, i32, vp, i32, i32, i32, i32, vp]
         L.or_seed_params.argtypes = [C.c_uint64, i32, vp]
+        L.or_berry_phase.argtypes = [vp, sz, sz, vp]
+        L.or_berry_flux.argtypes = [i32, vp, i32, vp, i32, i32, i32, i32, i32, f64, f64, f64, f64, i32, vp]
 
     def seed_params(self, seed: int, count: int) -> np.ndarray:
         th = np.zeros(count)
@@ -205,6 +207,23 @@ class Oracle:
         return out
 
 
+    def berry_phase(self, states):
+        """prod_i <psi_i|psi_{i+1 mod n}> / |.| as a complex number (0 when a link vanishes)."""
+        states = [np.ascontiguousarray(x, dtype=np.complex128) for x in states]
+        ptrs = (C.c_void_p * max(len(states), 1))(*[x.ctypes.data for x in states])
+        out = np.zeros(2)
+        self.lib.or_berry_phase(C.cast(ptrs, C.c_void_p), len(states), states[0].shape[0] if states else 0, _p(out))
+        return complex(out[0], out[1])
+
+    def berry_flux(self, n, gates, theta, pa, pb, rows, cols, a0, da, b0, db, periodic=True):
+        out = np.zeros((rows, cols))
+        theta = np.ascontiguousarray(theta, dtype=np.float64)
+        rc = self.lib.or_berry_flux(n, _p(gates), len(gates), _p(theta), len(theta), pa, pb, rows, cols,
+                                    a0, da, b0, db, int(bool(periodic)), _p(out))
+        assert rc == 0
+        return out
+
+
 class Reference:
     """The reference library's own code (compiled from its sources by oracle/Makefile)."""
 
@@ -221,6 +240,7 @@ class Reference:
         L.ref_berry_curvature.argtypes = [vp, sz, vp, sz, vp]
         L.ref_natural_gradient_cg.argtypes = [vp, vp, vp, sz]
         L.ref_invert_qfim_regularized.argtypes = [vp, vp, sz, C.c_float]
+        L.ref_berry_phase.argtypes = [vp, sz, sz, vp]
 
     @staticmethod
     def available(path: str = REF_SO) -> bool:
@@ -267,6 +287,14 @@ class Reference:
         rc = self.lib.ref_berry_curvature(_p(psi), psi.shape[0], _p(np.ascontiguousarray(D)), P, _p(out))
         assert rc == 0
         return out
+
+    def berry_phase(self, states):
+        """diffgeo_compute_berry_phase (differential_geometry.c:2908-2945) as a complex number."""
+        states = [np.ascontiguousarray(x, dtype=np.complex128) for x in states]
+        ptrs = (C.c_void_p * max(len(states), 1))(*[x.ctypes.data for x in states])
+        out = np.zeros(2)
+        self.lib.ref_berry_phase(C.cast(ptrs, C.c_void_p), len(states), states[0].shape[0] if states else 0, _p(out))
+        return complex(out[0], out[1])
 
     def pauli_expectation(self, psi, n, pauli: str) -> float:
         return self.lib.ref_pauli_expectation(_p(psi), n, pauli.encode())

@@ -561,3 +561,88 @@ int or_berry_map(int n, const og_gate_t* gates, int ngates, const double* theta,
     }
     return fail ? -1 : 0;
 }
+
+/* ---- Berry phases of loops (distributed/differential_geometry.c:2908-2945;
+ *      cuda/quantum_phase_cuda.cu:245-313) ---- */
+
+static void or_inner(const double* a, const double* b, size_t dim, double* re, double* im)
+{
+    double r = 0, i = 0;
+    for (size_t k = 0; k < dim; k++) {
+        r += a[2 * k] * b[2 * k] + a[2 * k + 1] * b[2 * k + 1];
+        i += a[2 * k] * b[2 * k + 1] - a[2 * k + 1] * b[2 * k];
+    }
+    *re = r;
+    *im = i;
+}
+
+int or_berry_phase(const double* const* states, size_t n, size_t dim, double* out)
+{
+    out[0] = 1.0;
+    out[1] = 0.0;
+    if (!states || n < 2 || dim == 0) return 0;
+    for (size_t i = 0; i < n; i++) {
+        double re, im;
+        or_inner(states[i], states[(i + 1) % n], dim, &re, &im);
+        double mag = sqrt(re * re + im * im);
+        if (!(mag > 1e-14)) { out[0] = out[1] = 0.0; return -1; }
+        re /= mag;
+        im /= mag;
+        double r = out[0] * re - out[1] * im;
+        out[1] = out[0] * im + out[1] * re;
+        out[0] = r;
+    }
+    return 0;
+}
+
+int or_berry_flux(int n, const og_gate_t* gates, int ngates, const double* theta, int P, int pa, int pb,
+                  int rows, int cols, double a0, double da, double b0, double db, int periodic, double* flux)
+{
+    if (pa < 0 || pb < 0 || pa >= P || pb >= P || pa == pb || rows < 2 || cols < 2) return -1;
+    const size_t dim = (size_t)1 << n, S = (size_t)rows * cols;
+    double* st = (double*)malloc(sizeof(double) * 2 * dim * S);
+    if (!st) return -1;
+    int fail = 0;
+    #pragma omp parallel
+    {
+        double* th = (double*)malloc(sizeof(double) * (size_t)(P > 0 ? P : 1));
+        if (!th) {
+            #pragma omp atomic write
+            fail = 1;
+        } else {
+            #pragma omp for schedule(dynamic, 4)
+            for (long ij = 0; ij < (long)S; ij++) {
+                memcpy(th, theta, sizeof(double) * (size_t)P);
+                th[pa] = a0 + (double)(ij / cols) * da;
+                th[pb] = b0 + (double)(ij % cols) * db;
+                if (or_simulate(n, gates, ngates, th, st + 2 * dim * (size_t)ij) != 0) {
+                    #pragma omp atomic write
+                    fail = 1;
+                }
+            }
+        }
+        free(th);
+    }
+    if (fail) { free(st); return -1; }
+    #pragma omp parallel for schedule(dynamic, 4)
+    for (long ij = 0; ij < (long)S; ij++) {
+        const int i = (int)(ij / cols), j = (int)(ij % cols);
+        if (!periodic && (i == rows - 1 || j == cols - 1)) { flux[ij] = 0.0; continue; }
+        const int i1 = (i + 1) % rows, j1 = (j + 1) % cols;
+        const double* p00 = st + 2 * dim * ((size_t)i * cols + j);
+        const double* p10 = st + 2 * dim * ((size_t)i1 * cols + j);
+        const double* p01 = st + 2 * dim * ((size_t)i * cols + j1);
+        const double* p11 = st + 2 * dim * ((size_t)i1 * cols + j1);
+        double u[4][2];
+        or_inner(p00, p10, dim, &u[0][0], &u[0][1]);
+        or_inner(p10, p11, dim, &u[1][0], &u[1][1]);
+        or_inner(p11, p01, dim, &u[2][0], &u[2][1]);
+        or_inner(p01, p00, dim, &u[3][0], &u[3][1]);
+        double w1r = u[0][0] * u[1][0] - u[0][1] * u[1][1], w1i = u[0][0] * u[1][1] + u[0][1] * u[1][0];
+        double w2r = u[2][0] * u[3][0] - u[2][1] * u[3][1], w2i = u[2][0] * u[3][1] + u[2][1] * u[3][0];
+        double wr = w1r * w2r - w1i * w2i, wi = w1r * w2i + w1i * w2r;
+        flux[ij] = sqrt(wr * wr + wi * wi) > 1e-15 ? atan2(wi, wr) : 0.0;
+    }
+    free(st);
+    return 0;
+}

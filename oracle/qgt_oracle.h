@@ -107,6 +107,21 @@ int or_pcg_solve(int P, const double* A, const double* b, double* x, int max_ite
 int or_berry_map(int n, const og_gate_t* gates, int ngates, const double* theta, int nparams,
                  int pa, int pb, int grid, double* out);
 
+/* Berry phase of a closed loop of states, restating
+ * diffgeo_compute_berry_phase (distributed/differential_geometry.c:2908-2945):
+ * out = prod_i <psi_i|psi_{i+1 mod n}> / |.|, in loop order; {1, 0} for
+ * n < 2 or dim 0; returns -1 (out = {0, 0}) when a link is <= 1e-14. */
+int or_berry_phase(const double* const* states, size_t n, size_t dim, double* out);
+
+/* Plaquette (Wilson-loop) flux over a rows x cols lattice of circuit states
+ * at (theta_a, theta_b) = (a0 + i da, b0 + j db), restating the link
+ * products of berry_curvature_kernel (src/cuda/quantum_phase_cuda.cu:245-313)
+ * with full-state inner products as links: W = <p00|p10><p10|p11> x
+ * <p11|p01><p01|p00>, flux = arg W (0 if |W| <= 1e-15); periodic lattices
+ * wrap, otherwise the last row and column are 0. */
+int or_berry_flux(int n, const og_gate_t* gates, int ngates, const double* theta, int nparams, int pa, int pb,
+                  int rows, int cols, double a0, double da, double b0, double db, int periodic, double* flux);
+
 #ifdef __cplusplus
 }
 #endif

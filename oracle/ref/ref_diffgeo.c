@@ -29,3 +29,15 @@ REF_EXPORT int ref_berry_curvature(const double* state, size_t dim, const double
     diffgeo_engine_destroy(e);
     return ok ? 0 : -1;
 }
+
+/* diffgeo_compute_berry_phase (differential_geometry.c:2908-2945): out = {re, im}. */
+REF_EXPORT int ref_berry_phase(const double* const* states, size_t n, size_t dim, double* out)
+{
+    diffgeo_engine_t* e = diffgeo_engine_create();
+    if (!e) return -1;
+    ComplexDouble r = diffgeo_compute_berry_phase(e, (const ComplexDouble**)states, n, dim);
+    diffgeo_engine_destroy(e);
+    out[0] = r.real;
+    out[1] = r.imag;
+    return 0;
+}

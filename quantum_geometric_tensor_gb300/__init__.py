@@ -55,6 +55,12 @@ class BatchInfo(C.Structure):
                 ("graph_kernels", C.c_int32), ("device_bytes", C.c_int64)]
 
 
+class FluxOptions(C.Structure):
+    _fields_ = [("param_a", C.c_int32), ("param_b", C.c_int32), ("rows", C.c_int32), ("cols", C.c_int32),
+                ("a0", C.c_double), ("da", C.c_double), ("b0", C.c_double), ("db", C.c_double),
+                ("periodic", C.c_int32), ("precision", C.c_int), ("device", C.c_int32)]
+
+
 class PrecondConfig(C.Structure):
     _fields_ = [("num_params", C.c_int32), ("width", C.c_int32), ("rank", C.c_int32), ("lam", C.c_double),
                 ("u_scale", C.c_double), ("seed", C.c_uint64), ("device", C.c_int32)]
@@ -109,6 +115,8 @@ def lib() -> C.CDLL:
         L.qgt_batch_execute_host.argtypes = [vp, vp, vp, vp]
         L.qgt_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
         L.qgt_batch_destroy.argtypes = [vp]
+        L.qgt_flux_default_options.argtypes = [C.POINTER(FluxOptions)]
+        L.qgt_berry_flux_grid.argtypes = [C.POINTER(CircuitDesc), vp, C.POINTER(FluxOptions), vp, vp]
         L.qgt_precond_default_config.argtypes = [C.POINTER(PrecondConfig)]
         L.qgt_precond_default_train_options.argtypes = [C.POINTER(PrecondTrainOptions)]
         L.qgt_precond_create.argtypes = [C.POINTER(PrecondConfig), C.POINTER(vp)]
@@ -473,3 +481,41 @@ def qgt_from_states(psi, D, precision=FP64):
     Q = np.zeros((P, P), dtype=np.complex128)
     _check(L.qgt_qgt_from_states(_ptr(psi), _ptr(D), psi.shape[0], P, precision, _ptr(Q)), "qgt_qgt_from_states")
     return Q
+
+
+def berry_flux(n, gates, theta, pa, pb, rows, cols, a0, da, b0, db, periodic=True, precision=MIXED, device=0):
+    """Plaquette (Wilson-loop) Berry flux over a rows x cols lattice of circuit
+    states on the GPU (qgt_berry_flux_grid) -> (flux rows x cols, sum)."""
+    L = lib()
+    th = np.ascontiguousarray(theta, dtype=np.float64)
+    d = circuit_desc(n, gates, th.shape[0])
+    o = FluxOptions()
+    L.qgt_flux_default_options(C.byref(o))
+    o.param_a, o.param_b, o.rows, o.cols = pa, pb, rows, cols
+    o.a0, o.da, o.b0, o.db = a0, da, b0, db
+    o.periodic, o.precision, o.device = int(bool(periodic)), precision, device
+    F = np.zeros((rows, cols))
+    tot = np.zeros(1)
+    _check(L.qgt_berry_flux_grid(C.byref(d), _ptr(th), C.byref(o), _ptr(F), _ptr(tot)), "qgt_berry_flux_grid")
+    return F, float(tot[0])
+
+
+class _ComplexDouble(C.Structure):
+    _fields_ = [("real", C.c_double), ("imag", C.c_double)]
+
+
+def berry_phase(states):
+    """diffgeo_compute_berry_phase on the GPU: prod_i <psi_i|psi_{i+1 mod n}> / |.| as a complex number."""
+    L = lib()
+    L.diffgeo_engine_create.restype = C.c_void_p
+    L.diffgeo_engine_destroy.argtypes = [C.c_void_p]
+    L.diffgeo_compute_berry_phase.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t]
+    L.diffgeo_compute_berry_phase.restype = _ComplexDouble
+    st = [np.ascontiguousarray(x, dtype=np.complex128) for x in states]
+    ptrs = (C.c_void_p * max(len(st), 1))(*[x.ctypes.data for x in st])
+    e = L.diffgeo_engine_create()
+    try:
+        r = L.diffgeo_compute_berry_phase(e, C.cast(ptrs, C.c_void_p), len(st), st[0].shape[0] if st else 0)
+    finally:
+        L.diffgeo_engine_destroy(e)
+    return complex(r.real, r.imag)

@@ -215,3 +215,53 @@ extern "C" int qgt_dev_gram_small(const void* V, int64_t N, int32_t rows, int32_
     gram_small_reduce_kernel<<<npoints, 64, 0, s>>>((const double2*)part, rows, nsplit, (double2*)HG);
     return qgt_dev_last_error();
 }
+
+// ---------------------------------------------------------------------------
+// Overlaps <V + a_off[k] | V + b_off[k]> of rows of N amplitudes (offsets in
+// amplitudes), FP64 sums: Berry phases around loops and plaquette links on
+// parameter lattices.  Pair k is split over nchunk CTAs (block k * nchunk + c
+// sums the amplitudes [c len, (c + 1) len)); part[k * nchunk + c] receives
+// the partial sums, which the caller adds in a fixed order.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) overlap_kernel(const T* __restrict__ V, int64_t N, int64_t len,
+                                                      int32_t nchunk, const int64_t* __restrict__ a_off,
+                                                      const int64_t* __restrict__ b_off, double2* __restrict__ part)
+{
+    __shared__ double2 red[8];
+    const int64_t k = blockIdx.x / nchunk, c = blockIdx.x % nchunk;
+    const T* a = V + a_off[k];
+    const T* b = V + b_off[k];
+    const int64_t lo = c * len, hi = lo + len < N ? lo + len : N;
+    double re = 0, im = 0;
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const T x = a[i], y = b[i];
+        re += (double)x.x * y.x + (double)x.y * y.y;
+        im += (double)x.x * y.y - (double)x.y * y.x;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, o);
+        im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = make_double2(re, im);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double2 t = make_double2(0, 0);
+        for (int w = 0; w < 8; w++) { t.x += red[w].x; t.y += red[w].y; }
+        part[blockIdx.x] = t;
+    }
+}
+
+extern "C" int qgt_dev_overlaps(const void* V, int32_t fp64, int64_t N, const int64_t* a_off, const int64_t* b_off,
+                                int32_t n, int32_t nchunk, double* part, void* stream)
+{
+    if (n <= 0) return 0;
+    if (N <= 0 || nchunk <= 0 || (int64_t)n * nchunk > 0x7fffffff)
+        return qgt_set_error(-1, "overlaps: %d pairs x %d chunks outside the grid", n, nchunk);
+    const int64_t len = (N + nchunk - 1) / nchunk;
+    cudaStream_t s = (cudaStream_t)stream;
+    const unsigned grid = (unsigned)((int64_t)n * nchunk);
+    if (fp64) overlap_kernel<double2><<<grid, 256, 0, s>>>((const double2*)V, N, len, nchunk, a_off, b_off, (double2*)part);
+    else overlap_kernel<float2><<<grid, 256, 0, s>>>((const float2*)V, N, len, nchunk, a_off, b_off, (double2*)part);
+    return qgt_dev_last_error();
+}

@@ -1728,6 +1728,12 @@ int qgt_plan_enqueue_step(qgt_plan_t* p, void* stream)
 double* qgt_plan_dev_theta(qgt_plan_t* p) { return p->theta_d; }
 double* qgt_plan_dev_Q(qgt_plan_t* p) { return p->Q_d; }
 int qgt_plan_launches(const qgt_plan_t* p) { return p->launches; }
+const void* qgt_plan_dev_V(qgt_plan_t* p, int64_t* point_stride, int32_t* fp64)
+{
+    if (point_stride) *point_stride = p->pstride;
+    if (fp64) *fp64 = p->fp64;
+    return p->V;
+}
 double* qgt_plan_dev_grad(qgt_plan_t* p) { return p->grad_d; }
 double* qgt_plan_dev_energy(qgt_plan_t* p) { return p->energy_d; }
 double* qgt_plan_dev_natgrad(qgt_plan_t* p) { return p->natgrad_d; }

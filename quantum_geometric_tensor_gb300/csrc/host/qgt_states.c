@@ -134,7 +134,7 @@ int qgt_qgt_from_states(const double* psi, const double* D, int64_t dim, int32_t
 
 struct diffgeo_engine {
     int precision;
-    size_t metric_evaluations, curvature_evaluations;
+    size_t metric_evaluations, curvature_evaluations, berry_phase_evaluations;
 };
 
 diffgeo_engine_t* diffgeo_engine_create(void)
@@ -181,4 +181,72 @@ bool diffgeo_compute_berry_curvature(diffgeo_engine_t* e, const ComplexDouble* s
     free(Q);
     e->curvature_evaluations++;
     return true;
+}
+
+/* Berry phase of a closed loop of states (reference:
+ * src/quantum_geometric/distributed/differential_geometry.c:2908-2945): the
+ * product over i of <psi_i|psi_{i+1 mod n}> / |<psi_i|psi_{i+1 mod n}>|,
+ * multiplied in loop order.  The n overlaps run as one GPU kernel over the
+ * states copied to HBM; {0, 0} when a link magnitude is <= 1e-14 (orthogonal
+ * neighbours, phase undefined) or the GPU fails (the last error says which). */
+ComplexDouble diffgeo_compute_berry_phase(diffgeo_engine_t* e, const ComplexDouble** states, size_t num_states,
+                                          size_t dim)
+{
+    ComplexDouble res = {1.0, 0.0};
+    if (!e || !states || num_states < 2 || dim == 0) return res;
+    const ComplexDouble zero = {0.0, 0.0};
+    for (size_t i = 0; i < num_states; i++)
+        if (!states[i]) { qgt_set_error(E_INVAL, "diffgeo_compute_berry_phase: state %zu is NULL", i); return zero; }
+    if (num_states > 0x7fffffff || dim > ((size_t)1 << 40)) {
+        qgt_set_error(E_INVAL, "diffgeo_compute_berry_phase: %zu states of %zu amplitudes too large", num_states, dim);
+        return zero;
+    }
+    const int32_t n = (int32_t)num_states;
+    const int32_t nch = qgt_overlap_chunks((int64_t)dim, n);
+    void* s = NULL;
+    double *X = NULL, *part = NULL;
+    int64_t* off_d = NULL;
+    int64_t* off = (int64_t*)malloc(sizeof(int64_t) * 2 * (size_t)n);
+    double* part_h = (double*)malloc(sizeof(double) * 2 * (size_t)n * (size_t)nch);
+    int rc = (!off || !part_h) ? qgt_set_error(E_NOMEM, "diffgeo_compute_berry_phase: out of memory") : 0;
+    for (int32_t i = 0; !rc && i < n; i++) {
+        off[i] = (int64_t)i * (int64_t)dim;
+        off[n + i] = (int64_t)((i + 1) % n) * (int64_t)dim;
+    }
+    if (!rc) rc = qgt_dev_stream_create(&s);
+    if (!rc) rc = qgt_dev_malloc((void**)&X, sizeof(ComplexDouble) * dim * num_states);
+    for (size_t i = 0; !rc && i < num_states; i++)
+        rc = qgt_dev_memcpy_h2d(X + 2 * dim * i, states[i], sizeof(ComplexDouble) * dim, s);
+    if (!rc) rc = qgt_dev_malloc((void**)&off_d, sizeof(int64_t) * 2 * (size_t)n);
+    if (!rc) rc = qgt_dev_malloc((void**)&part, sizeof(double) * 2 * (size_t)n * (size_t)nch);
+    if (!rc) rc = qgt_dev_memcpy_h2d(off_d, off, sizeof(int64_t) * 2 * (size_t)n, s);
+    if (!rc) rc = qgt_dev_overlaps(X, 1, (int64_t)dim, off_d, off_d + n, n, nch, part, s);
+    if (!rc) rc = qgt_dev_memcpy_d2h(part_h, part, sizeof(double) * 2 * (size_t)n * (size_t)nch, s);
+    if (!rc) rc = qgt_dev_stream_sync(s);
+    for (int32_t i = 0; !rc && i < n; i++) {
+        double re = 0, im = 0;
+        for (int32_t q = 0; q < nch; q++) {
+            re += part_h[2 * ((size_t)i * nch + q)];
+            im += part_h[2 * ((size_t)i * nch + q) + 1];
+        }
+        const double mag = sqrt(re * re + im * im);
+        if (!(mag > 1e-14)) {
+            rc = qgt_set_error(E_INVAL, "diffgeo_compute_berry_phase: states %d and %d are orthogonal", i, (i + 1) % n);
+            break;
+        }
+        re /= mag;
+        im /= mag;
+        const double r = res.real * re - res.imag * im;
+        res.imag = res.real * im + res.imag * re;
+        res.real = r;
+    }
+    qgt_dev_free(X);
+    qgt_dev_free(part);
+    qgt_dev_free(off_d);
+    if (s) qgt_dev_stream_destroy(s);
+    free(off);
+    free(part_h);
+    if (rc) return zero;
+    e->berry_phase_evaluations++;
+    return res;
 }

@@ -303,6 +303,15 @@ int qgt_dev_cholesky_batch(const double* A, int complex_input, const double* b, 
 int qgt_dev_gram_small(const void* V, int64_t N, int32_t rows, int32_t fp64, double* part, int32_t nsplit,
                        double* HG, int32_t npoints, int64_t point_stride, void* stream);
 
+/* <V + a_off[k] | V + b_off[k]> over N amplitudes (offsets in amplitudes), pair k split in nchunk
+ * ranges: part[k * nchunk + c] (complex double) holds the sum over range c */
+int qgt_dev_overlaps(const void* V, int32_t fp64, int64_t N, const int64_t* a_off, const int64_t* b_off, int32_t n,
+                     int32_t nchunk, double* part, void* stream);
+/* chunks per pair that fill the GPU for n pairs of N amplitudes */
+int32_t qgt_overlap_chunks(int64_t N, int32_t n);
+/* the device vector buffer of a plan and the amplitudes between its points */
+const void* qgt_plan_dev_V(struct qgt_plan* p, int64_t* point_stride, int32_t* fp64);
+
 /* ---- learned preconditioner and PCG (qgt_learned.cu) ---- */
 /* X = [cos theta, sin theta] of theta rows idx[0..S) (idx NULL: rows 0..S) */
 int qgt_dev_lr_features(const double* theta, const int32_t* idx, int32_t S, int32_t P, float* X, void* stream);

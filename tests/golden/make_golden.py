@@ -14,9 +14,18 @@ reference tree (oracle/_ref/libqgt_ref.so, built by oracle/Makefile):
              hybrid/classical_optimization_engine.c:543-611
   qfim_inv   invert_qfim_regularized (float)  learning/quantum_pipeline_impl.c:1601-1682
 
+The Berry-phase fixtures (berry/*.npz) hold states of the same simulator on a
+two-parameter lattice and, from diffgeo_compute_berry_phase
+(distributed/differential_geometry.c:2908-2945):
+  flux       arg of the loop phase of each plaquette p00 -> p10 -> p11 -> p01
+             (the Wilson loop of cuda/quantum_phase_cuda.cu:245-313 with
+             full-state links), the lattice wrapping at its edges
+  loop_phase the loop phase of the lattice's first row of sites
+
 Only the circuits and seeded angles are chosen here.  Run from the repository
 root in a container that has the reference tree:
-    make -C oracle && python tests/golden/make_golden.py
+    make -C oracle && python tests/golden/make_golden.py          (all fixtures)
+  make -C oracle && python tests/golden/make_golden.py berry    (Berry-phase fixtures only)
 """
 import math
 import os
@@ -66,7 +75,45 @@ def cases():
     return out
 
 
+def berry_cases():
+    """(name, n, gates, theta, pa, pb, rows, cols, a0, da, b0, db)"""
+    g4 = O.ansatz(4, 2, "cz")
+    g5 = O.ansatz(5, 2, "cnot")
+    return [
+        ("berry_cz_n4_l2_s5", 4, g4, O.splitmix64_params(5, O.num_params(g4)), 0, 4, 8, 8,
+         0.0, 2 * math.pi / 8, 0.0, 2 * math.pi / 8),
+        ("berry_cnot_n5_l2_s6", 5, g5, O.splitmix64_params(6, O.num_params(g5)), 1, 7, 6, 5,
+         0.3, 0.4, -0.2, 0.55),
+    ]
+
+
+def berry_main():
+    ref = O.Reference()
+    for name, n, gates, theta, pa, pb, rows, cols, a0, da, b0, db in berry_cases():
+        S = {}
+        for i in range(rows):
+            for j in range(cols):
+                t = np.array(theta, dtype=np.float64)
+                t[pa], t[pb] = a0 + i * da, b0 + j * db
+                S[i, j] = ref.simulate(n, gates, t)
+        flux = np.zeros((rows, cols))
+        for i in range(rows):
+            for j in range(cols):
+                i1, j1 = (i + 1) % rows, (j + 1) % cols
+                flux[i, j] = np.angle(ref.berry_phase([S[i, j], S[i1, j], S[i1, j1], S[i, j1]]))
+        loop = ref.berry_phase([S[0, j] for j in range(cols)])
+        path = os.path.join(ROOT, "tests", "golden", "berry", f"{name}.npz")
+        np.savez_compressed(path, n=n, gates=gates, theta=theta, pa=pa, pb=pb, rows=rows, cols=cols,
+                            a0=a0, da=da, b0=b0, db=db, flux=flux, loop_phase=loop,
+                            row0_states=np.stack([S[0, j] for j in range(cols)]))
+        print(f"{name}: {rows}x{cols} sum flux / 2 pi = {flux.sum() / (2 * math.pi):.3e} -> {os.path.relpath(path, ROOT)}")
+
+
 def main():
+    if sys.argv[1:] == ["berry"]:
+        berry_main()
+        return
+    berry_main()
     ref = O.Reference()
     for name, n, gates, theta in cases():
         psi = ref.simulate(n, gates, theta)

@@ -10,6 +10,7 @@ import pytest
 from oracle import oracle as O
 
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+BERRY = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "berry", "*.npz")))
 
 
 def rel(a, b):
@@ -131,3 +132,52 @@ def test_pauli_apply_matches_reference_expectation(orc):
     # the TFIM ring as Pauli strings equals the dedicated TFIM apply
     tf = [(c, s) for c, s in O.tfim_pauli_strings(n)]
     assert np.abs(orc.pauli_apply(n, psi, tf) - orc.tfim_apply(n, psi)).max() < 1e-13
+
+
+@pytest.mark.parametrize("path", BERRY, ids=[os.path.basename(p)[:-4] for p in BERRY])
+def test_berry_flux_and_loop_phase_match_reference(orc, path):
+    """Plaquette fluxes and the loop phase of the restated oracle against the
+    reference's diffgeo_compute_berry_phase on the reference simulator's states."""
+    z = np.load(path)
+    n, gates, theta = int(z["n"]), z["gates"], z["theta"]
+    rows, cols = int(z["rows"]), int(z["cols"])
+    args = (int(z["pa"]), int(z["pb"]), rows, cols, float(z["a0"]), float(z["da"]), float(z["b0"]), float(z["db"]))
+    F = orc.berry_flux(n, gates, theta, *args, periodic=True)
+    assert np.abs(F - z["flux"]).max() < 1e-12
+    # fluxes of a wrapped lattice sum to 2 pi x an integer (each link is met twice)
+    c = F.sum() / (2 * math.pi)
+    assert abs(c - round(c)) < 1e-10
+    Fo = orc.berry_flux(n, gates, theta, *args, periodic=False)
+    assert np.array_equal(Fo[:-1, :-1], F[:-1, :-1])
+    assert not Fo[-1].any() and not Fo[:, -1].any()
+    w = orc.berry_phase(list(z["row0_states"]))
+    assert abs(w - complex(z["loop_phase"])) < 1e-12 and abs(abs(w) - 1) < 1e-12
+
+
+def test_berry_phase_edge_cases(orc):
+    a = np.zeros(4, complex)
+    a[0] = 1
+    b = np.zeros(4, complex)
+    b[1] = 1
+    assert orc.berry_phase([a, b]) == 0                 # orthogonal neighbours: undefined
+    assert orc.berry_phase([a]) == 1                    # fewer than two states
+    # invariant under a phase of any one state; conjugating the loop reverses the phase
+    rng = np.random.default_rng(3)
+    st = [rng.standard_normal(16) + 1j * rng.standard_normal(16) for _ in range(6)]
+    w = orc.berry_phase(st)
+    st2 = list(st)
+    st2[2] = st2[2] * np.exp(0.7j)
+    assert abs(orc.berry_phase(st2) - w) < 1e-13
+    assert abs(orc.berry_phase(st[::-1]) - np.conj(w)) < 1e-13
+
+
+def test_small_plaquette_flux_is_twice_curvature(orc):
+    """flux / (da db) -> 2 Im Q_ab at the plaquette centre as the spacing shrinks."""
+    n = 4
+    g = O.ansatz(n, 2, "cz")
+    th = O.splitmix64_params(8, O.num_params(g))
+    pa, pb, h = 0, n, 1e-3
+    F = orc.berry_flux(n, g, th, pa, pb, 2, 2, th[pa] - h / 2, h, th[pb] - h / 2, h, periodic=False)
+    psi, D = orc.derivatives(n, g, th)
+    Q = orc.qgt_from_states(psi, D)
+    assert abs(F[0, 0] / h ** 2 - 2 * Q[pa, pb].imag) < 1e-5
