@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
         for (int i = threadIdx.x; i < a.nops; i += blockDim.x) sops[i] = a.ops[i];
         for (int i = threadIdx.x; i < 8 * a.nops; i += blockDim.x) {
             const int c = a.ops[i >> 3].coef;
-            scoef[i] = c >= 0 ? ctab[8 * c + (i & 7)] : (R)0;
+            scoef[i] = c >= 0 ? ctab[8 * c + (i & 7)] : (((i & 7) == 0 || (i & 7) == 6) ? (R)1 : (R)0);   // identity
         }
         __syncthreads();
     }
@@ -292,68 +292,34 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
         }
         if (op.kind == Q2_DIAG) {
             // combined phase of the run: c (thread factor) x prod_i f_i(reg bit i) x sign(static mask)
-            const int cnt = op.seg;
+            const int cnt = op.seg, nt = op.ra, nz = op.rb;
+            const int r0 = pc + 1, t0 = r0 + RB, z0 = t0 + nt;
             R cr = (R)1, ci = (R)0;
+            for (int u = t0; u < z0; u++) {
+                const qgt_dev_op2_t so = sops[u];
+                const R* c8 = scoef + 8 * u;
+                const int bit = role_bit(so.ra, so.q, lane, warp, base);
+                const R pr = bit ? c8[6] : c8[0], pi = bit ? c8[7] : c8[1];
+                const R t = cr * pr - ci * pi;
+                ci = cr * pi + ci * pr;
+                cr = t;
+            }
+            uint32_t par = 0;
+            for (int u = z0; u < z0 + nz; u++) {
+                const qgt_dev_op2_t so = sops[u];
+                par ^= (pthr >> so.q) & (uint32_t)__popc(pthr & (uint32_t)so.slot);
+            }
+            if (par & 1u) { cr = -cr; ci = -ci; }
+            // register-bit factors (|0>, |1>), the |1> factor negated by an odd CZ parity with the thread bits
             R f0r[RB], f0i[RB], f1r[RB], f1i[RB];
 #pragma unroll
-            for (int i = 0; i < RB; i++) { f0r[i] = (R)1; f0i[i] = (R)0; f1r[i] = (R)1; f1i[i] = (R)0; }
-            for (int u = 1; u <= cnt; u++) {
-                const qgt_dev_op2_t so = sops[pc + u];
-                const bool ra_reg = so.ra >= RL_REG && so.ra < RL_WARP;
-                if (so.kind == Q2_PHASE) {
-                    const R* c8 = scoef + 8 * (pc + u);
-                    const R p0r = c8[0], p0i = c8[1], p1r = c8[6], p1i = c8[7];
-                    if (ra_reg) {
-                        const int ri = so.ra - RL_REG;
-#pragma unroll
-                        for (int i = 0; i < RB; i++)
-                            if (i == ri) {
-                                R t = f0r[i] * p0r - f0i[i] * p0i;
-                                f0i[i] = f0r[i] * p0i + f0i[i] * p0r;
-                                f0r[i] = t;
-                                t = f1r[i] * p1r - f1i[i] * p1i;
-                                f1i[i] = f1r[i] * p1i + f1i[i] * p1r;
-                                f1r[i] = t;
-                            }
-                    } else {
-                        const int bit = role_bit(so.ra, so.q, lane, warp, base);
-                        const R pr = bit ? p1r : p0r, pi = bit ? p1i : p0i;
-                        const R t = cr * pr - ci * pi;
-                        ci = cr * pi + ci * pr;
-                        cr = t;
-                    }
-                } else if (so.kind == Q2_CZM) {
-                    // register bit ra against the thread qubits in slot: sign of its |1> factor
-                    if (__popc(pthr & (uint32_t)so.slot) & 1) {
-                        const int ri = so.ra - RL_REG;
-#pragma unroll
-                        for (int i = 0; i < RB; i++)
-                            if (i == ri) { f1r[i] = -f1r[i]; f1i[i] = -f1i[i]; }
-                    }
-                } else if (so.kind == Q2_CZT) {
-                    // thread qubit q against the thread qubits in slot
-                    if (((pthr >> so.q) & 1u) && (__popc(pthr & (uint32_t)so.slot) & 1)) {
-                        cr = -cr;
-                        ci = -ci;
-                    }
-                } else if (so.kind == Q2_ZGEN) {
-                    // marker of a derivative spawned in the run (applied after it)
-                } else {  // Q2_CZ
-                    const bool rb_reg = so.rb >= RL_REG && so.rb < RL_WARP;
-                    if (ra_reg && rb_reg) continue;  // in the static mask
-                    if (ra_reg || rb_reg) {
-                        const int ri = (ra_reg ? so.ra : so.rb) - RL_REG;
-                        const int tb = ra_reg ? role_bit(so.rb, so.q2, lane, warp, base) : role_bit(so.ra, so.q, lane, warp, base);
-                        if (tb) {
-#pragma unroll
-                            for (int i = 0; i < RB; i++)
-                                if (i == ri) { f1r[i] = -f1r[i]; f1i[i] = -f1i[i]; }
-                        }
-                    } else if (role_bit(so.ra, so.q, lane, warp, base) & role_bit(so.rb, so.q2, lane, warp, base)) {
-                        cr = -cr;
-                        ci = -ci;
-                    }
-                }
+            for (int i = 0; i < RB; i++) {
+                const R* c8 = scoef + 8 * (r0 + i);
+                const R sg = (__popc(pthr & (uint32_t)sops[r0 + i].slot) & 1) ? (R)-1 : (R)1;
+                f0r[i] = c8[0];
+                f0i[i] = c8[1];
+                f1r[i] = sg * c8[6];
+                f1i[i] = sg * c8[7];
             }
             // tables over register bits 0..2 (with c) and 3..RB-1, then one product per amplitude
             constexpr int LB = 3, HB = RB - 3;

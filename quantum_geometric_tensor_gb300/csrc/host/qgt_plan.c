@@ -836,15 +836,21 @@ static int comb_entry(qgt_plan_t* p, const int* list, int n)
     return p->ncoef + p->ncomb++;
 }
 
-/* One run of diagonal ops src[j, e) as a compact Q2_DIAG block: one phase
- * factor per register bit and per thread qubit (products of the run's
- * coefficients, formed once per step by the combine kernel), the CZs as
- * parity masks (register-register pairs in the header's static sign mask,
- * register-thread pairs per register bit, thread-thread pairs per qubit),
- * and a Q2_ZGEN marker for each derivative spawned inside the run. */
+/* One run of diagonal ops src[j, e) as a compact Q2_DIAG block (products of
+ * the run's coefficients are formed once per step by the combine kernel):
+ *   header   seg = sub-ops that follow, ra = thread phase entries, rb = CZT
+ *            entries, slot = static sign mask over the register index
+ *            (register-register CZs)
+ *   RB register entries, bit i = 0 .. RB-1 in order: the bit's combined
+ *            phase (coef -1: none) and in slot the physical qubits outside
+ *            the register bits that share a CZ with it
+ *   ra thread phase entries (lane, warp or outside qubit q)
+ *   rb Q2_CZT entries: thread qubit q against the thread qubits in slot
+ *   Q2_ZGEN markers, one per derivative spawned inside the run. */
 static int emit_diag_run(qgt_plan_t* p, const qgt_dev_op2_t* src, int j, int e, qgt_dev_op2_t* out_ops, int* out,
                          int nb, int* remap)
 {
+    const int RB = p->fp64 ? 4 : 5;
     int lists[40][64];
     int nl[40];
     int8_t role[40];
@@ -876,38 +882,40 @@ static int emit_diag_run(qgt_plan_t* p, const qgt_dev_op2_t* src, int j, int e, 
             }
         }
     }
-    int cnt = 0;
-    for (int k = 0; k < 40; k++) cnt += nl[k] > 0;
-    for (int i = 0; i < 8; i++) cnt += czm[i] != 0;
-    for (int a = 0; a < 32; a++) cnt += czt[a] != 0;
-    for (int t = j; t < e; t++) cnt += src[t].slot >= 0;
+    int nt = 0, nz = 0, ng = 0;
+    for (int k = 8; k < 40; k++) nt += nl[k] > 0;
+    for (int a = 0; a < 32; a++) nz += czt[a] != 0;
+    for (int t = j; t < e; t++) ng += src[t].slot >= 0;
+    if (nt > 255 || nz > 255) return qgt_set_error(E_STATE, "programs: diagonal run too wide");
     qgt_dev_op2_t h;
     memset(&h, 0, sizeof h);
     h.kind = Q2_DIAG;
-    h.seg = (int16_t)cnt;
+    h.seg = (int16_t)(RB + nt + nz + ng);
+    h.ra = (uint8_t)nt;
+    h.rb = (uint8_t)nz;
     h.coef = -1;
     h.slot = (int32_t)regmask;
     out_ops[(*out)++] = h;
-    for (int k = 0; k < 40; k++) {
+    for (int i = 0; i < RB; i++) {
+        qgt_dev_op2_t x;
+        memset(&x, 0, sizeof x);
+        x.kind = Q2_PHASE;
+        x.ra = (uint8_t)(RL_REG_ + i);
+        x.slot = (int32_t)czm[i];
+        x.coef = nl[i] ? comb_entry(p, lists[i], nl[i]) : -1;
+        if (nl[i] && x.coef < 0) return qgt_set_error(E_NOMEM, "programs: oom");
+        out_ops[(*out)++] = x;
+    }
+    for (int k = 8; k < 40; k++) {
         if (!nl[k]) continue;
         qgt_dev_op2_t x;
         memset(&x, 0, sizeof x);
         x.kind = Q2_PHASE;
         x.ra = (uint8_t)role[k];
-        x.q = (int8_t)(k >= 8 ? k - 8 : 0);
+        x.q = (int8_t)(k - 8);
         x.slot = -1;
         x.coef = comb_entry(p, lists[k], nl[k]);
         if (x.coef < 0) return qgt_set_error(E_NOMEM, "programs: oom");
-        out_ops[(*out)++] = x;
-    }
-    for (int i = 0; i < 8; i++) {
-        if (!czm[i]) continue;
-        qgt_dev_op2_t x;
-        memset(&x, 0, sizeof x);
-        x.kind = Q2_CZM;
-        x.ra = (uint8_t)(RL_REG_ + i);
-        x.coef = -1;
-        x.slot = (int32_t)czm[i];
         out_ops[(*out)++] = x;
     }
     for (int a = 0; a < 32; a++) {
@@ -937,7 +945,7 @@ static int fold_diagonal_runs(qgt_plan_t* p)
 {
     if (p->nprog == 0) return 0;
     int rc = 0;
-    const int cap = p->nprog + p->nprog / 2 + 16;
+    const int cap = 5 * p->nprog + 16;   /* a run of m ops emits at most 1 + RB + 2 m entries */
     qgt_dev_op2_t* np2 = (qgt_dev_op2_t*)calloc((size_t)cap, sizeof(qgt_dev_op2_t));
     int* remap = (int*)malloc(sizeof(int) * ((size_t)p->nprog + 1));
     if (!np2 || !remap) { free(np2); free(remap); return qgt_set_error(E_NOMEM, "programs: oom"); }
@@ -950,7 +958,7 @@ static int fold_diagonal_runs(qgt_plan_t* p)
         for (int j = 0; j < n;) {
             int e = j;
             while (e < n && (src[e].kind == Q2_PHASE || src[e].kind == Q2_CZ)) e++;
-            if (e - j >= 2 && out + (e - j) + 1 < cap) {
+            if (e - j >= 2 && out + 2 * (e - j) + 8 < cap) {
                 if ((rc = emit_diag_run(p, src, j, e, np2, &out, nb, remap)) != 0) { free(np2); free(remap); return rc; }
                 j = e;
             } else {
@@ -1785,6 +1793,11 @@ int qgt_plan_schedule_dump(const void* circuit, const void* options, const char*
             const qgt_dev_op_t* o = &p->ops_h[ps->op_begin + j];
             fprintf(f, "%s[%d, %d, %d, %d, %d, %d]", j ? ", " : "", (int)o->pad, (int)o->q, (int)o->q2, o->coef, o->slot,
                     (int)o->kind);
+        }
+        fprintf(f, "], \"prog\": [");
+        for (int j = 0; j < ps->prog_count; j++) {
+            const qgt_dev_op2_t* o = &p->prog_h[ps->prog_begin + j];
+            fprintf(f, "%s[%d, %d, %d, %d, %d]", j ? ", " : "", (int)o->kind, (int)o->ra, (int)o->rb, (int)o->seg, o->slot);
         }
         fprintf(f, "], \"entries\": [");
         for (int e = 0; e < ps->ent_count; e++) {

@@ -111,13 +111,15 @@ typedef struct {
  * role-encoded: 0..4 lane bit, 8 + i register bit i, 16 + w warp bit w,
  * 32 outside the tile (physical qubit in q / q2). */
 enum { Q2_SEG = 1, Q2_U = 2, Q2_UR = 3, Q2_PHASE = 4, Q2_CZ = 5, Q2_CNOT = 6, Q2_DIAG = 7,
-       Q2_CZM = 8,    /* in a diagonal run: register bit ra's |1> factor flips sign when popc(thread bits & slot) is odd */
        Q2_CZT = 9,    /* in a diagonal run: the thread factor flips when thread bit q and popc(thread bits & slot) are odd */
        Q2_ZGEN = 10 };/* in a diagonal run: marks a derivative spawned by the rotation on (ra, q) */
-/* Q2_DIAG: header of a run of `seg` diagonal ops (Q2_PHASE / Q2_CZ) that
- * follow it; the run is applied as one per-thread phase table.  `slot` holds
- * the sign mask over the register index of the run's CZs between two register
- * bits (those CZ ops stay in the run and are skipped). */
+/* Q2_DIAG: header of a run of diagonal gates applied as one per-thread phase
+ * table; `seg` sub-ops follow: RB register-bit entries (Q2_PHASE on register
+ * bit i = 0 .. RB-1 in order, coef -1 = no phase, slot = the physical qubits
+ * outside the register bits that share a CZ with bit i), then `ra` thread
+ * phase entries (Q2_PHASE on a lane, warp or outside qubit), then `rb` Q2_CZT
+ * entries, then Q2_ZGEN markers.  The header's `slot` is the sign mask over
+ * the register index of the run's CZs between two register bits. */
 typedef struct {
     uint8_t kind;
     uint8_t ra;     /* target / first bit (role-encoded) */
