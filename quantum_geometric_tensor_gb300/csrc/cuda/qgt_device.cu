@@ -621,10 +621,12 @@ int qgt_dev_event_elapsed(void* a, void* b, float* ms)
 // Every per-vector scale a gate applies is harmless (each vector of a step
 // carries the product of all gates' scales and Q = B/s - v v^H / s^2 is
 // invariant under it); only the rotation ANGLE of a rounded FP32 matrix is
-// an error, and it is coherent across all vectors.  For RX/RY/RZ the warp
+// an error, and it is coherent across all vectors.  For RX/RZ the warp
 // searches 512 radii r in [1 - 2^-15, 1 + 2^-15] for the FP32 pair
 // (fl(r cos a/2), fl(r sin a/2)) closest to the exact ray: angle error
-// ~1e-10 instead of ~6e-8.  Diagonal fixed gates get equal-modulus entries.
+// ~1e-10 instead of ~6e-8.  RY takes the tangent form below (angle error at
+// most 3e-8 rad, from rounding t).  Diagonal fixed gates get equal-modulus
+// entries.
 // One warp per coefficient; 8 floats per coefficient (2x2 complex, row-major).
 // ---------------------------------------------------------------------------
 __global__ void prepare32_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const double* theta, float* coef,
@@ -639,7 +641,26 @@ __global__ void prepare32_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const 
     const int inv = (g.type & QGT_COEF_INVERSE) != 0;   // the gate's inverse (backward transport)
     g.type &= ~QGT_COEF_INVERSE;
     float m[8] = {1.f, 0.f, 0.f, 0.f, 0.f, 0.f, 1.f, 0.f};
-    if (g.type == QGT_GATE_RX || g.type == QGT_GATE_RY || g.type == QGT_GATE_RZ) {
+    if (g.type == QGT_GATE_RY) {
+        // tangent form: RY = c [[1, -t], [t, 1]] (t = s / c, |t| <= 1) or
+        // |s| [[k, -g], [g, k]] (k = c / |s|, g = sign s); the pass kernels
+        // apply these scaled rotations with one multiply-add per component,
+        // and the scale (the column norm) is divided out by the pass
+        // renormalisation.  Both scales (c and |s|) are even in the angle, so
+        // a gate and its inverse (backward transport) carry the same sign and
+        // a vector that crosses both keeps its sign.
+        double a = g.param >= 0 ? theta[g.param] : g.angle;
+        if (inv) a = -a;
+        double s0, c0;
+        sincos(0.5 * a, &s0, &c0);
+        if (fabs(c0) >= fabs(s0)) {
+            const float t = (float)(s0 / c0);
+            m[0] = 1.f; m[2] = -t; m[4] = t; m[6] = 1.f;
+        } else {
+            const float k = (float)(c0 / fabs(s0)), g = s0 > 0 ? 1.f : -1.f;
+            m[0] = k; m[2] = -g; m[4] = g; m[6] = k;
+        }
+    } else if (g.type == QGT_GATE_RX || g.type == QGT_GATE_RZ) {
         double a = g.param >= 0 ? theta[g.param] : g.angle;
         if (inv) a = -a;
         double s0, c0;
@@ -659,7 +680,6 @@ __global__ void prepare32_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const 
             if (ob < best || (ob == best && oc < bc)) { best = ob; bc = oc; bs = os; }
         }
         if (g.type == QGT_GATE_RX) { m[0] = bc; m[1] = 0; m[2] = 0; m[3] = -bs; m[4] = 0; m[5] = -bs; m[6] = bc; m[7] = 0; }
-        else if (g.type == QGT_GATE_RY) { m[0] = bc; m[1] = 0; m[2] = -bs; m[3] = 0; m[4] = bs; m[5] = 0; m[6] = bc; m[7] = 0; }
         else { m[0] = bc; m[1] = -bs; m[2] = 0; m[3] = 0; m[4] = 0; m[5] = 0; m[6] = bc; m[7] = bs; }
     } else {
         const float r = 0.70710678118654752440f;
@@ -674,6 +694,42 @@ __global__ void prepare32_kernel(const qgt_dev_coef_desc_t* d, int ncoef, const 
         }
     }
     if (lane < 8) coef[8 * c + lane] = m[lane];
+}
+
+// Pass renormalisation: for each pass (blockIdx.x) of each point
+// (blockIdx.y), G = prod over the pass's coefficient entries of their scales
+// |column 0| (FP64), and the pass's designated entry (its last single-qubit
+// gate, ren[pass] >= 0) is multiplied by 1 / G, so that every vector leaves
+// the pass with the norm it entered with.  Every vector of a pass runs the
+// whole pass program, so all of them take the same factor.  One warp per
+// pass; runs after prepare32_kernel and before scale_product_kernel (which
+// then sees the applied scales).
+__global__ void renorm_kernel(float* __restrict__ coef, int coef_stride, const int32_t* __restrict__ ptr,
+                              const int32_t* __restrict__ src, const int32_t* __restrict__ ren)
+{
+    const int k = blockIdx.x, lane = threadIdx.x;
+    coef += (int64_t)8 * blockIdx.y * coef_stride;
+    const int d = ren[k];
+    if (d < 0) return;
+    double lg = 0;
+    for (int i = ptr[k] + lane; i < ptr[k + 1]; i += 32) {
+        const float* m = coef + 8 * src[i];
+        const double r2 = (double)m[0] * m[0] + (double)m[1] * m[1] + (double)m[4] * m[4] + (double)m[5] * m[5];
+        lg += 0.5 * log(r2);
+    }
+    for (int o = 16; o > 0; o >>= 1) lg += __shfl_xor_sync(0xffffffffu, lg, o);
+    const float f = (float)exp(-lg);
+    __syncwarp();
+    if (lane < 8) coef[8 * d + lane] *= f;
+}
+
+extern "C" int qgt_dev_renorm_passes(float* coef32, int32_t coef_stride, const int32_t* ptr, const int32_t* src,
+                                     const int32_t* ren, int32_t npasses, int32_t npoints, void* s)
+{
+    if (npasses <= 0) return 0;
+    if (npoints < 1 || npoints > 65535) return qgt_set_error(QGT_EINVAL, "renorm: bad point count");
+    renorm_kernel<<<dim3((unsigned)npasses, (unsigned)npoints), 32, 0, (cudaStream_t)s>>>(coef32, coef_stride, ptr, src, ren);
+    return qgt_dev_last_error();
 }
 
 // rho[point][m] = prod over groups 0..m of the amplitude scales r = |column 0|

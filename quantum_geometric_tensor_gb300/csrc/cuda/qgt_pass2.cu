@@ -92,6 +92,21 @@ __device__ __forceinline__ float2 cmad2<float2, float>(const float* m, float2 x,
     return __ffma2_rn(make_float2(m[0], m[0]), x, o);
 }
 
+// real a x + y
+template <typename T, typename R>
+__device__ __forceinline__ T fma_s(R a, T x, T y)
+{
+    T o;
+    o.x = a * x.x + y.x;
+    o.y = a * x.y + y.y;
+    return o;
+}
+template <>
+__device__ __forceinline__ float2 fma_s<float2, float>(float a, float2 x, float2 y)
+{
+    return __ffma2_rn(make_float2(a, a), x, y);
+}
+
 // (pr + i pi) x
 template <typename T, typename R>
 __device__ __forceinline__ T cmul_s(R pr, R pi, T x)
@@ -135,6 +150,44 @@ __device__ __forceinline__ void u_reg(T* v, const R* m)
         } else {
             v[j] = cmad2<T, R>(m, a0, a1);
             v[k] = cmad2<T, R>(m + 4, a0, a1);
+        }
+    }
+}
+
+// tangent-form rotation [[1, m2], [m4, 1]]: one multiply-add per component
+template <int RI, int NR, typename T, typename R>
+__device__ __forceinline__ void tan_reg(T* v, R m2, R m4)
+{
+#pragma unroll
+    for (int j = 0; j < NR; j++) {
+        if (j & (1 << RI)) continue;
+        const int k = j | (1 << RI);
+        const T a0 = v[j], a1 = v[k];
+        v[j] = fma_s<T, R>(m2, a1, a0);
+        v[k] = fma_s<T, R>(m4, a0, a1);
+    }
+}
+
+// cotangent form [[m0, -SG], [SG, m6]], SG = +1 or -1
+template <int RI, int NR, int SG, typename T, typename R>
+__device__ __forceinline__ void cot_reg(T* v, R m0, R m6)
+{
+#pragma unroll
+    for (int j = 0; j < NR; j++) {
+        if (j & (1 << RI)) continue;
+        const int k = j | (1 << RI);
+        const T a0 = v[j], a1 = v[k];
+        T n;
+        if (SG > 0) {
+            n.x = -a1.x;
+            n.y = -a1.y;
+            v[j] = fma_s<T, R>(m0, a0, n);
+            v[k] = fma_s<T, R>(m6, a1, a0);
+        } else {
+            n.x = -a0.x;
+            n.y = -a0.y;
+            v[j] = fma_s<T, R>(m0, a0, a1);
+            v[k] = fma_s<T, R>(m6, a1, n);
         }
     }
 }
@@ -184,6 +237,63 @@ __device__ __forceinline__ void gen_reg(T* v, int gen)
     default: if (RB > 4) { CALL(4 % RB); } break;   \
     }
 
+// one single-qubit gate on register bit RI; real rotations in tangent form
+// [[1, -t], [t, 1]] or [[k, -g], [g, k]] (g = +-1) take the one-multiply-add
+// paths (the form is uniform per CTA: one coefficient table per point)
+template <int RI, int NR, typename T, typename R>
+__device__ __forceinline__ void gate_reg(T* v, const R* m, bool real)
+{
+    const bool tanf = real && m[0] == (R)1 && m[6] == (R)1;
+    const bool cotf = real && !tanf && m[2] == -m[4] && (m[4] == (R)1 || m[4] == (R)-1);
+    if (tanf) tan_reg<RI, NR, T, R>(v, m[2], m[4]);
+    else if (cotf && m[4] > (R)0) cot_reg<RI, NR, 1, T, R>(v, m[0], m[6]);
+    else if (cotf) cot_reg<RI, NR, -1, T, R>(v, m[0], m[6]);
+    else if (real) u_reg<RI, NR, true, T, R>(v, m);
+    else u_reg<RI, NR, false, T, R>(v, m);
+}
+
+// the same on lane bit b: v' = c_self v + c_partner w (w = the partner lane's
+// amplitude); row 1 of the matrix for the upper lane, row 0 for the lower one
+template <int NR, typename T, typename R>
+__device__ __forceinline__ void gate_lane(T* v, const R* m, bool real, int b, int lane)
+{
+    const bool tanf = real && m[0] == (R)1 && m[6] == (R)1;
+    const bool cotf = real && !tanf && m[2] == -m[4] && (m[4] == (R)1 || m[4] == (R)-1);
+    const int hi = (lane >> b) & 1;
+    const R cs0 = hi ? m[6] : m[0], cs1 = hi ? m[7] : m[1];
+    const R cp0 = hi ? m[4] : m[2], cp1 = hi ? m[5] : m[3];
+    if (tanf) {
+        // own + c w
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            const T w = shfl_x<T>(v[j], 1 << b);
+            v[j] = fma_s<T, R>(cp0, w, v[j]);
+        }
+    } else if (cotf) {
+        // k own + c w with c = -g (lower lane) or +g (upper lane)
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            T w = shfl_x<T>(v[j], 1 << b);
+            w.x *= cp0;
+            w.y *= cp0;
+            v[j] = fma_s<T, R>(cs0, v[j], w);
+        }
+    } else if (real) {
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            const T w = shfl_x<T>(v[j], 1 << b);
+            v[j] = rmad2<T, R>(cs0, v[j], cp0, w);
+        }
+    } else {
+        const R mm[4] = {cs0, cs1, cp0, cp1};
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            const T w = shfl_x<T>(v[j], 1 << b);
+            v[j] = cmad2<T, R>(mm, v[j], w);
+        }
+    }
+}
+
 // bit value of a non-register role for this thread
 __device__ __forceinline__ int role_bit(int role, int q, int lane, int warp, uint64_t base)
 {
@@ -218,13 +328,32 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
     // the pass program and each op's coefficients, staged once per CTA
     qgt_dev_op2_t* sops = reinterpret_cast<qgt_dev_op2_t*>(p2_smem + ((size_t)sizeof(T) << (5 + RB + 3)));
     R* scoef = reinterpret_cast<R*>(sops + a.nops);
+    // per SEG op: its layout's local bits [0, 16) and their physical qubits [16, 32)
+    int8_t* sseg = reinterpret_cast<int8_t*>(scoef + 8 * a.nops);
+    // generator matrices (-i/2) X, (-i/2) Y, (-i/2) Z (2 x 2 complex, row-major)
+    __shared__ R sgen[24];
     {
+        if (threadIdx.x < 24) {
+            const int g = threadIdx.x >> 3, k = threadIdx.x & 7;
+            const R h = (R)0.5;
+            R x = (R)0;
+            if (g == 0 && (k == 3 || k == 5)) x = -h;              // X: -i/2 off the diagonal
+            if (g == 1) x = (k == 2) ? -h : ((k == 4) ? h : (R)0);  // Y: [[0, -1/2], [1/2, 0]]
+            if (g == 2) x = (k == 1) ? -h : ((k == 7) ? h : (R)0);  // Z: diag(-i/2, i/2)
+            sgen[threadIdx.x] = x;
+        }
         const R* ctab = ((sizeof(R) == 4) ? reinterpret_cast<const R*>(a.coef32) : reinterpret_cast<const R*>(a.coef)) +
                         (int64_t)8 * blockIdx.z * a.coef_stride;
         for (int i = threadIdx.x; i < a.nops; i += blockDim.x) sops[i] = a.ops[i];
         for (int i = threadIdx.x; i < 8 * a.nops; i += blockDim.x) {
             const int c = a.ops[i >> 3].coef;
             scoef[i] = c >= 0 ? ctab[8 * c + (i & 7)] : (((i & 7) == 0 || (i & 7) == 6) ? (R)1 : (R)0);   // identity
+        }
+        for (int i = threadIdx.x; i < 32 * a.nops; i += blockDim.x) {
+            const qgt_dev_op2_t o = a.ops[i >> 5];
+            if (o.kind != Q2_SEG) continue;
+            const int8_t lb = a.segs[16 * o.seg + (i & 15)];
+            sseg[i] = (i & 16) ? ((lb >= 0 && lb < 16) ? a.local_to_phys[lb] : (int8_t)0) : lb;
         }
         __syncthreads();
     }
@@ -240,17 +369,18 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
     uint32_t preg[RB];   // n <= 30: physical indices fit in 32 bits
     int lthr = 0;
     uint32_t pthr = 0;
-    auto set_layout = [&](int s) {
-        const int8_t* L = a.segs + 16 * s;
+    auto set_layout = [&](int at) {   // the layout of the SEG op at program index `at`
+        const int8_t* L = sseg + 32 * at;
+        const int8_t* Pq = L + 16;
         lthr = lane;
         pthr = (uint32_t)base | (uint32_t)lane;  // local bits 0..4 are physical qubits 0..4
 #pragma unroll
         for (int w = 0; w < 3; w++) {
             const int lb = L[8 + w];
-            if ((warp >> w) & 1) { lthr |= 1 << lb; pthr |= 1u << a.local_to_phys[lb]; }
+            if ((warp >> w) & 1) { lthr |= 1 << lb; pthr |= 1u << Pq[8 + w]; }
         }
 #pragma unroll
-        for (int i = 0; i < RB; i++) { lreg[i] = 1 << L[i]; preg[i] = 1u << a.local_to_phys[L[i]]; }
+        for (int i = 0; i < RB; i++) { lreg[i] = 1 << L[i]; preg[i] = 1u << Pq[i]; }
     };
     auto lidx = [&](int j) {
         int l = lthr;
@@ -266,7 +396,47 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
     };
 
     T v[NR];
-    set_layout(sops[0].seg);
+    // (-i/2) G of the rotation op `so` on the current vector (a derivative spawned there), through
+    // the gate paths with the generator matrices (-i/2) X, (-i/2) Y, (-i/2) Z (exact: entries 0, +-1/2)
+    auto spawn_gen = [&](const qgt_dev_op2_t& so) {
+        const R* gm = sgen + 8 * (so.gen - QGEN_X);
+        const bool reg = so.ra >= RL_REG && so.ra < RL_WARP;
+        if (so.gen == QGEN_Z) {
+            if (reg) {
+                const int ri = so.ra - RL_REG;
+#define G_CALL(I) phase_reg<I, NR, T, R>(v, gm)
+                RB_SWITCH(ri, G_CALL)
+#undef G_CALL
+            } else {
+                const int bit = role_bit(so.ra, so.q, lane, warp, base);
+                const R pr = bit ? gm[6] : gm[0], pi = bit ? gm[7] : gm[1];
+#pragma unroll
+                for (int j = 0; j < NR; j++) v[j] = cm<T, R>(pr, pi, v[j]);
+            }
+        } else if (reg) {
+            const int ri = so.ra - RL_REG;
+            if (so.gen == QGEN_Y) {
+#define G_CALL(I) u_reg<I, NR, true, T, R>(v, gm)
+                RB_SWITCH(ri, G_CALL)
+#undef G_CALL
+            } else {
+#define G_CALL(I) u_reg<I, NR, false, T, R>(v, gm)
+                RB_SWITCH(ri, G_CALL)
+#undef G_CALL
+            }
+        } else {
+            const int b = so.ra, hi = (lane >> b) & 1;
+            const R cs0 = hi ? gm[6] : gm[0], cs1 = hi ? gm[7] : gm[1];
+            const R cp0 = hi ? gm[4] : gm[2], cp1 = hi ? gm[5] : gm[3];
+            const R mm[4] = {cs0, cs1, cp0, cp1};
+#pragma unroll
+            for (int j = 0; j < NR; j++) {
+                const T w = shfl_x<T>(v[j], 1 << b);
+                v[j] = cmad2<T, R>(mm, v[j], w);
+            }
+        }
+    };
+    set_layout(0);
     {
         const T* src = reinterpret_cast<const T*>(a.V) + blockIdx.z * a.point_stride + (int64_t)e.src_row * a.N;
 #pragma unroll
@@ -285,7 +455,7 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
 #pragma unroll
             for (int j = 0; j < NR; j++) tile[lidx(j)] = v[j];
             __syncthreads();
-            set_layout(op.seg);
+            set_layout(pc);
 #pragma unroll
             for (int j = 0; j < NR; j++) v[j] = tile[lidx(j)];
             continue;
@@ -373,41 +543,43 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
             pc += cnt;
             continue;
         }
+        if (op.kind == Q2_UM) {
+            // commuting single-qubit gates on distinct bits: `ra` lane gates, then one gate per
+            // register bit set in `rb`, ascending; a derivative spawned at any of them is
+            // applied after the block (its generator commutes with the other gates)
+            const int cnt = op.seg, nl = op.ra;
+            const uint32_t rmask = op.rb;
+            for (int u = pc + 1; u <= pc + nl; u++) {
+                const R* mm = scoef + 8 * u;
+                gate_lane<NR, T, R>(v, mm, sops[u].kind == Q2_UR, sops[u].ra, lane);
+            }
+            int at = pc + 1 + nl;
+#pragma unroll
+            for (int i = 0; i < RB; i++) {
+                if ((rmask >> i) & 1u) {
+                    const R* mm = scoef + 8 * at;
+                    const bool real = sops[at].kind == Q2_UR;
+#define U_CALL(I) gate_reg<I, NR, T, R>(v, mm, real)
+                    RB_SWITCH(i, U_CALL)
+#undef U_CALL
+                    at++;
+                }
+            }
+            if (e.spawn_op > pc && e.spawn_op <= pc + cnt) spawn_gen(sops[e.spawn_op]);
+            pc += cnt;
+            continue;
+        }
         if (op.kind == Q2_U || op.kind == Q2_UR) {
 #pragma unroll
             for (int i = 0; i < 8; i++) m[i] = scoef[8 * pc + i];
             const bool real = op.kind == Q2_UR;
             if (op.ra >= RL_REG) {
                 const int ri = op.ra - RL_REG;
-                if (real) {
-#define U_CALL(I) u_reg<I, NR, true, T, R>(v, m)
-                    RB_SWITCH(ri, U_CALL)
+#define U_CALL(I) gate_reg<I, NR, T, R>(v, m, real)
+                RB_SWITCH(ri, U_CALL)
 #undef U_CALL
-                } else {
-#define U_CALL(I) u_reg<I, NR, false, T, R>(v, m)
-                    RB_SWITCH(ri, U_CALL)
-#undef U_CALL
-                }
             } else {
-                // lane bit: v' = c_self v + c_partner w (w = the partner lane's amplitude);
-                // row 1 of the matrix for the upper lane, row 0 for the lower one
-                const int b = op.ra, hi = (lane >> b) & 1;
-                R cs[2] = {hi ? m[6] : m[0], hi ? m[7] : m[1]};
-                R cp[2] = {hi ? m[4] : m[2], hi ? m[5] : m[3]};
-                if (real) {
-#pragma unroll
-                    for (int j = 0; j < NR; j++) {
-                        T w = shfl_x<T>(v[j], 1 << b);
-                        v[j] = rmad2<T, R>(cs[0], v[j], cp[0], w);
-                    }
-                } else {
-                    R mm[4] = {cs[0], cs[1], cp[0], cp[1]};
-#pragma unroll
-                    for (int j = 0; j < NR; j++) {
-                        T w = shfl_x<T>(v[j], 1 << b);
-                        v[j] = cmad2<T, R>(mm, v[j], w);
-                    }
-                }
+                gate_lane<NR, T, R>(v, m, real, op.ra, lane);
             }
         } else if (op.kind == Q2_PHASE) {
 #pragma unroll
@@ -448,37 +620,7 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
                 }
             }
         }
-        if (pc == e.spawn_op) {
-            if (op.gen == QGEN_Z) {
-                const uint32_t mk = role_mask<NR>(op.ra, op.q, lane, warp, base);
-                const R h = (R)0.5;
-#pragma unroll
-                for (int j = 0; j < NR; j++) {
-                    const R sg = ((mk >> j) & 1u) ? h : -h;  // (-i/2) Z: multiply by i * sg
-                    T o;
-                    o.x = -sg * v[j].y;
-                    o.y = sg * v[j].x;
-                    v[j] = o;
-                }
-            } else if (op.ra >= RL_REG) {
-                const int ri = op.ra - RL_REG;
-                const int gen = op.gen;
-#define G_CALL(I) gen_reg<I, NR, T, R>(v, gen)
-                RB_SWITCH(ri, G_CALL)
-#undef G_CALL
-            } else {
-                const int b = op.ra, hi = (lane >> b) & 1;
-                const R h = (R)0.5;
-#pragma unroll
-                for (int j = 0; j < NR; j++) {
-                    T w = shfl_x<T>(v[j], 1 << b), o;
-                    if (op.gen == QGEN_X) { o.x = h * w.y; o.y = -h * w.x; }   // (-i/2) X: both rows take the partner
-                    else if (hi) { o.x = h * w.x; o.y = h * w.y; }              // (-i/2) Y: row 1 = +a0/2
-                    else { o.x = -h * w.x; o.y = -h * w.y; }                   //           row 0 = -a1/2
-                    v[j] = o;
-                }
-            }
-        }
+        if (pc == e.spawn_op) spawn_gen(op);
     }
     // store
     T* dst = reinterpret_cast<T*>(a.V) + blockIdx.z * a.point_stride + (int64_t)e.dst_row * a.N;
@@ -523,7 +665,7 @@ extern "C" int qgt_dev_pass2(const qgt_dev_pass2_args_t* a, int fp64, void* stre
     if (a->nentries > 65535 || ntiles > 0x7fffffff || np > 65535) return qgt_set_error(-1, "pass2: grid too large");
     dim3 grid((unsigned)ntiles, (unsigned)a->nentries, (unsigned)np);
     size_t smem = ((size_t)1 << (tb + (fp64 ? 4 : 3))) +                               /* 64 KiB tile */
-                  (size_t)a->nops * (sizeof(qgt_dev_op2_t) + 8 * (fp64 ? sizeof(double) : sizeof(float)));
+                  (size_t)a->nops * (sizeof(qgt_dev_op2_t) + 8 * (fp64 ? sizeof(double) : sizeof(float)) + 32);
     if (smem > 112 * 1024) return qgt_set_error(-1, "pass2: program of %d ops too large", a->nops);
     static int attr[2] = {0, 0};
     cudaError_t e = cudaSuccess;

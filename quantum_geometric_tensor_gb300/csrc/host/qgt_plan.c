@@ -90,6 +90,9 @@ struct qgt_plan {
     int nscale_groups;
     int32_t *scale_ptr_h, *scale_src_h, *row_group_h;
     int32_t *scale_ptr_d, *scale_src_d, *row_group_d;
+    /* pass renormalisation (complex64 programs): per pass its coefficient entries and the entry scaled by 1 / G */
+    int32_t *ren_ptr_h, *ren_src_h, *ren_h;
+    int32_t *ren_ptr_d, *ren_src_d, *ren_d;
     double* rho_d;
     int Pd;                       /* parameters [0, Pd) get derivative rows; Q is Pd x Pd */
     int64_t pstride;              /* amplitudes between points in V: (rows + 1) N */
@@ -941,11 +944,37 @@ static int emit_diag_run(qgt_plan_t* p, const qgt_dev_op2_t* src, int j, int e, 
     return 0;
 }
 
+/* Pass renormalisation lists for complex64 register-resident programs: the
+ * tangent-form RY coefficients scale vectors by up to sqrt 2 per gate, so
+ * each pass's last single-qubit gate entry also divides by the product G of
+ * the scales of all the pass's entries (formed on the device every step). */
+static int build_renorm(qgt_plan_t* p)
+{
+    if (p->fp64 || p->nprog == 0 || p->npasses == 0) return 0;
+    p->ren_ptr_h = (int32_t*)calloc((size_t)p->npasses + 1, sizeof(int32_t));
+    p->ren_src_h = (int32_t*)malloc(sizeof(int32_t) * ((size_t)p->nops + 1));
+    p->ren_h = (int32_t*)malloc(sizeof(int32_t) * (size_t)p->npasses);
+    if (!p->ren_ptr_h || !p->ren_src_h || !p->ren_h) return qgt_set_error(E_NOMEM, "renormalisation: oom");
+    int n = 0;
+    for (int k = 0; k < p->npasses; k++) {
+        const spass_t* ps = &p->passes[k];
+        p->ren_h[k] = -1;
+        for (int j = 0; j < ps->op_count; j++) {
+            const qgt_dev_op_t* o = &p->ops_h[ps->op_begin + j];
+            if (o->coef < 0) continue;
+            p->ren_src_h[n++] = o->coef;
+            if (o->kind == QOP_1Q && ps->prog_count > 0) p->ren_h[k] = o->coef;
+        }
+        p->ren_ptr_h[k + 1] = n;
+    }
+    return 0;
+}
+
 static int fold_diagonal_runs(qgt_plan_t* p)
 {
     if (p->nprog == 0) return 0;
     int rc = 0;
-    const int cap = 5 * p->nprog + 16;   /* a run of m ops emits at most 1 + RB + 2 m entries */
+    const int cap = 5 * p->nprog + 16;   /* a run of m ops emits at most 1 + RB + 2 m entries, a U block 1 + m */
     qgt_dev_op2_t* np2 = (qgt_dev_op2_t*)calloc((size_t)cap, sizeof(qgt_dev_op2_t));
     int* remap = (int*)malloc(sizeof(int) * ((size_t)p->nprog + 1));
     if (!np2 || !remap) { free(np2); free(remap); return qgt_set_error(E_NOMEM, "programs: oom"); }
@@ -957,6 +986,34 @@ static int fold_diagonal_runs(qgt_plan_t* p)
         const int n = ps->prog_count, nb = out;
         for (int j = 0; j < n;) {
             int e = j;
+            /* single-qubit gates on distinct lane / register bits commute: one Q2_UM block */
+            uint32_t used = 0;
+            while (e < n && (src[e].kind == Q2_U || src[e].kind == Q2_UR) && src[e].ra < RL_WARP_ &&
+                   !((used >> src[e].ra) & 1u)) {
+                used |= 1u << src[e].ra;
+                e++;
+            }
+            if (e - j >= 2 && out + (e - j) + 2 < cap) {
+                qgt_dev_op2_t h;
+                memset(&h, 0, sizeof h);
+                h.kind = Q2_UM;
+                h.seg = (int16_t)(e - j);
+                h.coef = -1;
+                h.slot = -1;
+                int nl = 0;
+                for (int t = j; t < e; t++) nl += src[t].ra < RL_REG_;
+                h.ra = (uint8_t)nl;
+                h.rb = (uint8_t)((used >> RL_REG_) & 0xffu);
+                np2[out++] = h;
+                for (int t = j; t < e; t++)
+                    if (src[t].ra < RL_REG_) { remap[t] = out - nb; np2[out++] = src[t]; }
+                for (int b = RL_REG_; b < RL_WARP_; b++)
+                    for (int t = j; t < e; t++)
+                        if (src[t].ra == b) { remap[t] = out - nb; np2[out++] = src[t]; }
+                j = e;
+                continue;
+            }
+            e = j;
             while (e < n && (src[e].kind == Q2_PHASE || src[e].kind == Q2_CZ)) e++;
             if (e - j >= 2 && out + 2 * (e - j) + 8 < cap) {
                 if ((rc = emit_diag_run(p, src, j, e, np2, &out, nb, remap)) != 0) { free(np2); free(remap); return rc; }
@@ -1082,6 +1139,7 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
     if ((rc = (p->mitm ? build_entries_mitm(p) : build_entries(p))) != 0) goto fail;
     if ((rc = build_programs(p)) != 0) goto fail;
     if ((rc = fold_diagonal_runs(p)) != 0) goto fail;
+    if ((rc = build_renorm(p)) != 0) goto fail;
     if (p->opt.hamiltonian == QGT_HAMILTONIAN_PAULI) {
         /* parse the strings: character [n-1-q] acts on qubit q */
         const int T = p->opt.num_pauli_terms;
@@ -1177,6 +1235,17 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
                                                       p->stream)) != 0)
             goto fail;
     }
+    if (p->ren_h) {
+        const int np = p->npasses;
+        DALLOC(p->ren_ptr_d, sizeof(int32_t) * (size_t)(np + 1));
+        DALLOC(p->ren_src_d, sizeof(int32_t) * (size_t)(p->ren_ptr_h[np] + 1));
+        DALLOC(p->ren_d, sizeof(int32_t) * (size_t)np);
+        if ((rc = qgt_dev_memcpy_h2d(p->ren_ptr_d, p->ren_ptr_h, sizeof(int32_t) * (size_t)(np + 1), p->stream)) != 0) goto fail;
+        if ((rc = qgt_dev_memcpy_h2d(p->ren_d, p->ren_h, sizeof(int32_t) * (size_t)np, p->stream)) != 0) goto fail;
+        if (p->ren_ptr_h[np] &&
+            (rc = qgt_dev_memcpy_h2d(p->ren_src_d, p->ren_src_h, sizeof(int32_t) * (size_t)p->ren_ptr_h[np], p->stream)) != 0)
+            goto fail;
+    }
     DALLOC(p->slot_param_d, sizeof(int32_t) * (size_t)(p->nslots + 1));
     DALLOC(p->param_ptr_d, sizeof(int32_t) * (size_t)(p->Pd + 2));
     DALLOC(p->param_slots_d, sizeof(int32_t) * (size_t)(p->nslots + 1));
@@ -1251,6 +1320,7 @@ void qgt_plan_destroy(qgt_plan_t* p)
         free(p->gates); free(p->passes); free(p->ops_h); free(p->ents_h); free(p->coef_h); free(p->prog_h);
         free(p->segs_h); free(p->slot_param_h); free(p->param_ptr_h); free(p->param_slots_h); free(p->pauli_h);
         free(p->scale_ptr_h); free(p->scale_src_h); free(p->row_group_h);
+        free(p->ren_ptr_h); free(p->ren_src_h); free(p->ren_h);
         free(p->op_gate);
         free(p->comb_ptr_h);
         free(p->comb_src_h);
@@ -1264,11 +1334,12 @@ void qgt_plan_destroy(qgt_plan_t* p)
     qgt_dev_free(p->rowmax_d);
     free(p->pauli_h);
     free(p->scale_ptr_h); free(p->scale_src_h); free(p->row_group_h);
+    free(p->ren_ptr_h); free(p->ren_src_h); free(p->ren_h);
     free(p->op_gate);
     free(p->comb_ptr_h);
     free(p->comb_src_h);
     void* dev[] = {p->V, p->split, p->small_part_d, p->pauli_d, p->scale_ptr_d, p->scale_src_d, p->row_group_d,
-                   p->rho_d, p->comb_ptr_d, p->comb_src_d,
+                   p->rho_d, p->comb_ptr_d, p->comb_src_d, p->ren_ptr_d, p->ren_src_d, p->ren_d,
                    p->ops_d, p->ents_d, p->prog_d, p->segs_d, p->coef32_d, p->coef_desc_d, p->coef_d, p->theta_d, p->HG_d, p->part_d,
                    p->Q_d, p->grad_d, p->energy_d, p->natgrad_d, p->chol_work_d, p->status_d, p->slot_param_d,
                    p->param_ptr_d, p->param_slots_d};
@@ -1349,6 +1420,12 @@ static int run_step(qgt_plan_t* p)
         if ((rc = qgt_dev_prepare32(p->coef_desc_d, p->ncoef, p->theta_d, p->coef32_d, p->B, p->P, cstride, p->stream)) != 0)
             return rc;
         launches += p->ncoef > 0;
+        if (p->ren_d) {
+            if ((rc = qgt_dev_renorm_passes(p->coef32_d, cstride, p->ren_ptr_d, p->ren_src_d, p->ren_d, p->npasses, p->B,
+                                            p->stream)) != 0)
+                return rc;
+            launches++;
+        }
         if (p->rho_d) {
             if ((rc = qgt_dev_scale_product(p->coef32_d, cstride, p->scale_ptr_d, p->scale_src_d, p->nscale_groups,
                                             p->rho_d, p->B, p->stream)) != 0)
@@ -1793,6 +1870,11 @@ int qgt_plan_schedule_dump(const void* circuit, const void* options, const char*
             const qgt_dev_op_t* o = &p->ops_h[ps->op_begin + j];
             fprintf(f, "%s[%d, %d, %d, %d, %d, %d]", j ? ", " : "", (int)o->pad, (int)o->q, (int)o->q2, o->coef, o->slot,
                     (int)o->kind);
+        }
+        if (p->ren_h) {
+            fprintf(f, "], \"ren\": %d, \"ren_src\": [", p->ren_h[k]);
+            for (int j = p->ren_ptr_h[k]; j < p->ren_ptr_h[k + 1]; j++)
+                fprintf(f, "%s%d", j > p->ren_ptr_h[k] ? ", " : "", p->ren_src_h[j]);
         }
         fprintf(f, "], \"prog\": [");
         for (int j = 0; j < ps->prog_count; j++) {

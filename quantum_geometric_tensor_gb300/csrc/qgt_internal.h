@@ -112,7 +112,9 @@ typedef struct {
  * 32 outside the tile (physical qubit in q / q2). */
 enum { Q2_SEG = 1, Q2_U = 2, Q2_UR = 3, Q2_PHASE = 4, Q2_CZ = 5, Q2_CNOT = 6, Q2_DIAG = 7,
        Q2_CZT = 9,    /* in a diagonal run: the thread factor flips when thread bit q and popc(thread bits & slot) are odd */
-       Q2_ZGEN = 10 };/* in a diagonal run: marks a derivative spawned by the rotation on (ra, q) */
+       Q2_ZGEN = 10,  /* in a diagonal run: marks a derivative spawned by the rotation on (ra, q) */
+       Q2_UM = 11 };  /* header of `seg` commuting Q2_U / Q2_UR ops on distinct bits: `ra` lane ops, then one
+                         op per register bit set in `rb`, ascending */
 /* Q2_DIAG: header of a run of diagonal gates applied as one per-thread phase
  * table; `seg` sub-ops follow: RB register-bit entries (Q2_PHASE on register
  * bit i = 0 .. RB-1 in order, coef -1 = no phase, slot = the physical qubits
@@ -156,6 +158,10 @@ typedef struct {
 int qgt_dev_pass2(const qgt_dev_pass2_args_t* args, int fp64, void* stream);
 /* rho[point][m] = product over groups 0..m of the amplitude scales |column 0|
  * of the complex64 coefficient entries src[ptr[g] .. ptr[g+1]) */
+/* per pass and point: multiply the pass's designated entry ren[pass] by 1 / prod of the scales
+ * (|column 0|) of the pass's entries src[ptr[pass] .. ptr[pass + 1]) (complex64 tables) */
+int qgt_dev_renorm_passes(float* coef32, int32_t coef_stride, const int32_t* ptr, const int32_t* src,
+                          const int32_t* ren, int32_t npasses, int32_t npoints, void* stream);
 int qgt_dev_scale_product(const float* coef32, int32_t coef_stride, const int32_t* ptr, const int32_t* src,
                           int32_t ngroups, double* rho, int32_t npoints, void* stream);
 int qgt_dev_prepare32(const qgt_dev_coef_desc_t* descs_dev, int32_t ncoef, const double* theta_dev,
