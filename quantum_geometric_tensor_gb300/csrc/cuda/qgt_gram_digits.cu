@@ -127,10 +127,10 @@ static __device__ __forceinline__ uint64_t desc_sw32(uint32_t saddr)
     return d;
 }
 
-// kind::f16, D = F32, A = B = F16, K-major, M = N = 128
-static __device__ __forceinline__ uint32_t idesc_f16(int negA)
+// kind::f16, D = F32, A = B = F16, K-major, M = 128, N = n (a multiple of 16, 16 .. 128)
+static __device__ __forceinline__ uint32_t idesc_f16(int negA, uint32_t n)
 {
-    return (1u << 4) | ((uint32_t)negA << 13) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+    return (1u << 4) | ((uint32_t)negA << 13) | ((n >> 3) << 17) | ((128u >> 4) << 24);
 }
 
 static __device__ __forceinline__ void umma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc)
@@ -216,6 +216,10 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
     pair_of((int)(blockIdx.x % ntp), nbk, &mb, &nbo);
     const bool diag = (mb == nbo);
     const int nblk = diag ? 1 : 2;
+    // the last row block holds rows - 128 (nbk - 1) rows: its pairs use N = that count rounded up to 16
+    // (columns past N are neither computed nor written; the reduction reads only j < rows)
+    const int vlast = rows - 128 * (nbk - 1);
+    const int nN = (nbo == nbk - 1) ? ((vlast + 15) & ~15) : 128;
     const int64_t k0 = (int64_t)(blockIdx.x / ntp) * kchunk;
     int64_t k1 = k0 + kchunk;
     if (k1 > N) k1 = N;
@@ -281,7 +285,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
                 (void)bar_wait(smem_u32(&raw_full[u % DG_RAW_STAGES]), (u / DG_RAW_STAGES) & 1, deadline + DG_TIMEOUT_NS);
     } else if (warp == 1 && lane == 0) {
         // ---------- MMA issuer ----------
-        const uint32_t idp = idesc_f16(0), idn = idesc_f16(1);
+        const uint32_t idp = idesc_f16(0, (uint32_t)nN), idn = idesc_f16(1, (uint32_t)nN);
         for (int kt = 0; kt < nk; kt++) {
             const int s = kt % DG_PL_STAGES;
             if (!bar_wait(smem_u32(&pl_full[s]), (kt / DG_PL_STAGES) & 1, deadline)) {
@@ -324,8 +328,9 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
             for (int b = 0; b < nblk; b++) {
                 const float* raw = reinterpret_cast<const float*>(rawst + b * DG_RAW_BYTES);
                 uint8_t* planes = plst + b * 6 * DG_PLANE_BYTES;
+                const int rlim = b == 1 ? nN : 128;   // the MMAs read N rows of the B block
 #pragma unroll 4
-                for (int rr = 4 * cw; rr < 128; rr += 4 * DG_CONV_WARPS) {
+                for (int rr = 4 * cw; rr < rlim; rr += 4 * DG_CONV_WARPS) {
                     const int r = rr + sub;
                     const float4 q = *reinterpret_cast<const float4*>(raw + r * 32 + 2 * kp);
                     const float iu = inv_u[b][r];
@@ -364,9 +369,11 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
             const uint32_t lanebase = tmem + ((uint32_t)(quad * 32) << 16);
             for (int ri = 0; ri < 2; ri++) {
                 for (int c = 2 * half; c < 2 * half + 2; c++) {
+                    if (c * 32 >= nN) continue;
                     tmem_ld32(lanebase + ri * 128 + c * 32, hh);
                     tmem_ld32(lanebase + 256 + ri * 128 + c * 32, rsd);
-                    if (diag && ri == 0 && c == (row >> 5) && hh[row & 31] > 8388608.0f) atomicExch(err, DG_ERR_INEXACT);
+                    if (diag && ri == 0 && c == (row >> 5) && row < nN && hh[row & 31] > 8388608.0f)
+                        atomicExch(err, DG_ERR_INEXACT);
                     float4* o = reinterpret_cast<float4*>(out + ri * 128 * 128 + row * 128 + c * 32);
 #pragma unroll
                     for (int j = 0; j < 8; j++)

@@ -1212,7 +1212,11 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
         DALLOC(p->grad_d, sizeof(double) * (B * Pd + 1));
         DALLOC(p->energy_d, sizeof(double) * (B + 1));
         DALLOC(p->natgrad_d, sizeof(double) * (B * Pd + 1));
-        DALLOC(p->chol_work_d, sizeof(double) * B * Pd * Pd);
+        /* single points of complex64 plans solve with the refined FP32 factorisation */
+        size_t cw = B * Pd * Pd;
+        if (!p->fp64 && B == 1 && Pd > 0 && Pd <= 2048 && (size_t)qgt_dev_cholesky_refined_work((int32_t)Pd) > cw)
+            cw = (size_t)qgt_dev_cholesky_refined_work((int32_t)Pd);
+        DALLOC(p->chol_work_d, sizeof(double) * (cw + 1));
         DALLOC(p->status_d, sizeof(double) * 2 * B);
     }
     if (p->npauli) {
@@ -1564,6 +1568,11 @@ static int run_step(qgt_plan_t* p)
                                                  p->natgrad_d, p->status_d, p->B, p->stream)) != 0)
                     return rc;
                 launches++;
+            } else if (p->Pd <= 2048 && !p->fp64) {
+                if ((rc = qgt_dev_cholesky_refined(p->Q_d, 1, p->grad_d, p->Pd, p->opt.lambda, p->chol_work_d,
+                                                   p->natgrad_d, p->status_d, p->stream)) != 0)
+                    return rc;
+                launches += qgt_dev_cholesky_refined_launches(p->Pd);
             } else if (p->Pd <= 2048) {
                 if ((rc = qgt_dev_cholesky_blocked(p->Q_d, 1, p->grad_d, p->Pd, p->opt.lambda, p->chol_work_d,
                                                    p->natgrad_d, p->status_d, p->stream)) != 0)
@@ -1653,9 +1662,13 @@ int qgt_plan_execute_host(qgt_plan_t* p, const double* theta, double* Q, double*
         if ((rc = qgt_dev_stream_sync(p->stream)) != 0) return rc;
         if (B == 1) {
             /* the graph's blocked solve has no retries: on a non-positive pivot
-             * rerun the solve with lambda x 10 retries (outside the graph) */
+             * rerun the solve with lambda x 10 retries (outside the graph).  The
+             * refined solve of complex64 plans also stops when its FP32 factor
+             * loses a pivot or the refinement does not converge; the FP64
+             * solver then starts from lambda itself */
+            const double lam0 = p->fp64 || p->Pd > 2048 ? p->opt.lambda * 10.0 : p->opt.lambda;
             if ((int)p->status_pin[0] != 0 &&
-                (rc = qgt_dev_cholesky(p->Q_d, 1, p->grad_d, p->Pd, p->opt.lambda * 10.0, p->chol_work_d, p->natgrad_d,
+                (rc = qgt_dev_cholesky(p->Q_d, 1, p->grad_d, p->Pd, lam0, p->chol_work_d, p->natgrad_d,
                                        p->status_d, p->stream)) != 0)
                 return rc;
         } else {

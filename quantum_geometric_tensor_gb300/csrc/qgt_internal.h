@@ -301,6 +301,14 @@ int qgt_dev_cholesky(const double* A, int complex_input, const double* b, int32_
 int qgt_dev_cholesky_blocked(const double* A, int complex_input, const double* b, int32_t P,
                              double lambda, double* work, double* x, double* status, void* stream);
 int qgt_dev_cholesky_launches(int32_t P);
+/* the same solve with an FP32 blocked factorisation and FP64 iterative
+ * refinement (FP64-accurate; status[0] = QGT_ERROR_CONVERGENCE_FAILED or
+ * QGT_ERROR_NOT_POSITIVE_DEFINITE asks for the FP64 solver); work holds
+ * qgt_dev_cholesky_refined_work(P) doubles; P <= 2048 */
+int qgt_dev_cholesky_refined(const double* A, int complex_input, const double* b, int32_t P, double lambda,
+                             double* work, double* x, double* status, void* stream);
+int64_t qgt_dev_cholesky_refined_work(int32_t P);
+int qgt_dev_cholesky_refined_launches(int32_t P);
 /* nsys independent single-CTA solves with retries, systems contiguous
  * (A: nsys x P x P, b / x: nsys x P, work: nsys x P x P, status: nsys x 2) */
 int qgt_dev_cholesky_batch(const double* A, int complex_input, const double* b, int32_t P, double lambda,
