@@ -317,7 +317,9 @@ __device__ __forceinline__ uint32_t role_mask(int role, int q, int lane, int war
     return role_bit(role, q, lane, warp, base) ? all : 0u;
 }
 
-template <typename R, int RB>
+// CKPT: the launch's entries also store their state before every Q2_SEG op whose slot is >= 0 (the
+// checkpoint writers of a pass; spawns then run the program from that segment on)
+template <typename R, int RB, bool CKPT>
 __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_t a)
 {
     typedef typename v2of<R>::T T;
@@ -332,7 +334,15 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
     int8_t* sseg = reinterpret_cast<int8_t*>(scoef + 8 * a.nops);
     // generator matrices (-i/2) X, (-i/2) Y, (-i/2) Z (2 x 2 complex, row-major)
     __shared__ R sgen[24];
+    // physical offset of the tile's local bits 5 .. tile_bits - 1 (checkpoint stores)
+    __shared__ uint32_t supper[256];
     {
+        if (threadIdx.x < (1 << (a.tile_bits - 5))) {
+            uint32_t o = 0;
+            for (int b = 5; b < a.tile_bits; b++)
+                if ((threadIdx.x >> (b - 5)) & 1) o |= 1u << a.local_to_phys[b];
+            supper[threadIdx.x] = o;
+        }
         if (threadIdx.x < 24) {
             const int g = threadIdx.x >> 3, k = threadIdx.x & 7;
             const R h = (R)0.5;
@@ -455,6 +465,16 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
 #pragma unroll
             for (int j = 0; j < NR; j++) tile[lidx(j)] = v[j];
             __syncthreads();
+            if (CKPT && op.slot >= 0) {
+                // checkpoint writer: the state before this segment (the tile in local order), for the
+                // spawns that start here; warps copy 32 consecutive amplitudes (local bits 0..4 =
+                // physical qubits 0..4)
+                T* ck = reinterpret_cast<T*>(a.V) + blockIdx.z * a.point_stride + (int64_t)op.slot * a.N;
+                for (int i = 0; i < NR; i++) {
+                    const int l = threadIdx.x + (int)blockDim.x * i;
+                    ck[(uint32_t)base | (uint32_t)(l & 31) | supper[l >> 5]] = tile[l];
+                }
+            }
             set_layout(pc);
 #pragma unroll
             for (int j = 0; j < NR; j++) v[j] = tile[lidx(j)];
@@ -670,12 +690,17 @@ extern "C" int qgt_dev_pass2(const qgt_dev_pass2_args_t* a, int fp64, void* stre
     static int attr[2] = {0, 0};
     cudaError_t e = cudaSuccess;
     if (!attr[fp64 ? 1 : 0]) {
-        e = fp64 ? cudaFuncSetAttribute(pass2_kernel<double, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 112 * 1024)
-                 : cudaFuncSetAttribute(pass2_kernel<float, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, 112 * 1024);
+        e = fp64 ? cudaFuncSetAttribute(pass2_kernel<double, 4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 112 * 1024)
+                 : cudaFuncSetAttribute(pass2_kernel<float, 5, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 112 * 1024);
+        if (e == cudaSuccess)
+            e = fp64 ? cudaFuncSetAttribute(pass2_kernel<double, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 112 * 1024)
+                     : cudaFuncSetAttribute(pass2_kernel<float, 5, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 112 * 1024);
         if (e == cudaSuccess) attr[fp64 ? 1 : 0] = 1;
     }
     if (e != cudaSuccess) return qgt_set_error(-6, "pass2: %s", cudaGetErrorString(e));
-    if (fp64) pass2_kernel<double, 4><<<grid, 256, smem, (cudaStream_t)stream>>>(*a);
-    else pass2_kernel<float, 5><<<grid, 256, smem, (cudaStream_t)stream>>>(*a);
+    if (fp64 && a->ckpt) pass2_kernel<double, 4, true><<<grid, 256, smem, (cudaStream_t)stream>>>(*a);
+    else if (fp64) pass2_kernel<double, 4, false><<<grid, 256, smem, (cudaStream_t)stream>>>(*a);
+    else if (a->ckpt) pass2_kernel<float, 5, true><<<grid, 256, smem, (cudaStream_t)stream>>>(*a);
+    else pass2_kernel<float, 5, false><<<grid, 256, smem, (cudaStream_t)stream>>>(*a);
     return qgt_dev_last_error();
 }

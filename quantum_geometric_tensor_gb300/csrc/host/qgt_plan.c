@@ -40,6 +40,7 @@
 #define E_HW (-6)
 
 /* role encoding of register-resident programs (see qgt_dev_op2_t) */
+#define QGT_CKPT_GROUPS 16
 #define RL_REG_ 8
 #define RL_WARP_ 16
 #define RL_OUT_ 32
@@ -62,6 +63,11 @@ typedef struct {
     int part;                     /* 0 forward (with first-half slots); meet in the middle: 1 psi forward, 2 backward */
     int op_begin, op_count;
     int ent_begin, ent_count;
+    /* segment checkpoints (build_checkpoints): entry 0 writes them (launched first, alone); entries
+     * [grp_begin[g], + grp_count[g]) run the program from its op grp_start[g] (a Q2_SEG) */
+    int ckpt_writer;
+    int ngrp;
+    int grp_begin[QGT_CKPT_GROUPS], grp_count[QGT_CKPT_GROUPS], grp_start[QGT_CKPT_GROUPS];
     int prog_begin, prog_count;   /* register-resident program (full tiles), 0 = v1 pass */
     int tile_bits;
     uint32_t tile_mask;
@@ -944,6 +950,132 @@ static int emit_diag_run(qgt_plan_t* p, const qgt_dev_op2_t* src, int j, int e, 
     return 0;
 }
 
+/* Segment checkpoints.  Every vector of a pass runs the whole pass program, so
+ * a derivative spawned in segment s first repeats the source vector's
+ * evolution through segments 0 .. s-1.  For the largest group of spawns from
+ * one source row, a writer entry (the source's own transport if the pass has
+ * one, else an extra entry that stores nothing at the end) runs first and
+ * stores its state at the start of every segment that a spawn begins in;
+ * those spawns then start at their segment from the stored state (launched
+ * after the writer).  The arithmetic of every vector is unchanged. */
+static int build_checkpoints(qgt_plan_t* p)
+{
+    if (p->nprog == 0) return 0;
+    for (int i = 0; i < p->nprog; i++)
+        if (p->prog_h[i].kind == Q2_SEG) p->prog_h[i].slot = -1;
+    int total = 0;
+    for (int k = 0; k < p->npasses; k++) total += p->passes[k].ent_count + 1;
+    qgt_dev_entry_t* ne = (qgt_dev_entry_t*)malloc(sizeof(qgt_dev_entry_t) * ((size_t)total + 1));
+    int* segpos = (int*)malloc(sizeof(int) * ((size_t)p->nprog + 1));
+    int* ckrow = (int*)malloc(sizeof(int) * ((size_t)p->nprog + 1));
+    int* startof = (int*)malloc(sizeof(int) * ((size_t)total + 1));
+    if (!ne || !segpos || !ckrow || !startof) {
+        free(ne); free(segpos); free(ckrow); free(startof);
+        return qgt_set_error(E_NOMEM, "checkpoints: oom");
+    }
+    const int base_row = (int)(p->pstride / p->N);
+    int maxck = 0, out = 0;
+    for (int k = 0; k < p->npasses; k++) {
+        spass_t* ps = &p->passes[k];
+        const qgt_dev_entry_t* src = p->ents_h + ps->ent_begin;
+        const int nen = ps->ent_count, nb = out;
+        ps->ckpt_writer = 0;
+        ps->ngrp = 0;
+        qgt_dev_op2_t* prog = p->prog_h + ps->prog_begin;
+        int nseg = 0;
+        for (int i = 0; i < ps->prog_count; i++)
+            if (prog[i].kind == Q2_SEG) segpos[nseg++] = i;
+        /* the segment (program index of its Q2_SEG) that a spawn from row r starts in */
+#define SEG_OF(e) ({ int sp_ = 0; for (int t_ = 1; t_ < nseg; t_++) if (segpos[t_] <= (e)->spawn_op) sp_ = segpos[t_]; sp_; })
+        /* the source row (with its zero-state flag) with the most spawns beyond the first segment */
+        int best = -1, best_n = 0;
+        for (int a = 0; a < nen && nseg > 1; a++) {
+            if (src[a].spawn_op < 0) continue;
+            int na = 0;
+            for (int b = 0; b < nen; b++)
+                if (src[b].spawn_op >= 0 && src[b].src_row == src[a].src_row &&
+                    (src[b].flags & QENT_SRC_ZERO) == (src[a].flags & QENT_SRC_ZERO) && SEG_OF(&src[b]) > 0)
+                    na++;
+            if (na > best_n) { best_n = na; best = a; }
+        }
+        if (best_n < 2) {
+            for (int a = 0; a < nen; a++) ne[out++] = src[a];
+            ps->ent_begin = nb;
+            ps->ent_count = out - nb;
+            continue;
+        }
+        const int srow = src[best].src_row, szero = src[best].flags & QENT_SRC_ZERO;
+        /* segments that spawns start in: a checkpoint row and a launch group each (at most
+         * QGT_CKPT_GROUPS; spawns in further segments run the whole program as before) */
+        for (int i = 0; i < ps->prog_count; i++) ckrow[i] = -1;
+        int nck = 0;
+        for (int a = 0; a < nen; a++) {
+            const qgt_dev_entry_t* e = &src[a];
+            startof[a] = 0;
+            if (e->spawn_op < 0 || e->src_row != srow || (e->flags & QENT_SRC_ZERO) != szero) continue;
+            const int sp = SEG_OF(e);
+            if (sp == 0) continue;
+            if (ckrow[sp] < 0) {
+                if (nck >= QGT_CKPT_GROUPS) continue;
+                ps->grp_start[nck] = sp;
+                ckrow[sp] = nck++;
+            }
+            startof[a] = sp;
+        }
+#undef SEG_OF
+        for (int i = 0; i < ps->prog_count; i++)
+            if (ckrow[i] >= 0) prog[i].slot = base_row + ckrow[i];
+        if (nck > maxck) maxck = nck;
+        /* the writer: the source's transport, or an entry that keeps nothing */
+        int wi = -1;
+        for (int a = 0; a < nen; a++)
+            if (src[a].spawn_op < 0 && src[a].src_row == srow && (src[a].flags & QENT_SRC_ZERO) == szero) { wi = a; break; }
+        qgt_dev_entry_t w;
+        if (wi >= 0) w = src[wi];
+        else {
+            memset(&w, 0, sizeof w);
+            w.src_row = srow;
+            w.dst_row = srow;
+            w.spawn_op = -1;
+            w.flags = szero;
+            p->vector_passes++;
+        }
+        ne[out++] = w;
+        ps->ckpt_writer = 1;
+        /* entries that run the whole program, then one group per checkpoint */
+        for (int a = 0; a < nen; a++)
+            if (a != wi && startof[a] == 0) ne[out++] = src[a];
+        ps->ngrp = nck;
+        for (int g = 0; g < nck; g++) {
+            const int sp = ps->grp_start[g];
+            ps->grp_begin[g] = out - nb;
+            for (int a = 0; a < nen; a++) {
+                if (a == wi || startof[a] != sp) continue;
+                qgt_dev_entry_t e = src[a];
+                e.src_row = base_row + ckrow[sp];
+                e.spawn_op -= sp;
+                e.flags &= ~QENT_SRC_ZERO;
+                ne[out++] = e;
+            }
+            ps->grp_count[g] = out - nb - ps->grp_begin[g];
+        }
+        ps->ent_begin = nb;
+        ps->ent_count = out - nb;
+        if (ps->ent_count > 65535) {
+            free(ne); free(segpos); free(ckrow); free(startof);
+            return qgt_set_error(E_INVAL, "pass has more than 65535 vectors");
+        }
+    }
+    free(p->ents_h);
+    p->ents_h = ne;
+    p->nents = out;
+    p->pstride += (int64_t)maxck * p->N;
+    free(segpos);
+    free(ckrow);
+    free(startof);
+    return 0;
+}
+
 /* Pass renormalisation lists for complex64 register-resident programs: the
  * tangent-form RY coefficients scale vectors by up to sqrt 2 per gate, so
  * each pass's last single-qubit gate entry also divides by the product G of
@@ -1140,6 +1272,7 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
     if ((rc = build_programs(p)) != 0) goto fail;
     if ((rc = fold_diagonal_runs(p)) != 0) goto fail;
     if ((rc = build_renorm(p)) != 0) goto fail;
+    if (!host_only && (rc = build_checkpoints(p)) != 0) goto fail;
     if (p->opt.hamiltonian == QGT_HAMILTONIAN_PAULI) {
         /* parse the strings: character [n-1-q] acts on qubit q */
         const int T = p->opt.num_pauli_terms;
@@ -1501,7 +1634,34 @@ static int run_step(qgt_plan_t* p)
             b.coef_stride = a.coef_stride;
             b.point_stride = a.point_stride;
             b.rowmax_stride = a.rowmax_stride;
-            if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) return rc;
+            if (ps->ckpt_writer) {
+                /* the checkpoint writer first, then the entries that run the whole program, then
+                 * the spawns from each checkpoint on the program from that segment */
+                const int nall = b.nentries;
+                b.nentries = 1;
+                b.ckpt = 1;
+                if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) return rc;
+                b.ckpt = 0;
+                launches++;
+                const int rest = (ps->ngrp > 0 ? ps->grp_begin[0] : nall) - 1;
+                b.entries = a.entries + 1;
+                b.nentries = rest;
+                if (rest > 0) {
+                    if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) return rc;
+                    launches++;
+                }
+                for (int g = 0; g < ps->ngrp; g++) {
+                    b.ops = p->prog_d + ps->prog_begin + ps->grp_start[g];
+                    b.nops = ps->prog_count - ps->grp_start[g];
+                    b.entries = a.entries + ps->grp_begin[g];
+                    b.nentries = ps->grp_count[g];
+                    if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) return rc;
+                    launches++;
+                }
+                launches--;   /* counted once below */
+            } else if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) {
+                return rc;
+            }
         } else if ((rc = qgt_dev_pass(&a, p->fp64, p->stream)) != 0) {
             return rc;
         }

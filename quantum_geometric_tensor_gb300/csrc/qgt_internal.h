@@ -154,6 +154,8 @@ typedef struct {
     int32_t coef_stride;
     int64_t point_stride;
     int32_t rowmax_stride;
+    int32_t ckpt;                   /* 1: the entries store their state before every Q2_SEG op with slot >= 0
+                                       into row slot (checkpoints for spawns that start at that segment) */
 } qgt_dev_pass2_args_t;
 int qgt_dev_pass2(const qgt_dev_pass2_args_t* args, int fp64, void* stream);
 /* rho[point][m] = product over groups 0..m of the amplitude scales |column 0|
