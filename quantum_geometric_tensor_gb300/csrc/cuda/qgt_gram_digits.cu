@@ -21,10 +21,15 @@
 //
 // Data path per CTA (tile pair mb <= nb, K range of <= 1024 amplitudes):
 //   TMA: 128 rows x 16 amplitudes of complex64 per row block -> raw smem
-//   8 converter warps: raw -> 6 FP16 planes {Re D, Re l1, Re l2, Im D, Im l1,
-//                      Im l2} in the SWIZZLE_32B K-major UMMA layout
-//   1 thread: 24 tcgen05.mma (M = N = 128, K = 16) per k-step into
-//             TMEM [D*D Re | D*D Im | rest Re | rest Im] (512 columns)
+//   8 converter warps: raw -> FP16 planes in the SWIZZLE_32B K-major UMMA
+//                      layout: the A block as 6 planes {Re D, Im D, Re l1,
+//                      Im l1, Re l2, Im l2}, the B block as 9 planes
+//                      {Re D, Im D, -Re D, Re l1, Im l1, -Re l1, Re l2, Im l2,
+//                      -Re l2}, so that every (Re, Im) pair of B operands that
+//                      one A plane meets is two adjacent planes
+//   1 thread: 12 tcgen05.mma (M = 128, N = 256 = [Re partner | Im partner],
+//             K = 16) per k-step into TMEM [D*D Re | D*D Im | rest Re |
+//             rest Im] (512 columns)
 //   epilogue (the converter warps): TMEM -> FP32 (hh + rest) -> partials
 // The raw ring (3 stages) and the plane ring (2 stages) are decoupled, so a
 // raw buffer is refilled as soon as it has been converted.
@@ -48,7 +53,10 @@
 #define DG_PL_STAGES 2                              // plane ring: 2 x 2 blocks x 6 planes x 4 KiB
 #define DG_CONV_WARPS 8
 #define DG_THREADS (64 + 32 * DG_CONV_WARPS)
-#define DG_SMEM_BYTES (DG_RAW_STAGES * 2 * DG_RAW_BYTES + DG_PL_STAGES * 12 * DG_PLANE_BYTES + 1024)
+#define DG_PL_A 6                                   // planes of the A block
+#define DG_PL_B 9                                   // planes of the B block (with the negated real ones)
+#define DG_PL_STAGE ((DG_PL_A + DG_PL_B) * DG_PLANE_BYTES)
+#define DG_SMEM_BYTES (DG_RAW_STAGES * 2 * DG_RAW_BYTES + DG_PL_STAGES * DG_PL_STAGE + 1024)
 #define DG_KMAX 1024                                // amplitudes per CTA (exactness bound; shorter FP32 chains)
 #define DG_TIMEOUT_NS 4000000000ull
 #define DG_ERR_TIMEOUT (-13)
@@ -127,10 +135,10 @@ static __device__ __forceinline__ uint64_t desc_sw32(uint32_t saddr)
     return d;
 }
 
-// kind::f16, D = F32, A = B = F16, K-major, M = 128, N = n (a multiple of 16, 16 .. 128)
-static __device__ __forceinline__ uint32_t idesc_f16(int negA, uint32_t n)
+// kind::f16, D = F32, A = B = F16, K-major, M = 128, N = n (a multiple of 16, 16 .. 256)
+static __device__ __forceinline__ uint32_t idesc_f16(uint32_t n)
 {
-    return (1u << 4) | ((uint32_t)negA << 13) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+    return (1u << 4) | ((n >> 3) << 17) | ((128u >> 4) << 24);
 }
 
 static __device__ __forceinline__ void umma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc)
@@ -182,15 +190,16 @@ static __device__ __forceinline__ int unit_exp(uint32_t bits, int mbits)
     return e - mbits;
 }
 
-// 24 terms per k-step: (A plane, B plane, accumulator, negate A).  Planes per
-// row block: 0 Re D, 1 Re l1, 2 Re l2, 3 Im D, 4 Im l1, 5 Im l2.  Accumulator
-// 0 / 1 = exact D*D Re / Im, 2 / 3 = the residual terms Re / Im.
-__constant__ int8_t dg_terms[24][4] = {
-    {0, 0, 0, 0}, {3, 3, 0, 0}, {0, 3, 1, 0}, {3, 0, 1, 1},
-    {0, 1, 2, 0}, {1, 0, 2, 0}, {1, 1, 2, 0}, {0, 2, 2, 0}, {2, 0, 2, 0},
-    {3, 4, 2, 0}, {4, 3, 2, 0}, {4, 4, 2, 0}, {3, 5, 2, 0}, {5, 3, 2, 0},
-    {0, 4, 3, 0}, {1, 3, 3, 0}, {1, 4, 3, 0}, {0, 5, 3, 0}, {2, 3, 3, 0},
-    {3, 1, 3, 1}, {4, 0, 3, 1}, {4, 1, 3, 1}, {3, 2, 3, 1}, {5, 0, 3, 1}};
+// 12 terms per k-step: (A plane as (level, part), first B plane of the pair, accumulator region).
+// A planes: level 0 D, 1 l1, 2 l2; part 0 Re, 1 Im (A layout index 2 level + part; a diagonal
+// pair reads its A planes from the B layout, index 3 level + part).  B pairs [Re partner | Im
+// partner]: 0 [Re D | Im D], 1 [Im D | -Re D], 3 [Re l1 | Im l1], 4 [Im l1 | -Re l1],
+// 6 [Re l2 | Im l2], 7 [Im l2 | -Re l2].  Region 0 = exact D*D (Re, Im), 1 = the residual terms.
+//   Re <x|y> = xr yr + xi yi,  Im <x|y> = xr yi - xi yr  (x from A, y from B)
+__constant__ int8_t dg_terms[12][4] = {
+    {0, 0, 0, 0}, {0, 1, 1, 0},                                  // D  x D
+    {0, 0, 3, 1}, {0, 0, 6, 1}, {1, 0, 0, 1}, {1, 0, 3, 1}, {2, 0, 0, 1},   // Re parts of A
+    {0, 1, 4, 1}, {0, 1, 7, 1}, {1, 1, 1, 1}, {1, 1, 4, 1}, {2, 1, 1, 1}};  // Im parts of A
 
 __global__ void __launch_bounds__(DG_THREADS, 1)
     dg_gram_kernel(const __grid_constant__ CUtensorMap tmap, int nbk, int64_t N, int64_t kchunk,
@@ -216,10 +225,6 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
     pair_of((int)(blockIdx.x % ntp), nbk, &mb, &nbo);
     const bool diag = (mb == nbo);
     const int nblk = diag ? 1 : 2;
-    // the last row block holds rows - 128 (nbk - 1) rows: its pairs use N = that count rounded up to 16
-    // (columns past N are neither computed nor written; the reduction reads only j < rows)
-    const int vlast = rows - 128 * (nbk - 1);
-    const int nN = (nbo == nbk - 1) ? ((vlast + 15) & ~15) : 128;
     const int64_t k0 = (int64_t)(blockIdx.x / ntp) * kchunk;
     int64_t k1 = k0 + kchunk;
     if (k1 > N) k1 = N;
@@ -285,7 +290,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
                 (void)bar_wait(smem_u32(&raw_full[u % DG_RAW_STAGES]), (u / DG_RAW_STAGES) & 1, deadline + DG_TIMEOUT_NS);
     } else if (warp == 1 && lane == 0) {
         // ---------- MMA issuer ----------
-        const uint32_t idp = idesc_f16(0, (uint32_t)nN), idn = idesc_f16(1, (uint32_t)nN);
+        const uint32_t id = idesc_f16(256);
         for (int kt = 0; kt < nk; kt++) {
             const int s = kt % DG_PL_STAGES;
             if (!bar_wait(smem_u32(&pl_full[s]), (kt / DG_PL_STAGES) & 1, deadline)) {
@@ -295,14 +300,16 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
             }
             if (abort_sh) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t pa = smem_u32(pl_base + s * 2 * 6 * DG_PLANE_BYTES);
-            const uint32_t pb = diag ? pa : pa + 6 * DG_PLANE_BYTES;
+            // stage: A planes at 0 (6 x 4 KiB), B planes at 6 planes (9 x 4 KiB); a diagonal pair
+            // keeps only the B layout and reads its A planes from it
+            const uint32_t st = smem_u32(pl_base + s * DG_PL_STAGE);
+            const uint32_t pb = st + (diag ? 0 : DG_PL_A * DG_PLANE_BYTES);
 #pragma unroll
-            for (int t = 0; t < 24; t++) {
-                const int a = dg_terms[t][0], b = dg_terms[t][1], acc = dg_terms[t][2], ng = dg_terms[t][3];
-                const uint32_t first = (kt == 0) && (t == 0 || t == 2 || t == 4 || t == 14);
-                umma(tmem + (uint32_t)acc * 128u, desc_sw32(pa + a * DG_PLANE_BYTES), desc_sw32(pb + b * DG_PLANE_BYTES),
-                     ng ? idn : idp, first ? 0u : 1u);
+            for (int t = 0; t < 12; t++) {
+                const int lv = dg_terms[t][0], pt = dg_terms[t][1], b = dg_terms[t][2], rg = dg_terms[t][3];
+                const uint32_t pa = diag ? pb + (3 * lv + pt) * DG_PLANE_BYTES : st + (2 * lv + pt) * DG_PLANE_BYTES;
+                const uint32_t first = (kt == 0) && (t == 0 || t == 2);
+                umma(tmem + (uint32_t)rg * 256u, desc_sw32(pa), desc_sw32(pb + b * DG_PLANE_BYTES), id, first ? 0u : 1u);
             }
             umma_commit(smem_u32(&pl_empty[s]));
         }
@@ -324,13 +331,14 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
             }
             if (abort_sh) break;
             const uint8_t* rawst = raw_base + rs * 2 * DG_RAW_BYTES;
-            uint8_t* plst = pl_base + ps * 2 * 6 * DG_PLANE_BYTES;
+            uint8_t* plst = pl_base + ps * DG_PL_STAGE;
             for (int b = 0; b < nblk; b++) {
                 const float* raw = reinterpret_cast<const float*>(rawst + b * DG_RAW_BYTES);
-                uint8_t* planes = plst + b * 6 * DG_PLANE_BYTES;
-                const int rlim = b == 1 ? nN : 128;   // the MMAs read N rows of the B block
+                // the B layout (9 planes) for the B block and for a diagonal pair's only block
+                const bool blay = diag || b == 1;
+                uint8_t* planes = plst + (diag ? 0 : b * DG_PL_A * DG_PLANE_BYTES);
 #pragma unroll 4
-                for (int rr = 4 * cw; rr < rlim; rr += 4 * DG_CONV_WARPS) {
+                for (int rr = 4 * cw; rr < 128; rr += 4 * DG_CONV_WARPS) {
                     const int r = rr + sub;
                     const float4 q = *reinterpret_cast<const float4*>(raw + r * 32 + 2 * kp);
                     const float iu = inv_u[b][r];
@@ -344,10 +352,19 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
                         const __half2 h1 = __floats2half2_rn(l0, l1);
                         const float2 f1 = __half22float2(h1);
                         const __half2 h2 = __floats2half2_rn(l0 - f1.x, l1 - f1.y);
-                        uint8_t* pD = planes + (c ? 3 : 0) * DG_PLANE_BYTES + off;
-                        *reinterpret_cast<__half2*>(pD) = __floats2half2_rn(d0, d1);
-                        *reinterpret_cast<__half2*>(pD + DG_PLANE_BYTES) = h1;
-                        *reinterpret_cast<__half2*>(pD + 2 * DG_PLANE_BYTES) = h2;
+                        const __half2 hd = __floats2half2_rn(d0, d1);
+                        // level l plane: A layout 2 l + c, B layout 3 l + c (+ the negated real part at 3 l + 2)
+                        const int ls = blay ? 3 : 2;
+                        uint8_t* pD = planes + c * DG_PLANE_BYTES + off;
+                        *reinterpret_cast<__half2*>(pD) = hd;
+                        *reinterpret_cast<__half2*>(pD + ls * DG_PLANE_BYTES) = h1;
+                        *reinterpret_cast<__half2*>(pD + 2 * ls * DG_PLANE_BYTES) = h2;
+                        if (blay && c == 0) {
+                            uint8_t* pN = planes + 2 * DG_PLANE_BYTES + off;
+                            *reinterpret_cast<__half2*>(pN) = __hneg2(hd);
+                            *reinterpret_cast<__half2*>(pN + 3 * DG_PLANE_BYTES) = __hneg2(h1);
+                            *reinterpret_cast<__half2*>(pN + 6 * DG_PLANE_BYTES) = __hneg2(h2);
+                        }
                     }
                 }
             }
@@ -369,10 +386,9 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
             const uint32_t lanebase = tmem + ((uint32_t)(quad * 32) << 16);
             for (int ri = 0; ri < 2; ri++) {
                 for (int c = 2 * half; c < 2 * half + 2; c++) {
-                    if (c * 32 >= nN) continue;
                     tmem_ld32(lanebase + ri * 128 + c * 32, hh);
                     tmem_ld32(lanebase + 256 + ri * 128 + c * 32, rsd);
-                    if (diag && ri == 0 && c == (row >> 5) && row < nN && hh[row & 31] > 8388608.0f)
+                    if (diag && ri == 0 && c == (row >> 5) && hh[row & 31] > 8388608.0f)
                         atomicExch(err, DG_ERR_INEXACT);
                     float4* o = reinterpret_cast<float4*>(out + ri * 128 * 128 + row * 128 + c * 32);
 #pragma unroll
