@@ -292,7 +292,8 @@ def run_gb300(args, ws, rank, local):
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         try:
-            traffic = json.load(open(tp)).get(dom)
+            tj = json.load(open(tp))
+            traffic = tj.get(dom) if tj.get("workload") == workload else None   # measured for this workload only
         except Exception:
             traffic = None
     if dom == "passes":

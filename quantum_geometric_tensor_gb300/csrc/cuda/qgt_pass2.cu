@@ -330,6 +330,10 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
     // the pass program and each op's coefficients, staged once per CTA
     qgt_dev_op2_t* sops = reinterpret_cast<qgt_dev_op2_t*>(p2_smem + ((size_t)sizeof(T) << (5 + RB + 3)));
     R* scoef = reinterpret_cast<R*>(sops + a.nops);
+    // this CTA's vector entry runs the pass program from its start op (a Q2_SEG; a derivative
+    // spawned after a checkpoint starts at its segment); ops keep their program indices
+    const int start = a.entries[blockIdx.y].start_op;
+
     // per SEG op: its layout's local bits [0, 16) and their physical qubits [16, 32)
     int8_t* sseg = reinterpret_cast<int8_t*>(scoef + 8 * a.nops);
     // generator matrices (-i/2) X, (-i/2) Y, (-i/2) Z (2 x 2 complex, row-major)
@@ -354,16 +358,21 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
         }
         const R* ctab = ((sizeof(R) == 4) ? reinterpret_cast<const R*>(a.coef32) : reinterpret_cast<const R*>(a.coef)) +
                         (int64_t)8 * blockIdx.z * a.coef_stride;
-        for (int i = threadIdx.x; i < a.nops; i += blockDim.x) sops[i] = a.ops[i];
-        for (int i = threadIdx.x; i < 8 * a.nops; i += blockDim.x) {
+        for (int i = start + threadIdx.x; i < a.nops; i += blockDim.x) sops[i] = a.ops[i];
+        for (int i = 8 * start + threadIdx.x; i < 8 * a.nops; i += blockDim.x) {
             const int c = a.ops[i >> 3].coef;
             scoef[i] = c >= 0 ? ctab[8 * c + (i & 7)] : (((i & 7) == 0 || (i & 7) == 6) ? (R)1 : (R)0);   // identity
         }
-        for (int i = threadIdx.x; i < 32 * a.nops; i += blockDim.x) {
+        for (int i = 32 * start + threadIdx.x; i < 32 * a.nops; i += blockDim.x) {
             const qgt_dev_op2_t o = a.ops[i >> 5];
             if (o.kind != Q2_SEG) continue;
             const int8_t lb = a.segs[16 * o.seg + (i & 15)];
             sseg[i] = (i & 16) ? ((lb >= 0 && lb < 16) ? a.local_to_phys[lb] : (int8_t)0) : lb;
+        }
+        if (start > 0 && threadIdx.x < 32) {
+            // the starting segment's layout also in slot 0 (the initial layout of every entry)
+            const int8_t lb = a.segs[16 * a.ops[start].seg + (threadIdx.x & 15)];
+            sseg[threadIdx.x] = (threadIdx.x & 16) ? ((lb >= 0 && lb < 16) ? a.local_to_phys[lb] : (int8_t)0) : lb;
         }
         __syncthreads();
     }
@@ -456,7 +465,7 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
             else v[j] = src[ph];
         }
     }
-    for (int pc = 1; pc < a.nops; pc++) {
+    for (int pc = start + 1; pc < a.nops; pc++) {
         const qgt_dev_op2_t op = sops[pc];
         R m[8];
         if (op.kind == Q2_SEG) {

@@ -40,7 +40,7 @@
 #define E_HW (-6)
 
 /* role encoding of register-resident programs (see qgt_dev_op2_t) */
-#define QGT_CKPT_GROUPS 16
+#define QGT_CKPT_GROUPS 32
 #define RL_REG_ 8
 #define RL_WARP_ 16
 #define RL_OUT_ 32
@@ -63,8 +63,8 @@ typedef struct {
     int part;                     /* 0 forward (with first-half slots); meet in the middle: 1 psi forward, 2 backward */
     int op_begin, op_count;
     int ent_begin, ent_count;
-    /* segment checkpoints (build_checkpoints): entry 0 writes them (launched first, alone); entries
-     * [grp_begin[g], + grp_count[g]) run the program from its op grp_start[g] (a Q2_SEG) */
+    /* segment checkpoints (build_checkpoints): entry 0 writes them (launched first, alone); the
+     * entries [grp_begin[g], + grp_count[g]) start at op grp_start[g] (a Q2_SEG) from checkpoint g */
     int ckpt_writer;
     int ngrp;
     int grp_begin[QGT_CKPT_GROUPS], grp_count[QGT_CKPT_GROUPS], grp_start[QGT_CKPT_GROUPS];
@@ -1053,7 +1053,7 @@ static int build_checkpoints(qgt_plan_t* p)
                 if (a == wi || startof[a] != sp) continue;
                 qgt_dev_entry_t e = src[a];
                 e.src_row = base_row + ckrow[sp];
-                e.spawn_op -= sp;
+                e.start_op = sp;
                 e.flags &= ~QENT_SRC_ZERO;
                 ne[out++] = e;
             }
@@ -1643,22 +1643,10 @@ static int run_step(qgt_plan_t* p)
                 if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) return rc;
                 b.ckpt = 0;
                 launches++;
-                const int rest = (ps->ngrp > 0 ? ps->grp_begin[0] : nall) - 1;
+                /* every other entry in one launch; each runs the program from its start op */
                 b.entries = a.entries + 1;
-                b.nentries = rest;
-                if (rest > 0) {
-                    if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) return rc;
-                    launches++;
-                }
-                for (int g = 0; g < ps->ngrp; g++) {
-                    b.ops = p->prog_d + ps->prog_begin + ps->grp_start[g];
-                    b.nops = ps->prog_count - ps->grp_start[g];
-                    b.entries = a.entries + ps->grp_begin[g];
-                    b.nentries = ps->grp_count[g];
-                    if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) return rc;
-                    launches++;
-                }
-                launches--;   /* counted once below */
+                b.nentries = nall - 1;
+                if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) return rc;
             } else if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) {
                 return rc;
             }

@@ -75,7 +75,8 @@ typedef struct {
     int32_t spawn_op;   /* op index (in the pass) after which (-i/2)G is inserted; -1 = transport */
     int32_t flags;      /* QENT_* */
     int32_t split_row;
-    int32_t pad;
+    int32_t start_op;   /* register-resident passes: the entry runs the pass program from this op (a
+                           Q2_SEG) on; 0 = the whole program */
 } qgt_dev_entry_t;
 
 typedef struct {
