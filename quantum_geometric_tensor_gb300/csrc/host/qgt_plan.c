@@ -119,6 +119,11 @@ struct qgt_plan {
     /* device */
     void* stream;
     void* graph;
+    /* passes with a checkpoint writer fork onto aux_stream (the writer, then the spawns that start
+     * from its checkpoints) while the other entries run on stream; joined at the pass end */
+    void* aux_stream;
+    void* ev_fork;
+    void* ev_join;
     void* V;
     void* split;
     qgt_dev_op_t* ops_d;
@@ -1312,6 +1317,12 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
     if (host_only) { *out = p; return 0; }
     if ((rc = qgt_dev_set_device(p->opt.device)) != 0) goto fail;
     if ((rc = qgt_dev_stream_create(&p->stream)) != 0) goto fail;
+    for (int k = 0; k < p->npasses; k++)
+        if (p->passes[k].ckpt_writer && !p->aux_stream) {
+            if ((rc = qgt_dev_stream_create(&p->aux_stream)) != 0) goto fail;
+            if ((rc = qgt_dev_event_create(&p->ev_fork)) != 0) goto fail;
+            if ((rc = qgt_dev_event_create(&p->ev_join)) != 0) goto fail;
+        }
     {
         size_t ab = p->fp64 ? 16 : 8;
         DALLOC(p->V, (size_t)p->B * (size_t)p->pstride * ab);
@@ -1466,6 +1477,12 @@ void qgt_plan_destroy(qgt_plan_t* p)
     }
     if (p->stream) qgt_dev_stream_sync(p->stream);
     qgt_dev_graph_destroy(p->graph);
+    if (p->aux_stream) {
+        qgt_dev_stream_sync(p->aux_stream);
+        qgt_dev_stream_destroy(p->aux_stream);
+    }
+    qgt_dev_event_destroy(p->ev_fork);
+    qgt_dev_event_destroy(p->ev_join);
     qgt_dev_tc_gram_destroy(p->tc);
     qgt_dev_dg_gram_destroy(p->dg);
     qgt_dev_free(p->rowmax_d);
@@ -1635,18 +1652,31 @@ static int run_step(qgt_plan_t* p)
             b.point_stride = a.point_stride;
             b.rowmax_stride = a.rowmax_stride;
             if (ps->ckpt_writer) {
-                /* the checkpoint writer first, then the entries that run the whole program, then
-                 * the spawns from each checkpoint on the program from that segment */
+                /* fork: the checkpoint writer and then the spawns that start from its checkpoints
+                 * (each from its own segment of the program) on the auxiliary stream, the entries
+                 * that need no checkpoint on the main stream; join */
                 const int nall = b.nentries;
+                const int c0 = ps->ngrp > 0 ? ps->grp_begin[0] : nall;
+                if ((rc = qgt_dev_event_record(p->ev_fork, p->stream)) != 0) return rc;
+                if ((rc = qgt_dev_stream_wait_event(p->aux_stream, p->ev_fork)) != 0) return rc;
                 b.nentries = 1;
                 b.ckpt = 1;
-                if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) return rc;
+                if ((rc = qgt_dev_pass2(&b, p->fp64, p->aux_stream)) != 0) return rc;
                 b.ckpt = 0;
-                launches++;
-                /* every other entry in one launch; each runs the program from its start op */
-                b.entries = a.entries + 1;
-                b.nentries = nall - 1;
-                if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) return rc;
+                if (c0 < nall) {
+                    b.entries = a.entries + c0;
+                    b.nentries = nall - c0;
+                    if ((rc = qgt_dev_pass2(&b, p->fp64, p->aux_stream)) != 0) return rc;
+                    launches++;
+                }
+                if (c0 > 1) {
+                    b.entries = a.entries + 1;
+                    b.nentries = c0 - 1;
+                    if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) return rc;
+                    launches++;
+                }
+                if ((rc = qgt_dev_event_record(p->ev_join, p->aux_stream)) != 0) return rc;
+                if ((rc = qgt_dev_stream_wait_event(p->stream, p->ev_join)) != 0) return rc;
             } else if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) {
                 return rc;
             }
