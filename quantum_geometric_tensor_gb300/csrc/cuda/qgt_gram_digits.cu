@@ -424,48 +424,66 @@ static __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x
     lo = __fadd_rn(lo, err);
 }
 
-__global__ void dg_reduce_kernel(const float* __restrict__ part, const uint32_t* __restrict__ rowmax, int rows, int nbk,
-                                 int ntp, int nsplit, int mbits, double2* __restrict__ HG)
+// HG_ij for 32 consecutive j of row i (blockIdx.x = j chunk, blockIdx.y = i, blockIdx.z = point): warp w
+// sums the K ranges s = w (mod 8) as FP32 double-float (TwoSum) pairs, four of them for independent
+// loads; the 8 warps' pairs are added in FP64 in a fixed order (deterministic).  FP64 conversions and
+// adds are scarce on this part, so only the final pairs go to FP64.
+__global__ void __launch_bounds__(256) dg_reduce_kernel(const float* __restrict__ part, const uint32_t* __restrict__ rowmax,
+                                                         int rows, int nbk, int ntp, int nsplit, int mbits,
+                                                         double2* __restrict__ HG)
 {
-    part += (int64_t)blockIdx.y * nsplit * ntp * (2 * 128 * 128);   // parameter point
-    rowmax += (int64_t)blockIdx.y * rows;
-    HG += (int64_t)blockIdx.y * rows * rows;
-    int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)rows * rows) return;
-    int i = (int)(idx / rows), j = (int)(idx % rows);
-    if (i > j) return;
-    int ti = i >> 7, tj = j >> 7;
-    int tp = ti * nbk - ti * (ti - 1) / 2 + (tj - ti);
-    int64_t off = (int64_t)(i & 127) * 128 + (j & 127);
-    // double-float sums in FP32 (TwoSum: the high part and the accumulated
-    // rounding errors), four of them for independent loads; FP64 conversions
-    // and adds are scarce on this part, so only the final pairs go to FP64
-    float rh[4] = {0, 0, 0, 0}, rl[4] = {0, 0, 0, 0}, ih[4] = {0, 0, 0, 0}, il[4] = {0, 0, 0, 0};
+    __shared__ float red[4][8][33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int i = blockIdx.y, j = blockIdx.x * 32 + lane;
+    if (blockIdx.x * 32 + 31 < i) return;   // the whole chunk is below the diagonal
+    part += (int64_t)blockIdx.z * nsplit * ntp * (2 * 128 * 128);   // parameter point
+    rowmax += (int64_t)blockIdx.z * rows;
+    HG += (int64_t)blockIdx.z * rows * rows;
+    const bool live = j < rows && j >= i;
+    const int jj = live ? j : i;
+    const int ti = i >> 7, tj = jj >> 7;
+    const int tp = ti * nbk - ti * (ti - 1) / 2 + (tj - ti);
+    const int64_t off = (int64_t)(i & 127) * 128 + (jj & 127);
     const int64_t sstride = (int64_t)ntp * (2 * 128 * 128);
     const float* b0 = part + (int64_t)tp * (2 * 128 * 128) + off;
-    int s = 0;
-    for (; s + 4 <= nsplit; s += 4) {
+    float rh[4] = {0, 0, 0, 0}, rl[4] = {0, 0, 0, 0}, ih[4] = {0, 0, 0, 0}, il[4] = {0, 0, 0, 0};
+    int s = w;
+    for (; s + 24 < nsplit; s += 32) {
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            const float* b = b0 + (int64_t)(s + u) * sstride;
+            const float* b = b0 + (int64_t)(s + 8 * u) * sstride;
             two_sum_acc(rh[u], rl[u], __ldg(b));
             two_sum_acc(ih[u], il[u], __ldg(b + 128 * 128));
         }
     }
-    for (; s < nsplit; s++) {
+    for (; s < nsplit; s += 8) {
         const float* b = b0 + (int64_t)s * sstride;
         two_sum_acc(rh[0], rl[0], __ldg(b));
         two_sum_acc(ih[0], il[0], __ldg(b + 128 * 128));
     }
-    double re = 0, im = 0;
+    // fold the four pairs (FP32 TwoSum), then hand the warp's pair to the block
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-        re += (double)rh[u] + (double)rl[u];
-        im += (double)ih[u] + (double)il[u];
+    for (int u = 1; u < 4; u++) {
+        two_sum_acc(rh[0], rl[0], rh[u]);
+        rl[0] += rl[u];
+        two_sum_acc(ih[0], il[0], ih[u]);
+        il[0] += il[u];
     }
-    double uu = ldexp(1.0, unit_exp(rowmax[i], mbits) + unit_exp(rowmax[j], mbits));
-    HG[(int64_t)i * rows + j] = make_double2(re * uu, im * uu);
-    HG[(int64_t)j * rows + i] = make_double2(re * uu, -im * uu);
+    red[0][w][lane] = rh[0];
+    red[1][w][lane] = rl[0];
+    red[2][w][lane] = ih[0];
+    red[3][w][lane] = il[0];
+    __syncthreads();
+    if (w == 0 && live) {
+        double re = 0, im = 0;
+        for (int q = 0; q < 8; q++) {
+            re += (double)red[0][q][lane] + (double)red[1][q][lane];
+            im += (double)red[2][q][lane] + (double)red[3][q][lane];
+        }
+        const double uu = ldexp(1.0, unit_exp(rowmax[i], mbits) + unit_exp(rowmax[j], mbits));
+        HG[(int64_t)i * rows + j] = make_double2(re * uu, im * uu);
+        HG[(int64_t)j * rows + i] = make_double2(re * uu, -im * uu);
+    }
 }
 
 static PFN_cuTensorMapEncodeTiled_v12000 dg_encode(void)
@@ -487,7 +505,7 @@ extern "C" int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, co
     *out = NULL;
     if (N % DG_BK || rows < 1 || ((uintptr_t)V & 15))
         return qgt_set_error(-1, "digit gram: row length %lld must be a multiple of %d", (long long)N, DG_BK);
-    if (npoints < 1 || npoints > 65535 || point_rows < rows)
+    if (npoints < 1 || npoints > 65535 || point_rows < rows || rows > 65535)
         return qgt_set_error(-1, "digit gram: %d points of %d rows (stride %d rows)", npoints, rows, point_rows);
     if (2 * N > 0x7fffffffLL) return qgt_set_error(-1, "digit gram: row length too large for TMA coordinates");
     PFN_cuTensorMapEncodeTiled_v12000 enc = dg_encode();
@@ -556,9 +574,8 @@ extern "C" int qgt_dev_dg_gram_run(qgt_dg_gram_t* g, double* HG, void* stream)
                                                                        g->rows, g->mbits, g->part, g->err);
     int rc = qgt_dev_last_error();
     if (rc) return rc;
-    int64_t cnt = (int64_t)g->rows * g->rows;
-    dg_reduce_kernel<<<dim3((unsigned)((cnt + 255) / 256), g->npoints), 256, 0, s>>>(g->part, g->rowmax, g->rows, g->nbk, g->ntp, g->nsplit,
-                                                                   g->mbits, (double2*)HG);
+    dg_reduce_kernel<<<dim3((unsigned)((g->rows + 31) / 32), (unsigned)g->rows, g->npoints), 256, 0, s>>>(
+        g->part, g->rowmax, g->rows, g->nbk, g->ntp, g->nsplit, g->mbits, (double2*)HG);
     return qgt_dev_last_error();
 }
 
