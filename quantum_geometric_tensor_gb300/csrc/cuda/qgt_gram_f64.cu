@@ -118,8 +118,9 @@ extern "C" int qgt_dev_gram_f64(const void* V, int64_t N, int32_t rows, double* 
 // ---------------------------------------------------------------------------
 // Small Gram: rows <= 8 (a few vectors per point, e.g. psi and two derivative
 // slots of a Berry-curvature point).  Memory-bound: every thread reads its
-// amplitudes of all rows once and keeps the rows (rows + 1) / 2 products in
-// FP64 registers (complex64 inputs multiply exactly in FP64).  Block sums go
+// amplitudes of all rows once and keeps the rows (rows + 1) / 2 sums in FP64
+// registers (complex128 rows: FP64 products; complex64 rows: FP32 sums of
+// short blocks, gram_small32_kernel below).  Block sums go
 // to part[point][split][pair]; a second kernel adds the splits and writes the
 // Hermitian HG of each point.
 // ---------------------------------------------------------------------------
@@ -150,6 +151,68 @@ __global__ void __launch_bounds__(256) gram_small_kernel(const T* __restrict__ V
                 acc[p].x += xr[i] * xr[j] + xi[i] * xi[j];
                 acc[p].y += xr[i] * xi[j] - xi[i] * xr[j];
             }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int p = 0; p < NP; p++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            acc[p].x += __shfl_xor_sync(0xffffffffu, acc[p].x, o);
+            acc[p].y += __shfl_xor_sync(0xffffffffu, acc[p].y, o);
+        }
+        if (lane == 0) red[warp][p] = acc[p];
+    }
+    __syncthreads();
+    if (threadIdx.x < NP) {
+        double2 s = make_double2(0, 0);
+        for (int w = 0; w < 8; w++) { s.x += red[w][threadIdx.x].x; s.y += red[w][threadIdx.x].y; }
+        part[((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * NP + threadIdx.x] = s;
+    }
+}
+
+// complex64 rows: the products and sums of SB consecutive grid-stride
+// amplitudes of a thread run in FP32 (FMA), and each block sum is added to an
+// FP64 accumulator.  FP64 work drops SB-fold (GB300 issues about one FP64 FMA
+// per 64 FP32 FMAs), which leaves the kernel bound by HBM; the rounding of a
+// 32-term FP32 block adds about 2^-24 sqrt(32 / N) to an entry of unit
+// vectors, far below the complex64 amplitudes' own error.
+template <int ROWS, int SB>
+__global__ void __launch_bounds__(256) gram_small32_kernel(const float2* __restrict__ V, int64_t N, int64_t point_stride,
+                                                           double2* __restrict__ part)
+{
+    constexpr int NP = ROWS * (ROWS + 1) / 2;
+    __shared__ double2 red[8][NP];
+    V += blockIdx.y * point_stride;
+    double2 acc[NP];
+#pragma unroll
+    for (int p = 0; p < NP; p++) acc[p] = make_double2(0, 0);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t k0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k0 < N; k0 += SB * stride) {
+        float2 sb[NP];
+#pragma unroll
+        for (int p = 0; p < NP; p++) sb[p] = make_float2(0.f, 0.f);
+        constexpr int UN = ROWS <= 4 ? 4 : 1;   /* loads in flight vs registers of the sums */
+#pragma unroll UN
+        for (int t = 0; t < SB; t++) {
+            const int64_t k = k0 + t * stride;
+            if (k < N) {
+                float2 x[ROWS];
+#pragma unroll
+                for (int r = 0; r < ROWS; r++) x[r] = V[(int64_t)r * N + k];
+                int p = 0;
+#pragma unroll
+                for (int i = 0; i < ROWS; i++)
+#pragma unroll
+                    for (int j = i; j < ROWS; j++, p++) {
+                        sb[p].x = fmaf(x[i].x, x[j].x, fmaf(x[i].y, x[j].y, sb[p].x));
+                        sb[p].y = fmaf(x[i].x, x[j].y, fmaf(-x[i].y, x[j].x, sb[p].y));
+                    }
+            }
+        }
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            acc[p].x += (double)sb[p].x;
+            acc[p].y += (double)sb[p].y;
+        }
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -208,8 +271,23 @@ extern "C" int qgt_dev_gram_small(const void* V, int64_t N, int32_t rows, int32_
     if (rows < 1 || rows > 8 || nsplit < 1 || nsplit > 65535 || npoints < 1 || npoints > 65535)
         return qgt_set_error(-1, "gram_small: %d rows, %d splits, %d points", rows, nsplit, npoints);
     cudaStream_t s = (cudaStream_t)stream;
-    if (fp64) gram_small_launch<double2>(V, N, rows, nsplit, (double2*)part, npoints, point_stride, s);
-    else gram_small_launch<float2>(V, N, rows, nsplit, (double2*)part, npoints, point_stride, s);
+    if (fp64) {
+        gram_small_launch<double2>(V, N, rows, nsplit, (double2*)part, npoints, point_stride, s);
+    } else {
+        dim3 g((unsigned)nsplit, (unsigned)npoints);
+        const float2* v = (const float2*)V;
+        double2* pt = (double2*)part;
+        switch (rows) {
+        case 1: gram_small32_kernel<1, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
+        case 2: gram_small32_kernel<2, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
+        case 3: gram_small32_kernel<3, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
+        case 4: gram_small32_kernel<4, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
+        case 5: gram_small32_kernel<5, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
+        case 6: gram_small32_kernel<6, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
+        case 7: gram_small32_kernel<7, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
+        default: gram_small32_kernel<8, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
+        }
+    }
     int rc = qgt_dev_last_error();
     if (rc) return rc;
     gram_small_reduce_kernel<<<npoints, 64, 0, s>>>((const double2*)part, rows, nsplit, (double2*)HG);

@@ -316,8 +316,8 @@ int qgt_dev_cholesky_refined_launches(int32_t P);
  * (A: nsys x P x P, b / x: nsys x P, work: nsys x P x P, status: nsys x 2) */
 int qgt_dev_cholesky_batch(const double* A, int complex_input, const double* b, int32_t P, double lambda,
                            double* work, double* x, double* status, int32_t nsys, void* stream);
-/* small Gram (rows <= 8) of complex64 (fp64 = 0) or complex128 rows, FP64
- * sums: HG per point (npoints points point_stride amplitudes apart); part
+/* small Gram (rows <= 8) of complex64 (fp64 = 0; FP32 sums of 32-amplitude
+ * blocks, added in FP64) or complex128 rows (FP64): HG per point (npoints points point_stride amplitudes apart); part
  * holds npoints x nsplit x 36 complex partials */
 int qgt_dev_gram_small(const void* V, int64_t N, int32_t rows, int32_t fp64, double* part, int32_t nsplit,
                        double* HG, int32_t npoints, int64_t point_stride, void* stream);
