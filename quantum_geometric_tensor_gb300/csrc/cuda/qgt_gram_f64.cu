@@ -126,7 +126,7 @@ extern "C" int qgt_dev_gram_f64(const void* V, int64_t N, int32_t rows, double* 
 // ---------------------------------------------------------------------------
 template <typename T, int ROWS>
 __global__ void __launch_bounds__(256) gram_small_kernel(const T* __restrict__ V, int64_t N, int64_t point_stride,
-                                                         double2* __restrict__ part)
+                                                         int skip, double2* __restrict__ part)
 {
     constexpr int NP = ROWS * (ROWS + 1) / 2;
     __shared__ double2 red[8][NP];
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(256) gram_small_kernel(const T* __restrict__ V
         double xr[ROWS], xi[ROWS];
 #pragma unroll
         for (int r = 0; r < ROWS; r++) {
-            T v = V[(int64_t)r * N + k];
+            T v = V[(int64_t)(r + (r > 0 ? skip : 0)) * N + k];
             xr[r] = (double)v.x;
             xi[r] = (double)v.y;
         }
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(256) gram_small_kernel(const T* __restrict__ V
 // vectors, far below the complex64 amplitudes' own error.
 template <int ROWS, int SB>
 __global__ void __launch_bounds__(256) gram_small32_kernel(const float2* __restrict__ V, int64_t N, int64_t point_stride,
-                                                           double2* __restrict__ part)
+                                                           int skip, double2* __restrict__ part)
 {
     constexpr int NP = ROWS * (ROWS + 1) / 2;
     __shared__ double2 red[8][NP];
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(256) gram_small32_kernel(const float2* __restr
             if (k < N) {
                 float2 x[ROWS];
 #pragma unroll
-                for (int r = 0; r < ROWS; r++) x[r] = V[(int64_t)r * N + k];
+                for (int r = 0; r < ROWS; r++) x[r] = V[(int64_t)(r + (r > 0 ? skip : 0)) * N + k];
                 int p = 0;
 #pragma unroll
                 for (int i = 0; i < ROWS; i++)
@@ -231,72 +231,89 @@ __global__ void __launch_bounds__(256) gram_small32_kernel(const float2* __restr
     }
 }
 
-__global__ void gram_small_reduce_kernel(const double2* __restrict__ part, int rows, int nsplit, double2* __restrict__ HG)
+// HG (rows x rows) of each point from the splits' sums over the rows read
+// (row 1 skipped when skip = 1: its entries are written as zeros)
+__global__ void gram_small_reduce_kernel(const double2* __restrict__ part, int rows, int skip, int nsplit,
+                                         double2* __restrict__ HG)
 {
-    const int np = rows * (rows + 1) / 2;
+    const int rr = rows - skip;   // rows read
+    const int np = rr * (rr + 1) / 2;
+    HG += (int64_t)blockIdx.x * rows * rows;
+    if (skip)
+        for (int t = threadIdx.x; t < rows; t += blockDim.x) {
+            HG[rows + t] = make_double2(0, 0);
+            HG[(int64_t)t * rows + 1] = make_double2(0, 0);
+        }
     const int p = threadIdx.x;
     if (p >= np) return;
     part += (int64_t)blockIdx.x * nsplit * np;
-    HG += (int64_t)blockIdx.x * rows * rows;
     int i = 0, rem = p;
-    while (rem >= rows - i) { rem -= rows - i; i++; }
-    const int j = i + rem;
+    while (rem >= rr - i) { rem -= rr - i; i++; }
+    int j = i + rem;
     double2 s = make_double2(0, 0);
     for (int sp = 0; sp < nsplit; sp++) { s.x += part[(int64_t)sp * np + p].x; s.y += part[(int64_t)sp * np + p].y; }
+    if (i > 0) i += skip;
+    if (j > 0) j += skip;
     HG[(int64_t)i * rows + j] = s;
     HG[(int64_t)j * rows + i] = make_double2(s.x, -s.y);
 }
 
 template <typename T>
-static void gram_small_launch(const void* V, int64_t N, int rows, int nsplit, double2* part, int npoints, int64_t ps,
-                              cudaStream_t s)
+static void gram_small_launch(const void* V, int64_t N, int rows, int skip, int nsplit, double2* part, int npoints,
+                              int64_t ps, cudaStream_t s)
 {
     dim3 g((unsigned)nsplit, (unsigned)npoints);
     const T* v = (const T*)V;
     switch (rows) {
-    case 1: gram_small_kernel<T, 1><<<g, 256, 0, s>>>(v, N, ps, part); break;
-    case 2: gram_small_kernel<T, 2><<<g, 256, 0, s>>>(v, N, ps, part); break;
-    case 3: gram_small_kernel<T, 3><<<g, 256, 0, s>>>(v, N, ps, part); break;
-    case 4: gram_small_kernel<T, 4><<<g, 256, 0, s>>>(v, N, ps, part); break;
-    case 5: gram_small_kernel<T, 5><<<g, 256, 0, s>>>(v, N, ps, part); break;
-    case 6: gram_small_kernel<T, 6><<<g, 256, 0, s>>>(v, N, ps, part); break;
-    case 7: gram_small_kernel<T, 7><<<g, 256, 0, s>>>(v, N, ps, part); break;
-    default: gram_small_kernel<T, 8><<<g, 256, 0, s>>>(v, N, ps, part); break;
+    case 1: gram_small_kernel<T, 1><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
+    case 2: gram_small_kernel<T, 2><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
+    case 3: gram_small_kernel<T, 3><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
+    case 4: gram_small_kernel<T, 4><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
+    case 5: gram_small_kernel<T, 5><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
+    case 6: gram_small_kernel<T, 6><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
+    case 7: gram_small_kernel<T, 7><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
+    default: gram_small_kernel<T, 8><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
     }
 }
 
-extern "C" int qgt_dev_gram_small(const void* V, int64_t N, int32_t rows, int32_t fp64, double* part, int32_t nsplit,
-                                  double* HG, int32_t npoints, int64_t point_stride, void* stream)
+static void gram_small32_launch(const void* V, int64_t N, int rows, int skip, int nsplit, double2* part, int npoints,
+                                int64_t ps, cudaStream_t s)
 {
-    if (rows < 1 || rows > 8 || nsplit < 1 || nsplit > 65535 || npoints < 1 || npoints > 65535)
-        return qgt_set_error(-1, "gram_small: %d rows, %d splits, %d points", rows, nsplit, npoints);
-    cudaStream_t s = (cudaStream_t)stream;
-    if (fp64) {
-        gram_small_launch<double2>(V, N, rows, nsplit, (double2*)part, npoints, point_stride, s);
-    } else {
-        dim3 g((unsigned)nsplit, (unsigned)npoints);
-        const float2* v = (const float2*)V;
-        double2* pt = (double2*)part;
-        switch (rows) {
-        case 1: gram_small32_kernel<1, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
-        case 2: gram_small32_kernel<2, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
-        case 3: gram_small32_kernel<3, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
-        case 4: gram_small32_kernel<4, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
-        case 5: gram_small32_kernel<5, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
-        case 6: gram_small32_kernel<6, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
-        case 7: gram_small32_kernel<7, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
-        default: gram_small32_kernel<8, 32><<<g, 256, 0, s>>>(v, N, point_stride, pt); break;
-        }
+    dim3 g((unsigned)nsplit, (unsigned)npoints);
+    const float2* v = (const float2*)V;
+    switch (rows) {
+    case 1: gram_small32_kernel<1, 32><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
+    case 2: gram_small32_kernel<2, 32><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
+    case 3: gram_small32_kernel<3, 32><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
+    case 4: gram_small32_kernel<4, 32><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
+    case 5: gram_small32_kernel<5, 32><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
+    case 6: gram_small32_kernel<6, 32><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
+    case 7: gram_small32_kernel<7, 32><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
+    default: gram_small32_kernel<8, 32><<<g, 256, 0, s>>>(v, N, ps, skip, part); break;
     }
+}
+
+extern "C" int qgt_dev_gram_small(const void* V, int64_t N, int32_t rows, int32_t skip_row1, int32_t fp64, double* part,
+                                  int32_t nsplit, double* HG, int32_t npoints, int64_t point_stride, void* stream)
+{
+    if (rows < 1 || rows > 8 || nsplit < 1 || nsplit > 65535 || npoints < 1 || npoints > 65535 ||
+        (skip_row1 != 0 && skip_row1 != 1) || (skip_row1 && rows < 2))
+        return qgt_set_error(-1, "gram_small: %d rows (skip %d), %d splits, %d points", rows, skip_row1, nsplit,
+                             npoints);
+    cudaStream_t s = (cudaStream_t)stream;
+    const int rr = rows - skip_row1;
+    if (fp64) gram_small_launch<double2>(V, N, rr, skip_row1, nsplit, (double2*)part, npoints, point_stride, s);
+    else gram_small32_launch(V, N, rr, skip_row1, nsplit, (double2*)part, npoints, point_stride, s);
     int rc = qgt_dev_last_error();
     if (rc) return rc;
-    gram_small_reduce_kernel<<<npoints, 64, 0, s>>>((const double2*)part, rows, nsplit, (double2*)HG);
+    gram_small_reduce_kernel<<<npoints, 64, 0, s>>>((const double2*)part, rows, skip_row1, nsplit, (double2*)HG);
     return qgt_dev_last_error();
 }
 
 // ---------------------------------------------------------------------------
 // Overlaps <V + a_off[k] | V + b_off[k]> of rows of N amplitudes (offsets in
-// amplitudes), FP64 sums: Berry phases around loops and plaquette links on
+// amplitudes), FP64 sums (complex64 rows: FP32 sums of 32-term blocks added in
+// FP64): Berry phases around loops and plaquette links on
 // parameter lattices.  Pair k is split over nchunk CTAs (block k * nchunk + c
 // sums the amplitudes [c len, (c + 1) len)); part[k * nchunk + c] receives
 // the partial sums, which the caller adds in a fixed order.
@@ -312,10 +329,28 @@ __global__ void __launch_bounds__(256) overlap_kernel(const T* __restrict__ V, i
     const T* b = V + b_off[k];
     const int64_t lo = c * len, hi = lo + len < N ? lo + len : N;
     double re = 0, im = 0;
-    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-        const T x = a[i], y = b[i];
-        re += (double)x.x * y.x + (double)x.y * y.y;
-        im += (double)x.x * y.y - (double)x.y * y.x;
+    if constexpr (sizeof(T) == 16) {
+        for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+            const T x = a[i], y = b[i];
+            re += (double)x.x * y.x + (double)x.y * y.y;
+            im += (double)x.x * y.y - (double)x.y * y.x;
+        }
+    } else {
+        // complex64: FP32 sums of 32 consecutive strided terms, added in FP64 (as in gram_small32_kernel)
+        for (int64_t i0 = lo + threadIdx.x; i0 < hi; i0 += 32 * (int64_t)blockDim.x) {
+            float sr = 0.f, si = 0.f;
+#pragma unroll 8
+            for (int t = 0; t < 32; t++) {
+                const int64_t i = i0 + t * (int64_t)blockDim.x;
+                if (i < hi) {
+                    const T x = a[i], y = b[i];
+                    sr = fmaf(x.x, y.x, fmaf(x.y, y.y, sr));
+                    si = fmaf(x.x, y.y, fmaf(-x.y, y.x, si));
+                }
+            }
+            re += (double)sr;
+            im += (double)si;
+        }
     }
     for (int o = 16; o > 0; o >>= 1) {
         re += __shfl_xor_sync(0xffffffffu, re, o);

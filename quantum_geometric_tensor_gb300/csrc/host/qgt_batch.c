@@ -11,8 +11,10 @@
  *     dimension of every kernel, so a group costs one launch per kernel;
  *   - a Berry map Omega_ab = Im Q_ab on a G x G lattice over [0, 2pi)^2 (the
  *     other parameters at the circuit's theta) runs as a second batched plan
- *     per (group, pair): the circuit truncated after the last gate of a or b,
- *     parameters permuted so that a, b are derivative parameters 0, 1;
+ *     per (pair, truncated circuit): the circuit truncated after the last gate
+ *     of a or b, parameters permuted so that a, b are derivative parameters
+ *     0, 1; groups whose gates agree up to that gate (an ansatz with more
+ *     layers after a and b) share one plan;
  *   - all plans, with the uploads of theta and downloads of Q, are captured
  *     into one CUDA graph over a few streams (independent groups overlap).
  *
@@ -43,7 +45,8 @@ typedef struct {
     int pa, pb;             /* Berry parameters (circuit numbering) */
     int compact;            /* G points per circuit (exact reduction) instead of G^2 */
     int early_is_a;         /* a's gate precedes b's */
-    int* perm;              /* circuit parameter k -> plan parameter perm[k] */
+    int* perm;              /* circuit parameter k -> plan parameter perm[k], k < nperm */
+    int nperm;
     size_t th_off, out_off; /* doubles into the pinned staging buffers */
 } bplan_t;
 
@@ -73,10 +76,11 @@ void qgt_batch_default_options(qgt_batch_options_t* o)
     o->streams = 4;
 }
 
-static int same_structure(const qgt_circuit_desc_t* a, const qgt_circuit_desc_t* b)
+/* gates [0, ng) of a and b equal (types, qubits, parameter indices, fixed angles) */
+static int same_gates(const qgt_circuit_desc_t* a, const qgt_circuit_desc_t* b, int ng)
 {
-    if (a->num_qubits != b->num_qubits || a->num_gates != b->num_gates || a->num_params != b->num_params) return 0;
-    for (int g = 0; g < a->num_gates; g++) {
+    if (a->num_qubits != b->num_qubits || a->num_gates < ng || b->num_gates < ng) return 0;
+    for (int g = 0; g < ng; g++) {
         const qgt_gate_desc_t *x = &a->gates[g], *y = &b->gates[g];
         if (x->type != y->type || x->qubits[0] != y->qubits[0] || x->param != y->param) return 0;
         int two = x->type == QGT_GATE_CNOT || x->type == QGT_GATE_CZ || x->type == QGT_GATE_SWAP;
@@ -84,6 +88,20 @@ static int same_structure(const qgt_circuit_desc_t* a, const qgt_circuit_desc_t*
         if (x->param < 0 && memcmp(&x->angle, &y->angle, sizeof(double)) != 0) return 0;
     }
     return 1;
+}
+
+static int same_structure(const qgt_circuit_desc_t* a, const qgt_circuit_desc_t* b)
+{
+    return a->num_gates == b->num_gates && a->num_params == b->num_params && same_gates(a, b, a->num_gates);
+}
+
+/* last gate driven by parameter pa or pb (-1 if none) */
+static int last_gate_of(const qgt_circuit_desc_t* c, int pa, int pb)
+{
+    int gl = -1;
+    for (int g = 0; g < c->num_gates; g++)
+        if (c->gates[g].param == pa || c->gates[g].param == pb) gl = g;
+    return gl;
 }
 
 static int make_plan(const qgt_circuit_desc_t* c, const qgt_batch_options_t* bo, int batch, int Pd, qgt_plan_t** out)
@@ -195,14 +213,18 @@ int qgt_batch_create(const qgt_circuit_desc_t* circuits, int32_t count, const in
             bp->berry = 1;
             bp->pa = pa;
             bp->pb = pb;
-            bp->P = cc->num_params;
             bp->Pd = 2;
             bp->mem = (int*)malloc(sizeof(int) * (size_t)count);
             bp->perm = (int*)malloc(sizeof(int) * (size_t)cc->num_params);
             tg = (qgt_gate_desc_t*)malloc(sizeof(qgt_gate_desc_t) * (size_t)(cc->num_gates + 1));
             if (!bp->mem || !bp->perm || !tg) { rc = qgt_set_error(E_NOMEM, "qgt_batch_create: oom"); break; }
+            /* circuits whose gates up to the last one of a or b equal this circuit's (e.g. the
+             * same ansatz with more layers after a and b) share the truncated circuit's plan */
+            const int gl = last_gate_of(cc, pa, pb);
             for (int d = c; d < count; d++)
-                if (!done[d] && group[d] == group[c] && berry_params[2 * d] == pa && berry_params[2 * d + 1] == pb) {
+                if (!done[d] && berry_params[2 * d] == pa && berry_params[2 * d + 1] == pb &&
+                    (group[d] == group[c] || (gl >= 0 && last_gate_of(&circuits[d], pa, pb) == gl &&
+                                              same_gates(cc, &circuits[d], gl + 1)))) {
                     bp->mem[bp->nmem++] = d;
                     done[d] = 1;
                 }
@@ -222,13 +244,18 @@ int qgt_batch_create(const qgt_circuit_desc_t* circuits, int32_t count, const in
             bp->compact = (na == 1 && nb == 1);
             bp->early_is_a = ga < gb;
             bp->per = bp->compact ? b->G : b->G * b->G;
+            bp->nperm = cc->num_params;   /* members with more parameters map the rest beyond bp->P */
             for (int k = 0, nxt = 2; k < cc->num_params; k++)
                 bp->perm[k] = (k == pa) ? 0 : (k == pb) ? 1 : nxt++;
+            bp->P = 2;   /* plan parameters: a, b, then those of the truncated gates */
             for (int g = 0; g <= glast; g++) {
                 tg[g] = cc->gates[g];
-                if (tg[g].param >= 0) tg[g].param = bp->perm[tg[g].param];
+                if (tg[g].param >= 0) {
+                    tg[g].param = bp->perm[tg[g].param];
+                    if (tg[g].param + 1 > bp->P) bp->P = tg[g].param + 1;
+                }
             }
-            qgt_circuit_desc_t tc = {cc->num_qubits, glast + 1, tg, cc->num_params};
+            qgt_circuit_desc_t tc = {cc->num_qubits, glast + 1, tg, bp->P};
             if (bp->nmem * bp->per > 65535) {
                 rc = qgt_set_error(E_INVAL, "qgt_batch_create: %d Berry points in one group exceed 65535", bp->nmem * bp->per);
                 break;
@@ -312,7 +339,9 @@ int qgt_batch_execute_host(qgt_batch_t* b, const double* theta, double* Q, doubl
             for (int t = 0; t < bp->per; t++) {
                 double* dst = b->th_pin + bp->th_off + ((size_t)m * bp->per + t) * (size_t)bp->P;
                 if (!bp->berry) { memcpy(dst, th, sizeof(double) * (size_t)bp->P); continue; }
-                for (int k = 0; k < bp->P; k++) dst[bp->perm[k]] = th[k];
+                const int np = b->P[bp->mem[m]] < bp->nperm ? b->P[bp->mem[m]] : bp->nperm;
+                for (int k = 0; k < np; k++)
+                    if (bp->perm[k] < bp->P) dst[bp->perm[k]] = th[k];
                 if (bp->compact) {
                     dst[0] = bp->early_is_a ? step * t : 0.0;
                     dst[1] = bp->early_is_a ? 0.0 : step * t;

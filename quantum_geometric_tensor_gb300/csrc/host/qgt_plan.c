@@ -1703,8 +1703,8 @@ static int run_step(qgt_plan_t* p)
     if (!h_done && (rc = apply_hamiltonian(p, &launches)) != 0) return rc;
     MARK(3);
     if (p->small_nsplit) {
-        if ((rc = qgt_dev_gram_small(p->V, p->N, p->rows, p->fp64, p->small_part_d, p->small_nsplit, p->HG_d, p->B,
-                                     p->pstride, p->stream)) != 0)
+        if ((rc = qgt_dev_gram_small(p->V, p->N, p->rows, !has_h, p->fp64, p->small_part_d, p->small_nsplit, p->HG_d,
+                                     p->B, p->pstride, p->stream)) != 0)
             return rc;
     } else if (p->fp64) {
         if ((rc = qgt_dev_gram_f64(p->V, p->N, p->rows, p->part_d, p->part_nsplit, p->HG_d, p->B, p->pstride,

@@ -317,10 +317,12 @@ int qgt_dev_cholesky_refined_launches(int32_t P);
 int qgt_dev_cholesky_batch(const double* A, int complex_input, const double* b, int32_t P, double lambda,
                            double* work, double* x, double* status, int32_t nsys, void* stream);
 /* small Gram (rows <= 8) of complex64 (fp64 = 0; FP32 sums of 32-amplitude
- * blocks, added in FP64) or complex128 rows (FP64): HG per point (npoints points point_stride amplitudes apart); part
+ * blocks, added in FP64) or complex128 rows (FP64): HG per point (npoints
+ * points point_stride amplitudes apart); skip_row1 = 1 leaves row 1 (H psi of
+ * a plan without Hamiltonian) unread and writes its entries as zeros; part
  * holds npoints x nsplit x 36 complex partials */
-int qgt_dev_gram_small(const void* V, int64_t N, int32_t rows, int32_t fp64, double* part, int32_t nsplit,
-                       double* HG, int32_t npoints, int64_t point_stride, void* stream);
+int qgt_dev_gram_small(const void* V, int64_t N, int32_t rows, int32_t skip_row1, int32_t fp64, double* part,
+                       int32_t nsplit, double* HG, int32_t npoints, int64_t point_stride, void* stream);
 
 /* <V + a_off[k] | V + b_off[k]> over N amplitudes (offsets in amplitudes), pair k split in nchunk
  * ranges: part[k * nchunk + c] (complex double) holds the sum over range c */

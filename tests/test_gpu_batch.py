@@ -106,3 +106,23 @@ def test_berry_map_shared_parameter_full_lattice(Q, orc):
         _, maps = b.run([th])
     ref = orc.berry_map(n, O.gates_array(gates), th, 0, n + 1, G)
     assert np.abs(maps[0] - ref.reshape(G, G)).max() < 1e-10
+
+
+@pytest.mark.parametrize("prec,tol", [("FP64", 1e-10), ("MIXED", 1e-6)])
+def test_berry_plan_shared_by_deeper_circuits(Q, orc, prec, tol):
+    """The same ansatz at 1, 2 and 3 layers with the Berry pair in the first
+    layer: the truncated circuits coincide, so the three structural groups
+    share one Berry plan (each circuit keeps its own theta); a pair in the
+    last layer of the 3-layer circuit needs a plan of its own."""
+    n, G = 7, 6
+    circs = [(n, 1), (n, 2), (n, 3), (n, 3)]
+    spec = [(n, Q.ansatz_gates(n, L, "cnot"), 2 * n * L) for (n, L) in circs]
+    pairs = [(0, n), (0, n), (0, n), (4 * n + 1, 5 * n + 2)]
+    thetas = [O.splitmix64_params(900 + c, s[2]) for c, s in enumerate(spec)]
+    with Q.Batch(spec, pairs, precision=getattr(Q, prec), grid=G) as b:
+        info = b.info()
+        _, maps = b.run(thetas)
+    assert info.num_groups == 3 and info.num_berry_plans == 2
+    for c, ((n_, L), th) in enumerate(zip(circs, thetas)):
+        ref = orc.berry_map(n_, O.gates_array(spec[c][1]), th, pairs[c][0], pairs[c][1], G)
+        assert np.abs(maps[c] - ref.reshape(G, G)).max() < tol, (c, L, pairs[c])
