@@ -332,7 +332,8 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
     R* scoef = reinterpret_cast<R*>(sops + a.nops);
     // this CTA's vector entry runs the pass program from its start op (a Q2_SEG; a derivative
     // spawned after a checkpoint starts at its segment); ops keep their program indices
-    const int start = a.entries[blockIdx.y].start_op;
+    const qgt_dev_entry_t e = a.entries[blockIdx.y];
+    const int start = e.start_op;
 
     // per SEG op: its layout's local bits [0, 16) and their physical qubits [16, 32)
     int8_t* sseg = reinterpret_cast<int8_t*>(scoef + 8 * a.nops);
@@ -340,6 +341,56 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
     __shared__ R sgen[24];
     // physical offset of the tile's local bits 5 .. tile_bits - 1 (checkpoint stores)
     __shared__ uint32_t supper[256];
+    uint64_t base = 0;
+    {
+        uint32_t rest = blockIdx.x;
+        for (int q = 0; q < a.n; q++)
+            if (!((a.tile_mask >> q) & 1)) { base |= (uint64_t)(rest & 1u) << q; rest >>= 1; }
+    }
+    // layout of the current segment: local index contributions of reg bits and of this thread
+    int lreg[RB];
+    uint32_t preg[RB];   // n <= 30: physical indices fit in 32 bits
+    int lthr = 0;
+    uint32_t pthr = 0;
+    auto set_layout_from = [&](const int8_t* L) {   // 16 local bits, then their physical qubits
+        const int8_t* Pq = L + 16;
+        lthr = lane;
+        pthr = (uint32_t)base | (uint32_t)lane;  // local bits 0..4 are physical qubits 0..4
+#pragma unroll
+        for (int w = 0; w < 3; w++) {
+            const int lb = L[8 + w];
+            if ((warp >> w) & 1) { lthr |= 1 << lb; pthr |= 1u << Pq[8 + w]; }
+        }
+#pragma unroll
+        for (int i = 0; i < RB; i++) { lreg[i] = 1 << L[i]; preg[i] = 1u << Pq[i]; }
+    };
+    auto set_layout = [&](int at) { set_layout_from(sseg + 32 * at); };   // the SEG op at program index `at`
+    auto lidx = [&](int j) {
+        int l = lthr;
+#pragma unroll
+        for (int i = 0; i < RB; i++) if ((j >> i) & 1) l |= lreg[i];
+        return l;
+    };
+    auto pidx = [&](int j) {
+        uint32_t p = pthr;
+#pragma unroll
+        for (int i = 0; i < RB; i++) if ((j >> i) & 1) p |= preg[i];
+        return p;
+    };
+
+    // the tile loads go out first, from the entry's own copy of its starting layout; the program
+    // is staged into shared memory while they are in flight
+    T v[NR];
+    set_layout_from(e.lay);
+    {
+        const T* src = reinterpret_cast<const T*>(a.V) + blockIdx.z * a.point_stride + (int64_t)e.src_row * a.N;
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            const uint32_t ph = pidx(j);
+            if (e.flags & QENT_SRC_ZERO) { v[j].x = (ph == 0) ? (R)1 : (R)0; v[j].y = (R)0; }
+            else v[j] = src[ph];
+        }
+    }
     {
         if (threadIdx.x < (1 << (a.tile_bits - 5))) {
             uint32_t o = 0;
@@ -376,45 +427,6 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
         }
         __syncthreads();
     }
-    const qgt_dev_entry_t e = a.entries[blockIdx.y];
-    uint64_t base = 0;
-    {
-        uint32_t rest = blockIdx.x;
-        for (int q = 0; q < a.n; q++)
-            if (!((a.tile_mask >> q) & 1)) { base |= (uint64_t)(rest & 1u) << q; rest >>= 1; }
-    }
-    // layout of the current segment: local index contributions of reg bits and of this thread
-    int lreg[RB];
-    uint32_t preg[RB];   // n <= 30: physical indices fit in 32 bits
-    int lthr = 0;
-    uint32_t pthr = 0;
-    auto set_layout = [&](int at) {   // the layout of the SEG op at program index `at`
-        const int8_t* L = sseg + 32 * at;
-        const int8_t* Pq = L + 16;
-        lthr = lane;
-        pthr = (uint32_t)base | (uint32_t)lane;  // local bits 0..4 are physical qubits 0..4
-#pragma unroll
-        for (int w = 0; w < 3; w++) {
-            const int lb = L[8 + w];
-            if ((warp >> w) & 1) { lthr |= 1 << lb; pthr |= 1u << Pq[8 + w]; }
-        }
-#pragma unroll
-        for (int i = 0; i < RB; i++) { lreg[i] = 1 << L[i]; preg[i] = 1u << Pq[i]; }
-    };
-    auto lidx = [&](int j) {
-        int l = lthr;
-#pragma unroll
-        for (int i = 0; i < RB; i++) if ((j >> i) & 1) l |= lreg[i];
-        return l;
-    };
-    auto pidx = [&](int j) {
-        uint32_t p = pthr;
-#pragma unroll
-        for (int i = 0; i < RB; i++) if ((j >> i) & 1) p |= preg[i];
-        return p;
-    };
-
-    T v[NR];
     // (-i/2) G of the rotation op `so` on the current vector (a derivative spawned there), through
     // the gate paths with the generator matrices (-i/2) X, (-i/2) Y, (-i/2) Z (exact: entries 0, +-1/2)
     auto spawn_gen = [&](const qgt_dev_op2_t& so) {
@@ -455,16 +467,6 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
             }
         }
     };
-    set_layout(0);
-    {
-        const T* src = reinterpret_cast<const T*>(a.V) + blockIdx.z * a.point_stride + (int64_t)e.src_row * a.N;
-#pragma unroll
-        for (int j = 0; j < NR; j++) {
-            const uint32_t ph = pidx(j);
-            if (e.flags & QENT_SRC_ZERO) { v[j].x = (ph == 0) ? (R)1 : (R)0; v[j].y = (R)0; }
-            else v[j] = src[ph];
-        }
-    }
     for (int pc = start + 1; pc < a.nops; pc++) {
         const qgt_dev_op2_t op = sops[pc];
         R m[8];

@@ -1425,6 +1425,18 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
     }
     if ((rc = qgt_dev_memset(p->theta_d, 0, sizeof(double) * ((size_t)p->B * p->P + 1), p->stream)) != 0) goto fail;
     if ((rc = qgt_dev_memcpy_h2d(p->ops_d, p->ops_h, sizeof(qgt_dev_op_t) * (size_t)p->nops, p->stream)) != 0) goto fail;
+    for (int k = 0; k < p->npasses; k++) {   /* initial layouts of the register-resident entries */
+        const spass_t* ps = &p->passes[k];
+        if (ps->prog_count <= 0) continue;
+        for (int i = ps->ent_begin; i < ps->ent_begin + ps->ent_count; i++) {
+            qgt_dev_entry_t* e = &p->ents_h[i];
+            const int8_t* L = p->segs_h + 16 * p->prog_h[ps->prog_begin + e->start_op].seg;
+            for (int b = 0; b < 16; b++) {
+                e->lay[b] = L[b];
+                e->lay[16 + b] = (L[b] >= 0 && L[b] < 16) ? ps->l2p[L[b]] : (int8_t)0;
+            }
+        }
+    }
     if ((rc = qgt_dev_memcpy_h2d(p->ents_d, p->ents_h, sizeof(qgt_dev_entry_t) * (size_t)p->nents, p->stream)) != 0) goto fail;
     if (p->nprog && (rc = qgt_dev_memcpy_h2d(p->prog_d, p->prog_h, sizeof(qgt_dev_op2_t) * (size_t)p->nprog, p->stream)) != 0) goto fail;
     if (p->nsegs && (rc = qgt_dev_memcpy_h2d(p->segs_d, p->segs_h, (size_t)16 * p->nsegs, p->stream)) != 0) goto fail;

@@ -77,6 +77,8 @@ typedef struct {
     int32_t split_row;
     int32_t start_op;   /* register-resident passes: the entry runs the pass program from this op (a
                            Q2_SEG) on; 0 = the whole program */
+    int8_t lay[32];     /* register-resident passes: the layout of op start_op (its 16 local bits,
+                           then their physical qubits), so that the tile loads need no program */
 } qgt_dev_entry_t;
 
 typedef struct {
