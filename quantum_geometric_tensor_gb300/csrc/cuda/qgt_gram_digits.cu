@@ -225,6 +225,11 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
     pair_of((int)(blockIdx.x % ntp), nbk, &mb, &nbo);
     const bool diag = (mb == nbo);
     const int nblk = diag ? 1 : 2;
+    // the B block's planes hold its valid rows rounded up to 32 (the last block of a plan is
+    // partly padding): plane stride pbB, MMA N = 2 rbB ([Re partner | Im partner])
+    const int vb = rows - 128 * nbo < 128 ? rows - 128 * nbo : 128;
+    const int rbB = (vb + 31) & ~31;
+    const uint32_t pbB = (uint32_t)rbB * DG_BK * 2;
     const int64_t k0 = (int64_t)(blockIdx.x / ntp) * kchunk;
     int64_t k1 = k0 + kchunk;
     if (k1 > N) k1 = N;
@@ -290,7 +295,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
                 (void)bar_wait(smem_u32(&raw_full[u % DG_RAW_STAGES]), (u / DG_RAW_STAGES) & 1, deadline + DG_TIMEOUT_NS);
     } else if (warp == 1 && lane == 0) {
         // ---------- MMA issuer ----------
-        const uint32_t id = idesc_f16(256);
+        const uint32_t id = idesc_f16(2u * (uint32_t)rbB);
         for (int kt = 0; kt < nk; kt++) {
             const int s = kt % DG_PL_STAGES;
             if (!bar_wait(smem_u32(&pl_full[s]), (kt / DG_PL_STAGES) & 1, deadline)) {
@@ -307,9 +312,10 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
 #pragma unroll
             for (int t = 0; t < 12; t++) {
                 const int lv = dg_terms[t][0], pt = dg_terms[t][1], b = dg_terms[t][2], rg = dg_terms[t][3];
-                const uint32_t pa = diag ? pb + (3 * lv + pt) * DG_PLANE_BYTES : st + (2 * lv + pt) * DG_PLANE_BYTES;
+                // a diagonal pair's A rows past rbB read other planes: those output rows are padding
+                const uint32_t pa = diag ? pb + (3 * lv + pt) * pbB : st + (2 * lv + pt) * DG_PLANE_BYTES;
                 const uint32_t first = (kt == 0) && (t == 0 || t == 2);
-                umma(tmem + (uint32_t)rg * 256u, desc_sw32(pa), desc_sw32(pb + b * DG_PLANE_BYTES), id, first ? 0u : 1u);
+                umma(tmem + (uint32_t)rg * 256u, desc_sw32(pa), desc_sw32(pb + b * pbB), id, first ? 0u : 1u);
             }
             umma_commit(smem_u32(&pl_empty[s]));
         }
@@ -337,8 +343,12 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
                 // the B layout (9 planes) for the B block and for a diagonal pair's only block
                 const bool blay = diag || b == 1;
                 uint8_t* planes = plst + (diag ? 0 : b * DG_PL_A * DG_PLANE_BYTES);
-#pragma unroll 4
-                for (int rr = 4 * cw; rr < 128; rr += 4 * DG_CONV_WARPS) {
+                const uint32_t ps_ = blay ? pbB : (uint32_t)DG_PLANE_BYTES;   // plane stride
+                const int rlim = blay ? rbB : 128;
+#pragma unroll
+                for (int it = 0; it < 128 / (4 * DG_CONV_WARPS); it++) {
+                    const int rr = 4 * cw + 4 * DG_CONV_WARPS * it;
+                    if (rr >= rlim) break;   // warp-uniform: rlim is a multiple of 32
                     const int r = rr + sub;
                     const float4 q = *reinterpret_cast<const float4*>(raw + r * 32 + 2 * kp);
                     const float iu = inv_u[b][r];
@@ -355,15 +365,15 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
                         const __half2 hd = __floats2half2_rn(d0, d1);
                         // level l plane: A layout 2 l + c, B layout 3 l + c (+ the negated real part at 3 l + 2)
                         const int ls = blay ? 3 : 2;
-                        uint8_t* pD = planes + c * DG_PLANE_BYTES + off;
+                        uint8_t* pD = planes + c * ps_ + off;
                         *reinterpret_cast<__half2*>(pD) = hd;
-                        *reinterpret_cast<__half2*>(pD + ls * DG_PLANE_BYTES) = h1;
-                        *reinterpret_cast<__half2*>(pD + 2 * ls * DG_PLANE_BYTES) = h2;
+                        *reinterpret_cast<__half2*>(pD + ls * ps_) = h1;
+                        *reinterpret_cast<__half2*>(pD + 2 * ls * ps_) = h2;
                         if (blay && c == 0) {
-                            uint8_t* pN = planes + 2 * DG_PLANE_BYTES + off;
+                            uint8_t* pN = planes + 2 * ps_ + off;
                             *reinterpret_cast<__half2*>(pN) = __hneg2(hd);
-                            *reinterpret_cast<__half2*>(pN + 3 * DG_PLANE_BYTES) = __hneg2(h1);
-                            *reinterpret_cast<__half2*>(pN + 6 * DG_PLANE_BYTES) = __hneg2(h2);
+                            *reinterpret_cast<__half2*>(pN + 3 * ps_) = __hneg2(h1);
+                            *reinterpret_cast<__half2*>(pN + 6 * ps_) = __hneg2(h2);
                         }
                     }
                 }
@@ -386,8 +396,9 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
             const uint32_t lanebase = tmem + ((uint32_t)(quad * 32) << 16);
             for (int ri = 0; ri < 2; ri++) {
                 for (int c = 2 * half; c < 2 * half + 2; c++) {
-                    tmem_ld32(lanebase + ri * 128 + c * 32, hh);
-                    tmem_ld32(lanebase + 256 + ri * 128 + c * 32, rsd);
+                    if (c * 32 >= rbB) continue;   // columns past the B block's rows (never read)
+                    tmem_ld32(lanebase + ri * rbB + c * 32, hh);
+                    tmem_ld32(lanebase + 256 + ri * rbB + c * 32, rsd);
                     if (diag && ri == 0 && c == (row >> 5) && hh[row & 31] > 8388608.0f)
                         atomicExch(err, DG_ERR_INEXACT);
                     float4* o = reinterpret_cast<float4*>(out + ri * 128 * 128 + row * 128 + c * 32);
