@@ -26,10 +26,11 @@
 //                      Im l1, Re l2, Im l2}, the B block as 9 planes
 //                      {Re D, Im D, -Re D, Re l1, Im l1, -Re l1, Re l2, Im l2,
 //                      -Re l2}, so that every (Re, Im) pair of B operands that
-//                      one A plane meets is two adjacent planes
-//   1 thread: 12 tcgen05.mma (M = 128, N = 256 = [Re partner | Im partner],
-//             K = 16) per k-step into TMEM [D*D Re | D*D Im | rest Re |
-//             rest Im] (512 columns)
+//                      one A plane meets is two adjacent planes; B planes
+//                      hold the block's valid rows rounded up to 32 (rbB)
+//   1 thread: 12 tcgen05.mma (M = 128, N = 2 rbB <= 256 = [Re partner |
+//             Im partner], K = 16) per k-step into TMEM [D*D Re | D*D Im |
+//             rest Re | rest Im] (two regions of 256 columns)
 //   epilogue (the converter warps): TMEM -> FP32 (hh + rest) -> partials
 // The raw ring (3 stages) and the plane ring (2 stages) are decoupled, so a
 // raw buffer is refilled as soon as it has been converted.
