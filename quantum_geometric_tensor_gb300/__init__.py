@@ -225,17 +225,31 @@ class Plan:
         _check(lib().qgt_plan_get_info(self.h, C.byref(i)), "qgt_plan_get_info")
         return i
 
-    def run(self, theta, want=("Q", "grad", "energy", "natgrad")):
+    def output_buffers(self, want=("Q", "grad", "energy", "natgrad")):
+        """Host arrays for run(..., out=): reusing them across steps saves the
+        allocation and first-touch page faults of fresh outputs."""
+        B, P = self.B, self.Pd
+        return {"Q": np.zeros((B, P, P), dtype=np.complex128) if "Q" in want else None,
+                "grad": np.zeros((B, P)) if "grad" in want else None,
+                "energy": np.zeros(B) if "energy" in want else None,
+                "natgrad": np.zeros((B, P)) if "natgrad" in want else None}
+
+    def run(self, theta, want=("Q", "grad", "energy", "natgrad"), out=None):
         """One step.  theta: (P,) or, for a batched plan, (batch, P); outputs
-        gain a leading batch axis when batch > 1."""
+        gain a leading batch axis when batch > 1.  out: arrays from
+        output_buffers() to write into (their set replaces `want`)."""
         B, P = self.B, self.Pd
         theta = np.ascontiguousarray(theta, dtype=np.float64)
         if theta.size != B * self.P:
             raise ValueError(f"theta has {theta.size} values, plan wants {B} x {self.P}")
-        Q = np.zeros((B, P, P), dtype=np.complex128) if "Q" in want else None
-        g = np.zeros((B, P)) if "grad" in want else None
-        e = np.zeros(B) if "energy" in want else None
-        x = np.zeros((B, P)) if "natgrad" in want else None
+        if out is None:
+            out = self.output_buffers(want)
+        for k, shape, dt in (("Q", (B, P, P), np.complex128), ("grad", (B, P), np.float64),
+                             ("energy", (B,), np.float64), ("natgrad", (B, P), np.float64)):
+            a = out.get(k)
+            if a is not None and (a.shape != shape or a.dtype != dt or not a.flags.c_contiguous):
+                raise ValueError(f"out[{k!r}] must be a C-contiguous {dt.__name__} array of shape {shape}")
+        Q, g, e, x = out.get("Q"), out.get("grad"), out.get("energy"), out.get("natgrad")
         _check(lib().qgt_plan_execute_host(self.h, _ptr(theta), _ptr(Q), _ptr(g), _ptr(e), _ptr(x)),
                "qgt_plan_execute_host")
         if B == 1:

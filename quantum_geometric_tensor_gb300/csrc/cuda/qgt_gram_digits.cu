@@ -591,6 +591,8 @@ extern "C" int qgt_dev_dg_gram_run(qgt_dg_gram_t* g, double* HG, void* stream)
     return qgt_dev_last_error();
 }
 
+extern "C" const int* qgt_dev_dg_gram_err(const qgt_dg_gram_t* g) { return g ? g->err : NULL; }
+
 extern "C" int qgt_dev_dg_gram_status(qgt_dg_gram_t* g, void* stream)
 {
     int h = 0;

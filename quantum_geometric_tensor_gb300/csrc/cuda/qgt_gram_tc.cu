@@ -399,6 +399,8 @@ extern "C" int qgt_dev_tc_gram_run(qgt_tc_gram_t* g, double inv_scale2, double* 
     return qgt_dev_last_error();
 }
 
+extern "C" const int* qgt_dev_tc_gram_err(const qgt_tc_gram_t* g) { return g ? g->err : NULL; }
+
 extern "C" int qgt_dev_tc_gram_status(qgt_tc_gram_t* g, void* stream)
 {
     int h = 0;

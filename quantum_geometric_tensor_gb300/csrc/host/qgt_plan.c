@@ -153,6 +153,7 @@ struct qgt_plan {
     int32_t *slot_param_d, *param_ptr_d, *param_slots_d;
     /* pinned host staging */
     double *theta_pin, *Q_pin, *grad_pin, *energy_pin, *natgrad_pin, *status_pin;
+    int* gerr_pin;                /* the tensor-core Gram's error flag, copied with the outputs */
     double hscale;
     float split_scale;
     int64_t device_bytes;
@@ -1452,6 +1453,7 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
         if ((rc = qgt_dev_host_alloc((void**)&p->natgrad_pin, sizeof(double) * (B * Pd + 1))) != 0) goto fail;
         if ((rc = qgt_dev_host_alloc((void**)&p->energy_pin, sizeof(double) * (B + 1))) != 0) goto fail;
         if ((rc = qgt_dev_host_alloc((void**)&p->status_pin, sizeof(double) * 2 * B)) != 0) goto fail;
+        if ((rc = qgt_dev_host_alloc((void**)&p->gerr_pin, sizeof(int) * 4)) != 0) goto fail;
     }
     if ((rc = qgt_dev_stream_sync(p->stream)) != 0) goto fail;
     /* first step eagerly (sets kernel attributes, validates), then capture */
@@ -1510,7 +1512,7 @@ void qgt_plan_destroy(qgt_plan_t* p)
                    p->Q_d, p->grad_d, p->energy_d, p->natgrad_d, p->chol_work_d, p->status_d, p->slot_param_d,
                    p->param_ptr_d, p->param_slots_d};
     for (size_t i = 0; i < sizeof dev / sizeof dev[0]; i++) qgt_dev_free(dev[i]);
-    void* pin[] = {p->theta_pin, p->Q_pin, p->grad_pin, p->natgrad_pin, p->energy_pin, p->status_pin};
+    void* pin[] = {p->theta_pin, p->Q_pin, p->grad_pin, p->natgrad_pin, p->energy_pin, p->status_pin, p->gerr_pin};
     for (size_t i = 0; i < sizeof pin / sizeof pin[0]; i++) qgt_dev_host_free(pin[i]);
     qgt_dev_stream_destroy(p->stream);
     free(p->gates); free(p->passes); free(p->ops_h); free(p->ents_h); free(p->coef_h); free(p->prog_h); free(p->segs_h);
@@ -1847,9 +1849,17 @@ int qgt_plan_execute_host(qgt_plan_t* p, const double* theta, double* Q, double*
         if ((rc = qgt_dev_memcpy_h2d(p->theta_d, p->theta_pin, sizeof(double) * nth, p->stream)) != 0) return rc;
     }
     if ((rc = launch_step(p)) != 0) return rc;
-    if (has_h && p->Pd > 0) {
-        if ((rc = qgt_dev_memcpy_d2h(p->status_pin, p->status_d, sizeof(double) * 2 * B, p->stream)) != 0) return rc;
-        if ((rc = qgt_dev_stream_sync(p->stream)) != 0) return rc;
+    /* every output copy is queued behind the step: one synchronisation in the common case */
+    const int need_status = has_h && p->Pd > 0;
+    const int* gerr = p->tc ? qgt_dev_tc_gram_err(p->tc) : (p->dg ? qgt_dev_dg_gram_err(p->dg) : NULL);
+    if (need_status && (rc = qgt_dev_memcpy_d2h(p->status_pin, p->status_d, sizeof(double) * 2 * B, p->stream)) != 0) return rc;
+    if (gerr && (rc = qgt_dev_memcpy_d2h(p->gerr_pin, gerr, sizeof(int), p->stream)) != 0) return rc;
+    if (Q && (rc = qgt_dev_memcpy_d2h(p->Q_pin, p->Q_d, sizeof(double) * 2 * B * Pd * Pd, p->stream)) != 0) return rc;
+    if (grad && (rc = qgt_dev_memcpy_d2h(p->grad_pin, p->grad_d, sizeof(double) * B * Pd, p->stream)) != 0) return rc;
+    if (energy && (rc = qgt_dev_memcpy_d2h(p->energy_pin, p->energy_d, sizeof(double) * B, p->stream)) != 0) return rc;
+    if (natgrad && (rc = qgt_dev_memcpy_d2h(p->natgrad_pin, p->natgrad_d, sizeof(double) * B * Pd, p->stream)) != 0) return rc;
+    if ((rc = qgt_dev_stream_sync(p->stream)) != 0) return rc;
+    if (need_status) {
         if (B == 1) {
             /* the graph's blocked solve has no retries: on a non-positive pivot
              * rerun the solve with lambda x 10 retries (outside the graph).  The
@@ -1857,29 +1867,27 @@ int qgt_plan_execute_host(qgt_plan_t* p, const double* theta, double* Q, double*
              * loses a pivot or the refinement does not converge; the FP64
              * solver then starts from lambda itself */
             const double lam0 = p->fp64 || p->Pd > 2048 ? p->opt.lambda * 10.0 : p->opt.lambda;
-            if ((int)p->status_pin[0] != 0 &&
-                (rc = qgt_dev_cholesky(p->Q_d, 1, p->grad_d, p->Pd, lam0, p->chol_work_d, p->natgrad_d,
-                                       p->status_d, p->stream)) != 0)
-                return rc;
+            if ((int)p->status_pin[0] != 0) {
+                if ((rc = qgt_dev_cholesky(p->Q_d, 1, p->grad_d, p->Pd, lam0, p->chol_work_d, p->natgrad_d,
+                                           p->status_d, p->stream)) != 0)
+                    return rc;
+                if (natgrad &&
+                    (rc = qgt_dev_memcpy_d2h(p->natgrad_pin, p->natgrad_d, sizeof(double) * B * Pd, p->stream)) != 0)
+                    return rc;
+                if ((rc = qgt_dev_stream_sync(p->stream)) != 0) return rc;
+            }
         } else {
             for (size_t b = 0; b < B; b++)
                 if ((int)p->status_pin[2 * b] != 0)
                     return qgt_set_error((int)p->status_pin[2 * b], "cholesky: point %zu not positive definite after lambda retries", b);
         }
     }
-    if (Q && (rc = qgt_dev_memcpy_d2h(p->Q_pin, p->Q_d, sizeof(double) * 2 * B * Pd * Pd, p->stream)) != 0) return rc;
-    if (grad && (rc = qgt_dev_memcpy_d2h(p->grad_pin, p->grad_d, sizeof(double) * B * Pd, p->stream)) != 0) return rc;
-    if (energy && (rc = qgt_dev_memcpy_d2h(p->energy_pin, p->energy_d, sizeof(double) * B, p->stream)) != 0) return rc;
-    if (natgrad && (rc = qgt_dev_memcpy_d2h(p->natgrad_pin, p->natgrad_d, sizeof(double) * B * Pd, p->stream)) != 0) return rc;
-    if ((rc = qgt_dev_stream_sync(p->stream)) != 0) return rc;
     if (Q) memcpy(Q, p->Q_pin, sizeof(double) * 2 * B * Pd * Pd);
     if (grad) memcpy(grad, p->grad_pin, sizeof(double) * B * Pd);
     if (energy) memcpy(energy, p->energy_pin, sizeof(double) * B);
     if (natgrad) memcpy(natgrad, p->natgrad_pin, sizeof(double) * B * Pd);
-    if (p->tc || p->dg) {
-        int st = p->tc ? qgt_dev_tc_gram_status(p->tc, p->stream) : qgt_dev_dg_gram_status(p->dg, p->stream);
-        if (st) return qgt_set_error(st, "tensor-core Gram reported device status %d", st);
-    }
+    if (gerr && p->gerr_pin[0])
+        return qgt_set_error(p->gerr_pin[0], "tensor-core Gram reported device status %d", p->gerr_pin[0]);
     return 0;
 }
 

@@ -253,6 +253,8 @@ int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, const uint32_
                            int32_t point_rows, qgt_dg_gram_t** g);
 int qgt_dev_dg_gram_run(qgt_dg_gram_t* g, double* HG, void* stream);
 int qgt_dev_dg_gram_status(qgt_dg_gram_t* g, void* stream);
+/* device address of the kernel's error flag (int; 0 = no error), for a copy queued with others */
+const int* qgt_dev_dg_gram_err(const qgt_dg_gram_t* g);
 void qgt_dev_dg_gram_destroy(qgt_dg_gram_t* g);
 int64_t qgt_dev_dg_gram_scratch_bytes(const qgt_dg_gram_t* g);
 void qgt_dev_dg_gram_shape(const qgt_dg_gram_t* g, int* ntp, int* nsplit, int64_t* kchunk);
@@ -274,6 +276,7 @@ int qgt_dev_tc_gram_run(qgt_tc_gram_t* g, double inv_scale2, double* HG, void* s
 void qgt_dev_tc_gram_destroy(qgt_tc_gram_t* g);
 /* device error word of the last run (0 ok, QGT_ERROR_TIMEOUT on an expired wait); synchronises */
 int qgt_dev_tc_gram_status(qgt_tc_gram_t* g, void* stream);
+const int* qgt_dev_tc_gram_err(const qgt_tc_gram_t* g);
 int64_t qgt_dev_tc_gram_scratch_bytes(const qgt_tc_gram_t* g);
 /* HG -> Q, grad, energy (FP64 renormalisation + projector + slot->param sum) */
 typedef struct {

@@ -105,3 +105,20 @@ def test_cholesky_retry_and_solve(Q):
     x, used = Q.cholesky_solve(B, np.ones(40), 1e-3)
     assert used == pytest.approx(0.1)
     assert rel((B + used * np.eye(40)) @ x, np.ones(40)) < 1e-12
+
+
+def test_reused_output_buffers(Q):
+    """run(theta, out=...) writes the same outputs into caller-owned arrays (one
+    synchronisation per call; bad buffers are refused before any copy)."""
+    n, L = 12, 2
+    P = 2 * n * L
+    g = Q.ansatz_gates(n, L, "cz")
+    with Q.Plan(n, g, P, precision=Q.MIXED) as p:
+        ref = p.run(O.splitmix64_params(61, P))
+        bufs = p.output_buffers()
+        for seed in (62, 61):
+            out = p.run(O.splitmix64_params(seed, P), out=bufs)
+        assert out["Q"] is not None and np.array_equal(out["Q"], ref["Q"])
+        assert np.array_equal(out["natgrad"], ref["natgrad"]) and out["energy"] == ref["energy"]
+        with pytest.raises(ValueError):
+            p.run(ref["grad"], out={"Q": np.zeros((1, P, P))})
