@@ -1,7 +1,7 @@
 // qgt_pass2.cu -- register-resident tile passes (the gate-application hot path).
 //
 // A full tile (2^13 complex64 or 2^12 complex128 amplitudes) is held in the
-// registers of one 256-thread CTA: each thread owns NR = 2^RB amplitudes
+// registers of one CTA of 2^WB warps (256 or 512 threads): each thread owns NR = 2^RB amplitudes
 // (RB = 5 for complex64, 4 for complex128).  The tile's local bits play three
 // roles:
 //   lane bits  0..4   (always; physical qubits 0..4, so every global access of
@@ -319,8 +319,8 @@ __device__ __forceinline__ uint32_t role_mask(int role, int q, int lane, int war
 
 // CKPT: the launch's entries also store their state before every Q2_SEG op whose slot is >= 0 (the
 // checkpoint writers of a pass; spawns then run the program from that segment on)
-template <typename R, int RB, bool CKPT>
-__global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_t a)
+template <typename R, int RB, int WB, bool CKPT>
+__global__ void __launch_bounds__(32 << WB, (WB >= 4) ? 1 : 2) pass2_kernel(const qgt_dev_pass2_args_t a)
 {
     typedef typename v2of<R>::T T;
     constexpr int NR = 1 << RB;
@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
     T* tile = reinterpret_cast<T*>(p2_smem);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     // the pass program and each op's coefficients, staged once per CTA
-    qgt_dev_op2_t* sops = reinterpret_cast<qgt_dev_op2_t*>(p2_smem + ((size_t)sizeof(T) << (5 + RB + 3)));
+    qgt_dev_op2_t* sops = reinterpret_cast<qgt_dev_op2_t*>(p2_smem + ((size_t)sizeof(T) << (5 + RB + WB)));
     R* scoef = reinterpret_cast<R*>(sops + a.nops);
     // this CTA's vector entry runs the pass program from its start op (a Q2_SEG; a derivative
     // spawned after a checkpoint starts at its segment); ops keep their program indices
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
     // generator matrices (-i/2) X, (-i/2) Y, (-i/2) Z (2 x 2 complex, row-major)
     __shared__ R sgen[24];
     // physical offset of the tile's local bits 5 .. tile_bits - 1 (checkpoint stores)
-    __shared__ uint32_t supper[256];
+    __shared__ uint32_t supper[1 << (RB + WB)];
     uint64_t base = 0;
     {
         uint32_t rest = blockIdx.x;
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
         lthr = lane;
         pthr = (uint32_t)base | (uint32_t)lane;  // local bits 0..4 are physical qubits 0..4
 #pragma unroll
-        for (int w = 0; w < 3; w++) {
+        for (int w = 0; w < WB; w++) {
             const int lb = L[8 + w];
             if ((warp >> w) & 1) { lthr |= 1 << lb; pthr |= 1u << Pq[8 + w]; }
         }
@@ -674,44 +674,54 @@ __global__ void __launch_bounds__(256, 2) pass2_kernel(const qgt_dev_pass2_args_
         }
     }
     if (e.flags & QENT_ROWMAX) {
-        __shared__ float red[8];
+        __shared__ float red[1 << WB];
         for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
         if (lane == 0) red[warp] = vmax;
         __syncthreads();
         if (threadIdx.x == 0) {
             float mx = 0.f;
-            for (int w = 0; w < 8; w++) mx = fmaxf(mx, red[w]);
+            for (int w = 0; w < (1 << WB); w++) mx = fmaxf(mx, red[w]);
             atomicMax(a.rowmax + (int64_t)blockIdx.z * a.rowmax_stride + e.dst_row, __float_as_uint(mx));
         }
     }
 }
 
+template <typename R, int RB, int WB>
+static int pass2_launch(const qgt_dev_pass2_args_t* a, dim3 grid, size_t smem, size_t smax, cudaStream_t stream)
+{
+    static int attr = 0;   // per instantiation: the dynamic shared-memory limit is raised once
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(pass2_kernel<R, RB, WB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smax);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(pass2_kernel<R, RB, WB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax);
+        if (e != cudaSuccess) return qgt_set_error(-6, "pass2: %s", cudaGetErrorString(e));
+        attr = 1;
+    }
+    if (a->ckpt) pass2_kernel<R, RB, WB, true><<<grid, 32 << WB, smem, stream>>>(*a);
+    else pass2_kernel<R, RB, WB, false><<<grid, 32 << WB, smem, stream>>>(*a);
+    return qgt_dev_last_error();
+}
+
 extern "C" int qgt_dev_pass2(const qgt_dev_pass2_args_t* a, int fp64, void* stream)
 {
     if (a->nentries <= 0) return 0;
-    const int tb = fp64 ? QGT_TILE_MAX_F64 : QGT_TILE_MAX_F32;
-    if (a->tile_bits != tb) return qgt_set_error(-1, "pass2: tile of %d bits (needs %d)", a->tile_bits, tb);
+    // tiles: complex128 12 bits (4 register, 3 warp bits); complex64 13 bits (5 register, 3 warp
+    // bits, 2 CTAs per SM) or 14 bits (5 register, 4 warp bits: 512 threads, 1 CTA per SM)
+    const bool ok = fp64 ? a->tile_bits == QGT_TILE_MAX_F64
+                         : (a->tile_bits == QGT_TILE_MAX_F32 || a->tile_bits == QGT_TILE_WIDE_F32);
+    if (!ok) return qgt_set_error(-1, "pass2: tile of %d bits not supported", a->tile_bits);
     int64_t ntiles = (int64_t)1 << (a->n - a->tile_bits);
     const int np = a->npoints > 0 ? a->npoints : 1;
     if (a->nentries > 65535 || ntiles > 0x7fffffff || np > 65535) return qgt_set_error(-1, "pass2: grid too large");
     dim3 grid((unsigned)ntiles, (unsigned)a->nentries, (unsigned)np);
-    size_t smem = ((size_t)1 << (tb + (fp64 ? 4 : 3))) +                               /* 64 KiB tile */
+    const bool wide = !fp64 && a->tile_bits == QGT_TILE_WIDE_F32;
+    size_t smem = ((size_t)1 << (a->tile_bits + (fp64 ? 4 : 3))) +                       /* the tile */
                   (size_t)a->nops * (sizeof(qgt_dev_op2_t) + 8 * (fp64 ? sizeof(double) : sizeof(float)) + 32);
-    if (smem > 112 * 1024) return qgt_set_error(-1, "pass2: program of %d ops too large", a->nops);
-    static int attr[2] = {0, 0};
-    cudaError_t e = cudaSuccess;
-    if (!attr[fp64 ? 1 : 0]) {
-        e = fp64 ? cudaFuncSetAttribute(pass2_kernel<double, 4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 112 * 1024)
-                 : cudaFuncSetAttribute(pass2_kernel<float, 5, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 112 * 1024);
-        if (e == cudaSuccess)
-            e = fp64 ? cudaFuncSetAttribute(pass2_kernel<double, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 112 * 1024)
-                     : cudaFuncSetAttribute(pass2_kernel<float, 5, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 112 * 1024);
-        if (e == cudaSuccess) attr[fp64 ? 1 : 0] = 1;
-    }
-    if (e != cudaSuccess) return qgt_set_error(-6, "pass2: %s", cudaGetErrorString(e));
-    if (fp64 && a->ckpt) pass2_kernel<double, 4, true><<<grid, 256, smem, (cudaStream_t)stream>>>(*a);
-    else if (fp64) pass2_kernel<double, 4, false><<<grid, 256, smem, (cudaStream_t)stream>>>(*a);
-    else if (a->ckpt) pass2_kernel<float, 5, true><<<grid, 256, smem, (cudaStream_t)stream>>>(*a);
-    else pass2_kernel<float, 5, false><<<grid, 256, smem, (cudaStream_t)stream>>>(*a);
-    return qgt_dev_last_error();
+    const size_t smax = wide ? 200 * 1024 : 112 * 1024;
+    if (smem > smax) return qgt_set_error(-1, "pass2: program of %d ops too large", a->nops);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (fp64) return pass2_launch<double, 4, 3>(a, grid, smem, smax, s);
+    if (wide) return pass2_launch<float, 5, 4>(a, grid, smem, smax, s);
+    return pass2_launch<float, 5, 3>(a, grid, smem, smax, s);
 }

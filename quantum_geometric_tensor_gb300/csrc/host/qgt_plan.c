@@ -158,6 +158,7 @@ struct qgt_plan {
     float split_scale;
     int64_t device_bytes;
     int64_t vector_passes, gate_bytes;
+    int wide;                     /* complex64 passes on 14-bit tiles (choose_tile) */
     int launches;
     int has_run;
     void* prof_ev[7];             /* phase events of qgt_plan_profile_step (NULL otherwise) */
@@ -290,10 +291,18 @@ static int mirror_backward_passes(qgt_plan_t* p)
     return 0;
 }
 
+/* width of a full register-resident tile: complex128 12 bits; complex64 13 bits, or 14 when
+ * choose_tile found that they save vector passes */
+static int full_tile_bits(const qgt_plan_t* p)
+{
+    if (p->fp64) return QGT_TILE_MAX_F64;
+    return p->wide ? QGT_TILE_WIDE_F32 : QGT_TILE_MAX_F32;
+}
+
 static int compile_schedule(qgt_plan_t* p)
 {
     const int n = p->n, G = p->ngates;
-    const int tmax = n < (p->fp64 ? QGT_TILE_MAX_F64 : QGT_TILE_MAX_F32) ? n : (p->fp64 ? QGT_TILE_MAX_F64 : QGT_TILE_MAX_F32);
+    const int tmax = n < full_tile_bits(p) ? n : full_tile_bits(p);
     const int lane = n < QGT_LANE_BITS ? n : QGT_LANE_BITS;
     char* placed = (char*)calloc((size_t)G + 1, 1);
     int* blocked = (int*)malloc(sizeof(int) * ((size_t)G + 1));
@@ -400,6 +409,37 @@ static int compile_schedule(qgt_plan_t* p)
     free(blocked);
     free(order);
     return p->mitm ? mirror_backward_passes(p) : 0;
+}
+
+static int build_entries(qgt_plan_t* p);
+static int build_entries_mitm(qgt_plan_t* p);
+
+static void free_schedule(qgt_plan_t* p)
+{
+    free(p->passes); free(p->ops_h); free(p->ents_h);
+    free(p->scale_ptr_h); free(p->scale_src_h); free(p->row_group_h);
+    p->passes = NULL; p->ops_h = NULL; p->ents_h = NULL;
+    p->scale_ptr_h = NULL; p->scale_src_h = NULL; p->row_group_h = NULL;
+}
+
+/* complex64 plans of 14 or more qubits: 14-bit tiles (512-thread CTAs, one per SM) when their
+ * schedule needs at least 8 % fewer vector passes than 13-bit tiles (two 256-thread CTAs per
+ * SM), the cost of a vector pass being about 8 % higher with the wide tile */
+static int choose_tile(qgt_plan_t* p)
+{
+    p->wide = 0;
+    if (p->fp64 || p->n < QGT_TILE_WIDE_F32) return 0;
+    int64_t vp[2];
+    for (int w = 1; w >= 0; w--) {
+        p->wide = w;
+        int rc = compile_schedule(p);
+        if (!rc) rc = p->mitm ? build_entries_mitm(p) : build_entries(p);
+        vp[w] = p->vector_passes;
+        free_schedule(p);
+        if (rc) return rc;
+    }
+    p->wide = 100 * vp[1] <= 92 * vp[0];
+    return 0;
 }
 
 /* entries: psi ping-pongs between row 0 and row `rows`, ending in row 0 */
@@ -712,7 +752,7 @@ static int build_entries_mitm(qgt_plan_t* p)
  * shared-memory re-layouts are few.  SWAP becomes three CNOTs. */
 static int build_programs(qgt_plan_t* p)
 {
-    const int tb = p->fp64 ? QGT_TILE_MAX_F64 : QGT_TILE_MAX_F32;
+    const int tb = full_tile_bits(p);
     const int RB = p->fp64 ? 4 : 5;
     int cap = 3 * p->nops + 2 * p->npasses + 16, scap = 2 * p->nops + p->npasses + 16;
     p->prog_h = (qgt_dev_op2_t*)calloc((size_t)cap, sizeof(qgt_dev_op2_t));
@@ -1273,6 +1313,7 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
         free(fill);
     }
     if ((rc = setup_transport(p)) != 0) goto fail;
+    if ((rc = choose_tile(p)) != 0) goto fail;
     if ((rc = compile_schedule(p)) != 0) goto fail;
     if ((rc = (p->mitm ? build_entries_mitm(p) : build_entries(p))) != 0) goto fail;
     if ((rc = build_programs(p)) != 0) goto fail;

@@ -25,6 +25,7 @@ extern "C" {
 
 #define QGT_MAX_QUBITS 30
 #define QGT_TILE_MAX_F32 13   /* 2^13 complex64 = 64 KiB of shared memory */
+#define QGT_TILE_WIDE_F32 14  /* 2^14 complex64 = 128 KiB: registers tiles of 512 threads, from 14 qubits */
 #define QGT_TILE_MAX_F64 12   /* 2^12 complex128 = 64 KiB */
 #define QGT_LANE_BITS 5       /* qubits 0..4 are always tile bits: 256 B coalesced segments */
 #define QGT_PASS_THREADS 256
