@@ -298,7 +298,7 @@ def run_gb300(args, ws, rank, local):
         except Exception:
             traffic = None
     if dom == "passes":
-        roof = {"bound": "hbm", "kernel": "pass2_kernel<float,5> (all tile passes of a step)", "achieved": gate_gbs,
+        roof = {"bound": "hbm", "kernel": "pass2_kernel (all register-tile passes of a step)", "achieved": gate_gbs,
                 "peak": hbm, "unit": "GB/s", "frac": gate_gbs / hbm, "traffic": traffic,
                 "peak_source": peak_src, "algorithmic_bytes": info.gate_bytes, "ms": prof.passes_ms}
     else:
