@@ -122,3 +122,25 @@ def test_reused_output_buffers(Q):
         assert np.array_equal(out["natgrad"], ref["natgrad"]) and out["energy"] == ref["energy"]
         with pytest.raises(ValueError):
             p.run(ref["grad"], out={"Q": np.zeros((1, P, P))})
+
+
+def test_wide_tiles_against_fp64(Q):
+    """19 qubits, 8 layers: the scheduler takes 14-qubit register tiles (512-thread CTAs; 6 passes
+    instead of 9), with 32 tiles per vector and segment checkpoints; single and batched complex64
+    plans against the FP64 plan (12-qubit tiles)."""
+    n, L = 19, 8
+    gates = Q.ansatz_gates(n, L, "cz")
+    P = 2 * n * L
+    th = np.stack([O.splitmix64_params(90, P), O.splitmix64_params(91, P)])
+    with Q.Plan(n, gates, P, precision=Q.FP64) as p64:
+        ref = p64.run(th[0])
+    with Q.Plan(n, gates, P, precision=Q.MIXED) as pm:
+        assert pm.info().tile_bits == 14
+        out = pm.run(th[0])
+    with Q.Plan(n, gates, P, precision=Q.MIXED, batch=2) as pb:
+        outb = pb.run(th)
+    for o in (out, {k: (v[0] if v is not None else None) for k, v in outb.items()}):
+        assert rel(o["Q"].real, ref["Q"].real) < 1e-6
+        assert rel(o["Q"], ref["Q"]) < 2e-6
+        assert rel(o["grad"], ref["grad"]) < 2e-6
+        assert abs(o["energy"] - ref["energy"]) < 1e-6
