@@ -27,7 +27,7 @@
 //                      {Re D, Im D, -Re D, Re l1, Im l1, -Re l1, Re l2, Im l2,
 //                      -Re l2}, so that every (Re, Im) pair of B operands that
 //                      one A plane meets is two adjacent planes; B planes
-//                      hold the block's valid rows rounded up to 32 (rbB)
+//                      hold the block's valid rows rounded up to 16 (rbB)
 //   1 thread: 12 tcgen05.mma (M = 128, N = 2 rbB <= 256 = [Re partner |
 //             Im partner], K = 16) per k-step into TMEM [D*D Re | D*D Im |
 //             rest Re | rest Im] (two regions of 256 columns)
@@ -157,20 +157,18 @@ static __device__ __forceinline__ void umma_commit(uint32_t bar)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-static __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
+static __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
 {
-    uint32_t r[32];
+    uint32_t r[16];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
 static __device__ __forceinline__ void pair_of(int tp, int nb, int* mb, int* nbo)
@@ -226,10 +224,10 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
     pair_of((int)(blockIdx.x % ntp), nbk, &mb, &nbo);
     const bool diag = (mb == nbo);
     const int nblk = diag ? 1 : 2;
-    // the B block's planes hold its valid rows rounded up to 32 (the last block of a plan is
+    // the B block's planes hold its valid rows rounded up to 16 (the last block of a plan is
     // partly padding): plane stride pbB, MMA N = 2 rbB ([Re partner | Im partner])
     const int vb = rows - 128 * nbo < 128 ? rows - 128 * nbo : 128;
-    const int rbB = (vb + 31) & ~31;
+    const int rbB = (vb + 15) & ~15;
     const uint32_t pbB = (uint32_t)rbB * DG_BK * 2;
     const int64_t k0 = (int64_t)(blockIdx.x / ntp) * kchunk;
     int64_t k1 = k0 + kchunk;
@@ -349,7 +347,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
 #pragma unroll
                 for (int it = 0; it < 128 / (4 * DG_CONV_WARPS); it++) {
                     const int rr = 4 * cw + 4 * DG_CONV_WARPS * it;
-                    if (rr >= rlim) break;   // warp-uniform: rlim is a multiple of 32
+                    if (rr >= rlim) break;   // warp-uniform (rr depends on the warp only)
                     const int r = rr + sub;
                     const float4 q = *reinterpret_cast<const float4*>(raw + r * 32 + 2 * kp);
                     const float iu = inv_u[b][r];
@@ -393,18 +391,18 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
         const int row = quad * 32 + lane;
         if (ok) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            float hh[32], rsd[32];
+            float hh[16], rsd[16];
             const uint32_t lanebase = tmem + ((uint32_t)(quad * 32) << 16);
             for (int ri = 0; ri < 2; ri++) {
-                for (int c = 2 * half; c < 2 * half + 2; c++) {
-                    if (c * 32 >= rbB) continue;   // columns past the B block's rows (never read)
-                    tmem_ld32(lanebase + ri * rbB + c * 32, hh);
-                    tmem_ld32(lanebase + 256 + ri * rbB + c * 32, rsd);
-                    if (diag && ri == 0 && c == (row >> 5) && hh[row & 31] > 8388608.0f)
+                for (int c = 4 * half; c < 4 * half + 4; c++) {   // chunks of 16 columns
+                    if (c * 16 >= rbB) continue;   // columns past the B block's rows (never read)
+                    tmem_ld16(lanebase + ri * rbB + c * 16, hh);
+                    tmem_ld16(lanebase + 256 + ri * rbB + c * 16, rsd);
+                    if (diag && ri == 0 && c == (row >> 4) && hh[row & 15] > 8388608.0f)
                         atomicExch(err, DG_ERR_INEXACT);
-                    float4* o = reinterpret_cast<float4*>(out + ri * 128 * 128 + row * 128 + c * 32);
+                    float4* o = reinterpret_cast<float4*>(out + ri * 128 * 128 + row * 128 + c * 16);
 #pragma unroll
-                    for (int j = 0; j < 8; j++)
+                    for (int j = 0; j < 4; j++)
                         o[j] = make_float4(hh[4 * j] + rsd[4 * j], hh[4 * j + 1] + rsd[4 * j + 1],
                                            hh[4 * j + 2] + rsd[4 * j + 2], hh[4 * j + 3] + rsd[4 * j + 3]);
                 }
