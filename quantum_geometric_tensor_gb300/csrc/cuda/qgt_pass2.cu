@@ -1,13 +1,13 @@
 // qgt_pass2.cu -- register-resident tile passes (the gate-application hot path).
 //
-// A full tile (2^13 complex64 or 2^12 complex128 amplitudes) is held in the
+// A full tile (2^13 or 2^14 complex64, or 2^12 complex128 amplitudes) is held in the
 // registers of one CTA of 2^WB warps (256 or 512 threads): each thread owns NR = 2^RB amplitudes
 // (RB = 5 for complex64, 4 for complex128).  The tile's local bits play three
 // roles:
 //   lane bits  0..4   (always; physical qubits 0..4, so every global access of
 //                      a warp is 32 consecutive amplitudes)
 //   reg bits   RB bits chosen per segment (index into the thread's registers)
-//   warp bits  the remaining 3 bits (the warp index)
+//   warp bits  the remaining WB = 3 or 4 bits (the warp index)
 // A pass is compiled on the host into a program of segments.  Within a
 // segment every non-diagonal gate acts on a reg bit (in-register butterfly,
 // statically indexed) or a lane bit (warp shuffle); diagonal gates act on any

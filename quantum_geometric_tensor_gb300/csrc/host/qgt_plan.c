@@ -745,8 +745,8 @@ static int build_entries_mitm(qgt_plan_t* p)
 }
 
 /* Register-resident programs for passes whose tile has the full width
- * (13 bits complex64 / 12 bits complex128).  Lanes are local bits 0..4; the
- * other local bits are split into RB register bits and 3 warp bits per
+ * (13 or 14 bits complex64 / 12 bits complex128).  Lanes are local bits 0..4;
+ * the other local bits are split into RB register bits and 3 (or 4) warp bits per
  * segment.  A gate whose target is a warp bit opens a new segment whose
  * register bits are the next distinct targets (looking ahead), so that the
  * shared-memory re-layouts are few.  SWAP becomes three CNOTs. */
