@@ -157,6 +157,22 @@ static __device__ __forceinline__ void umma_commit(uint32_t bar)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
+static __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
 static __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
 {
     uint32_t r[16];
@@ -391,20 +407,40 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
         const int row = quad * 32 + lane;
         if (ok) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            float hh[16], rsd[16];
             const uint32_t lanebase = tmem + ((uint32_t)(quad * 32) << 16);
-            for (int ri = 0; ri < 2; ri++) {
-                for (int c = 4 * half; c < 4 * half + 4; c++) {   // chunks of 16 columns
-                    if (c * 16 >= rbB) continue;   // columns past the B block's rows (never read)
-                    tmem_ld16(lanebase + ri * rbB + c * 16, hh);
-                    tmem_ld16(lanebase + 256 + ri * rbB + c * 16, rsd);
-                    if (diag && ri == 0 && c == (row >> 4) && hh[row & 15] > 8388608.0f)
-                        atomicExch(err, DG_ERR_INEXACT);
-                    float4* o = reinterpret_cast<float4*>(out + ri * 128 * 128 + row * 128 + c * 16);
+            if ((rbB & 31) == 0) {
+                // 32-column chunks (full blocks and rows rounded to 32)
+                float hh[32], rsd[32];
+                for (int ri = 0; ri < 2; ri++) {
+                    for (int c = 2 * half; c < 2 * half + 2; c++) {
+                        if (c * 32 >= rbB) continue;   // columns past the B block's rows (never read)
+                        tmem_ld32(lanebase + ri * rbB + c * 32, hh);
+                        tmem_ld32(lanebase + 256 + ri * rbB + c * 32, rsd);
+                        if (diag && ri == 0 && c == (row >> 5) && hh[row & 31] > 8388608.0f)
+                            atomicExch(err, DG_ERR_INEXACT);
+                        float4* o = reinterpret_cast<float4*>(out + ri * 128 * 128 + row * 128 + c * 32);
 #pragma unroll
-                    for (int j = 0; j < 4; j++)
-                        o[j] = make_float4(hh[4 * j] + rsd[4 * j], hh[4 * j + 1] + rsd[4 * j + 1],
-                                           hh[4 * j + 2] + rsd[4 * j + 2], hh[4 * j + 3] + rsd[4 * j + 3]);
+                        for (int j = 0; j < 8; j++)
+                            o[j] = make_float4(hh[4 * j] + rsd[4 * j], hh[4 * j + 1] + rsd[4 * j + 1],
+                                               hh[4 * j + 2] + rsd[4 * j + 2], hh[4 * j + 3] + rsd[4 * j + 3]);
+                    }
+                }
+            } else {
+                // 16-column chunks: the Im half starts at column rbB, a multiple of 16
+                float hh[16], rsd[16];
+                for (int ri = 0; ri < 2; ri++) {
+                    for (int c = 4 * half; c < 4 * half + 4; c++) {
+                        if (c * 16 >= rbB) continue;
+                        tmem_ld16(lanebase + ri * rbB + c * 16, hh);
+                        tmem_ld16(lanebase + 256 + ri * rbB + c * 16, rsd);
+                        if (diag && ri == 0 && c == (row >> 4) && hh[row & 15] > 8388608.0f)
+                            atomicExch(err, DG_ERR_INEXACT);
+                        float4* o = reinterpret_cast<float4*>(out + ri * 128 * 128 + row * 128 + c * 16);
+#pragma unroll
+                        for (int j = 0; j < 4; j++)
+                            o[j] = make_float4(hh[4 * j] + rsd[4 * j], hh[4 * j + 1] + rsd[4 * j + 1],
+                                               hh[4 * j + 2] + rsd[4 * j + 2], hh[4 * j + 3] + rsd[4 * j + 3]);
+                    }
                 }
             }
         } else {
