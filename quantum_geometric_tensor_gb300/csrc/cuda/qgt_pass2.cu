@@ -1,8 +1,8 @@
 // qgt_pass2.cu -- register-resident tile passes (the gate-application hot path).
 //
-// A full tile (2^13 or 2^14 complex64, or 2^12 complex128 amplitudes) is held in the
+// A full tile (2^12, 2^13 or 2^14 complex64, or 2^12 complex128 amplitudes) is held in the
 // registers of one CTA of 2^WB warps (256 or 512 threads): each thread owns NR = 2^RB amplitudes
-// (RB = 5 for complex64, 4 for complex128).  The tile's local bits play three
+// (RB = 5 for complex64 tiles of 13 or 14 bits, 4 for 12-bit tiles and complex128).  The tile's local bits play three
 // roles:
 //   lane bits  0..4   (always; physical qubits 0..4, so every global access of
 //                      a warp is 32 consecutive amplitudes)
@@ -320,7 +320,8 @@ __device__ __forceinline__ uint32_t role_mask(int role, int q, int lane, int war
 // CKPT: the launch's entries also store their state before every Q2_SEG op whose slot is >= 0 (the
 // checkpoint writers of a pass; spawns then run the program from that segment on)
 template <typename R, int RB, int WB, bool CKPT>
-__global__ void __launch_bounds__(32 << WB, (WB >= 4) ? 1 : 2) pass2_kernel(const qgt_dev_pass2_args_t a)
+__global__ void __launch_bounds__(32 << WB, (WB >= 4) ? 1 : ((sizeof(R) == 4 && RB == 4) ? 3 : 2))
+    pass2_kernel(const qgt_dev_pass2_args_t a)
 {
     typedef typename v2of<R>::T T;
     constexpr int NR = 1 << RB;
@@ -706,10 +707,12 @@ static int pass2_launch(const qgt_dev_pass2_args_t* a, dim3 grid, size_t smem, s
 extern "C" int qgt_dev_pass2(const qgt_dev_pass2_args_t* a, int fp64, void* stream)
 {
     if (a->nentries <= 0) return 0;
-    // tiles: complex128 12 bits (4 register, 3 warp bits); complex64 13 bits (5 register, 3 warp
-    // bits, 2 CTAs per SM) or 14 bits (5 register, 4 warp bits: 512 threads, 1 CTA per SM)
+    // tiles: complex128 12 bits (4 register, 3 warp bits); complex64 12 bits (4 register, 3 warp
+    // bits: 12-qubit circuits), 13 bits (5 register, 3 warp bits, 2 CTAs per SM) or 14 bits
+    // (5 register, 4 warp bits: 512 threads, 1 CTA per SM)
     const bool ok = fp64 ? a->tile_bits == QGT_TILE_MAX_F64
-                         : (a->tile_bits == QGT_TILE_MAX_F32 || a->tile_bits == QGT_TILE_WIDE_F32);
+                         : (a->tile_bits == QGT_TILE_MAX_F64 || a->tile_bits == QGT_TILE_MAX_F32 ||
+                            a->tile_bits == QGT_TILE_WIDE_F32);
     if (!ok) return qgt_set_error(-1, "pass2: tile of %d bits not supported", a->tile_bits);
     int64_t ntiles = (int64_t)1 << (a->n - a->tile_bits);
     const int np = a->npoints > 0 ? a->npoints : 1;
@@ -723,5 +726,6 @@ extern "C" int qgt_dev_pass2(const qgt_dev_pass2_args_t* a, int fp64, void* stre
     cudaStream_t s = (cudaStream_t)stream;
     if (fp64) return pass2_launch<double, 4, 3>(a, grid, smem, smax, s);
     if (wide) return pass2_launch<float, 5, 4>(a, grid, smem, smax, s);
+    if (a->tile_bits == QGT_TILE_MAX_F64) return pass2_launch<float, 4, 3>(a, grid, smem, smax, s);
     return pass2_launch<float, 5, 3>(a, grid, smem, smax, s);
 }

@@ -296,8 +296,13 @@ static int mirror_backward_passes(qgt_plan_t* p)
 static int full_tile_bits(const qgt_plan_t* p)
 {
     if (p->fp64) return QGT_TILE_MAX_F64;
+    if (p->n == QGT_TILE_MAX_F64) return QGT_TILE_MAX_F64;   /* 12 qubits: one 12-bit tile, 16 registers */
     return p->wide ? QGT_TILE_WIDE_F32 : QGT_TILE_MAX_F32;
 }
+
+/* register bits of the plan's register-resident tiles: 4 for complex128 and for 12-bit complex64
+ * tiles, 5 otherwise */
+static int reg_bits(const qgt_plan_t* p) { return (p->fp64 || full_tile_bits(p) == QGT_TILE_MAX_F64) ? 4 : 5; }
 
 static int compile_schedule(qgt_plan_t* p)
 {
@@ -753,7 +758,7 @@ static int build_entries_mitm(qgt_plan_t* p)
 static int build_programs(qgt_plan_t* p)
 {
     const int tb = full_tile_bits(p);
-    const int RB = p->fp64 ? 4 : 5;
+    const int RB = reg_bits(p);
     int cap = 3 * p->nops + 2 * p->npasses + 16, scap = 2 * p->nops + p->npasses + 16;
     p->prog_h = (qgt_dev_op2_t*)calloc((size_t)cap, sizeof(qgt_dev_op2_t));
     p->segs_h = (int8_t*)calloc((size_t)scap * 16, 1);
@@ -905,7 +910,7 @@ static int comb_entry(qgt_plan_t* p, const int* list, int n)
 static int emit_diag_run(qgt_plan_t* p, const qgt_dev_op2_t* src, int j, int e, qgt_dev_op2_t* out_ops, int* out,
                          int nb, int* remap)
 {
-    const int RB = p->fp64 ? 4 : 5;
+    const int RB = reg_bits(p);
     int lists[40][64];
     int nl[40];
     int8_t role[40];
