@@ -16,9 +16,11 @@ The gb300 arm prints one JSON line with value (device-resident theta and
 outputs), e2e (host buffers through qgt_plan_execute_host), roofline of the
 dominant kernel, the FP64 GPU path timed on the same point with the mixed
 path's error against it, clocks sampled during the timed region, and the
-oracle's CPU baseline.  The reference arm times the CPU implementation of the
-path (the FP64 oracle port of the reference algorithms; the reference's own
-tree is not present on the GPU host) on the host cores.
+oracle's CPU baseline (one complete QGT step on the host cores, measured).
+The reference arm times the CPU implementation of the path (the FP64 oracle
+port of the reference algorithms; the reference's own tree is not present on
+the GPU host) on the host cores: its K steps are the K slices of one complete
+QGT step, so their total time is one measured QGT.
 """
 from __future__ import annotations
 
@@ -133,79 +135,79 @@ def replica_value(ms_max: float, ws: int) -> float:
     return ws * 1000.0 / ms_max
 
 
-def cpu_baseline(threads: int | None = None, S: int = 16):
-    """The FP64 oracle on the host cores on a bounded sample of the workload,
-    extrapolated to one full QGT step:
-      derivative generation: all 480 gates on psi + the first S parameters'
-        derivative vectors (the longest-lived ones); cost per vector-gate
-        application x the exact count for all 320 derivatives;
-      contraction: the Gram of S rows x 2^20 amplitudes; cost per pair x P(P+1)/2;
-      energy, gradient and Cholesky solve: measured in full."""
+def workload_config(ws: int = 1) -> dict:
+    """The workload of both arms (identical dicts: implementation details live outside it)."""
+    return {"workload": WORKLOAD, "qubits": N_QUBITS, "layers": LAYERS, "params": 2 * N_QUBITS * LAYERS,
+            "entangler": "cz_ring", "hamiltonian": "tfim_ring J=h=1", "lambda": LAMBDA,
+            "parallelism": f"replicas{ws}" if ws > 1 else "single",
+            "l2": "working set > L2 (3.6 GB device, 5.4 GB host): no flush needed"}
+
+
+def cpu_qgt_job(slices: int):
+    """The FP64 CPU oracle's full QGT step of the headline workload, cut into `slices` calls that
+    together compute one complete QGT (psi, all 320 derivative states, the full Gram, projector,
+    TFIM energy and gradient, Cholesky step), each piece of work once."""
     from oracle import oracle as O
     O.build()
     orc = O.Oracle()
-    if threads:
-        os.environ["OMP_NUM_THREADS"] = str(threads)
     g = O.ansatz(N_QUBITS, LAYERS, ENT)
-    P = O.num_params(g)
-    th = O.splitmix64_params(SEED, P)
-    # keep only the first S parameters as parameters (others fixed) for the sample
-    gs = g.copy()
-    for i in range(len(gs)):
-        if gs[i]["param"] >= S:
-            gs[i]["angle"] = th[gs[i]["param"]]
-            gs[i]["param"] = -1
+    th = O.splitmix64_params(SEED, O.num_params(g))
+    return orc.qgt_job(N_QUBITS, g, th, slices, 1.0, 1.0, LAMBDA)
+
+
+def cpu_baseline(slices: int = 20):
+    """One complete QGT step of the workload on the host cores (OpenMP, all threads), timed end to
+    end: no extrapolation."""
+    job = cpu_qgt_job(slices)
     t0 = time.perf_counter()
-    psi, D = orc.derivatives(N_QUBITS, gs, th[:S], S)
-    t_deriv = time.perf_counter() - t0
-    live, a_sample, a_full = 0, 0, 0
-    live_full = 0
-    for gt in g:
-        a_full += 1 + live_full
-        if gt["param"] >= 0:
-            live_full += 1
-    for gt in gs:
-        a_sample += 1 + live
-        if gt["param"] >= 0:
-            live += 1
-    t_deriv_full = t_deriv / a_sample * a_full
-    t0 = time.perf_counter()
-    orc.qgt_from_states(psi, D)
-    t_gram = time.perf_counter() - t0
-    t_gram_full = t_gram / (S * (S + 1) / 2 + S) * (P * (P + 1) / 2 + P)
-    t0 = time.perf_counter()
-    hp = orc.tfim_apply(N_QUBITS, psi)
-    orc.energy_grad(D, hp)
-    A = np.eye(P) * 0.25
-    orc.cholesky_solve(A, np.ones(P), LAMBDA)
-    t_rest = time.perf_counter() - t0
-    total = t_deriv_full + t_gram_full + t_rest
+    while job.step() > 0:
+        pass
+    total = time.perf_counter() - t0
+    job.close()
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return {"value": 1.0 / total, "unit": "QGTs/sec", "cores": cores, "kind": "port",
-            "sample": (f"20q/8 layers, psi + {S} of {P} derivative states through all 480 gates "
-                       f"({t_deriv:.1f} s) and their {S}x{S} Gram ({t_gram:.1f} s), extrapolated by exact "
-                       f"vector-gate ({a_full}/{a_sample}) and pair counts; {total:.0f} s per QGT"),
+            "sample": (f"one full QGT step of the workload on the host (FP64 oracle port, OpenMP {cores} threads): "
+                       f"psi + all 320 derivative states through the 480 gates, full 320x320 Gram, projector, "
+                       f"TFIM energy/gradient, Cholesky step; {total:.1f} s measured"),
             "seconds_per_qgt": total}
 
 
 def run_reference(args, ws, rank):
+    """The CPU implementation of the path (FP64 oracle port of the reference algorithms) on the host
+    cores.  A step is 1/K of one full QGT step of the workload (K = --steps): a slice of the 320
+    derivative states with their Gram rows, the last step also the projector, gradient and solve, so
+    the K timed steps compute exactly one complete QGT and value = 1 / (their total time)."""
     if rank != 0:
         return 0
-    vals = []
-    for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(S=4)   # ~7 s of host work per step
-        if i >= args.warmup:
-            vals.append(cb["value"])
-    v = statistics.mean(vals)
-    line = {"metric": METRIC, "value": v, "unit": "QGTs/sec", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "qubits": N_QUBITS, "layers": LAYERS, "params": 320,
-                       "entangler": "cz_ring", "hamiltonian": "tfim_ring J=h=1", "lambda": LAMBDA},
+    K, W = max(1, args.steps), max(0, args.warmup)
+    if W:
+        warm = cpu_qgt_job(K)
+        for _ in range(min(W, warm.slices)):
+            warm.step()
+        warm.close()
+    job = cpu_qgt_job(K)
+    ts = []
+    t_all = time.perf_counter()
+    for _ in range(job.slices):
+        t0 = time.perf_counter()
+        job.step()
+        ts.append(time.perf_counter() - t0)
+    total = time.perf_counter() - t_all
+    job.close()
+    steps = len(ts)
+    v = 1.0 / total
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    sample = (f"{steps} steps = one full QGT step of the workload (each 1/{steps} of it: a slice of the 320 "
+              f"derivative states through the remaining gates and their Gram rows; the last step also the "
+              f"projector, TFIM gradient and Cholesky solve); FP64 oracle port, OpenMP {cores} threads; "
+              f"{total:.1f} s measured")
+    line = {"metric": METRIC, "value": v, "unit": "QGTs/sec", "n_gpus": ws, "steps": steps,
+            "warmup": W, "ms_per_step": 1000.0 * total / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(ws),
             "impl": "reference",
-            "cpu_baseline": {"value": v, "unit": "QGTs/sec", "cores": cb["cores"], "kind": cb["kind"],
-                             "sample": cb["sample"]},
-            "e2e": {"value": v, "unit": "QGTs/sec", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "cpu_baseline": {"value": v, "unit": "QGTs/sec", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "QGTs/sec", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "step_seconds": [round(t, 3) for t in ts]}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -344,10 +346,12 @@ def run_gb300(args, ws, rank, local):
     line = {"metric": METRIC, "value": value, "unit": "QGTs/sec", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64/fp16-digits/f64", "data": "synthetic",
-            "config": {"workload": workload, "qubits": nq, "layers": nl, "params": P,
-                       "entangler": "cz_ring", "hamiltonian": "tfim_ring J=h=1", "lambda": LAMBDA,
-                       "precision": "mixed", "parallelism": f"replicas{ws}" if ws > 1 else "single",
-                       "l2": f"working set {info.device_bytes / 1e9:.1f} GB > L2 (no flush needed)"},
+            "config": workload_config(ws) if workload == WORKLOAD else
+            {"workload": workload, "qubits": nq, "layers": nl, "params": P, "entangler": "cz_ring",
+             "hamiltonian": "tfim_ring J=h=1", "lambda": LAMBDA,
+             "parallelism": f"replicas{ws}" if ws > 1 else "single",
+             "l2": f"working set {info.device_bytes / 1e9:.1f} GB > L2 (no flush needed)"},
+            "precision": "mixed (complex64 evolution, FP16-digit tcgen05 Gram, FP64 projector and solve)",
             "e2e": {"value": ws * 1000.0 / e2e_ms, "unit": "QGTs/sec", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
             "gpu_launches": info.num_launches * args.steps,

@@ -371,6 +371,17 @@ int qgt_cholesky_solve_f64(const double* A, const double* g, double lambda, int3
 int qgt_cholesky_solve_f64_noalloc(const double* A, const double* g, double lambda, int32_t P,
                                    double* x, double* lambda_used);
 
+/* Fault-injection hook for tests of the failure path (no reference
+ * counterpart).  Every mbarrier wait of the integer-digit Gram kernel is
+ * bounded by the GPU's global timer; when one runs out the CTA stops, waits
+ * (bounded) for its own TMA loads and MMAs in flight, frees its tensor memory
+ * and records QGT_ERROR_TIMEOUT, which the step then returns.  With stall = 1
+ * the kernel's converter warps wait on a barrier that nothing arrives on, so
+ * that limit (timeout_ns, in (0, 4e9]) runs out on purpose; stall = 0 and
+ * timeout_ns = 0 restore the default (no stall, 4 s limit).  Plans of
+ * MIXED precision with more than 8 rows only; no GPU fault is involved. */
+int qgt_plan_test_gram_stall(qgt_plan_t* plan, int stall, int64_t timeout_ns);
+
 /* Thread-local text of the last error. */
 const char* qgt_last_error(void);
 /* Library version string. */

@@ -14,6 +14,9 @@ extern "C" {
 qgt_error_t geometric_create_metric(quantum_geometric_metric_t** metric, geometric_metric_type_t type,
                                     size_t dimension);
 void geometric_destroy_metric(quantum_geometric_metric_t* metric);
+/* the state-space metric of a state: Euclidean unchanged, Fubini-Study
+ * delta_ij - conj(psi_i) psi_j (dimension = the state's dimension) */
+qgt_error_t geometric_compute_metric(quantum_geometric_metric_t* metric, const quantum_state_t* state);
 qgt_error_t geometric_clone_metric(quantum_geometric_metric_t** dest, const quantum_geometric_metric_t* src);
 qgt_error_t geometric_compute_fubini_study_metric(quantum_geometric_metric_t* metric,
                                                   const quantum_geometric_tensor_network_t* qgtn,

@@ -1,8 +1,8 @@
 /*
- * quantum_types.h -- gate and circuit structs of the reference ABI, same
- * field order (reference: include/quantum_geometric/core/quantum_types.h:
- * 170-190 quantum_gate_t, 238-274 circuit_layer_t / quantum_circuit_t).
- * Types this path never dereferences are kept opaque.
+ * quantum_types.h -- gate, circuit and state structs of the reference ABI,
+ * same field order (reference: include/quantum_geometric/core/quantum_types.h:
+ * 170-190 quantum_gate_t, 195-232 quantum_state_t, 238-274 circuit_layer_t /
+ * quantum_circuit_t).  Types this path never dereferences are kept opaque.
  */
 #ifndef QUANTUM_TYPES_H
 #define QUANTUM_TYPES_H
@@ -29,6 +29,38 @@ struct quantum_gate_t {
     size_t num_parameters;
     ComplexFloat* matrix;
     void* custom_data;
+};
+
+typedef struct quantum_state_t quantum_state_t;
+typedef struct StabilizerMeasurement StabilizerMeasurement;
+typedef struct TopologicalAnyon TopologicalAnyon;
+
+/* geometric_compute_metric reads dimension and coordinates; the other fields
+ * keep the reference layout */
+struct quantum_state_t {
+    quantum_state_type_t type;
+    size_t num_qubits;
+    size_t dimension;
+    size_t manifold_dim;
+    ComplexFloat* coordinates;
+    ComplexFloat* metric;
+    ComplexFloat* connection;
+    void* auxiliary_data;
+    bool is_normalized;
+    HardwareType hardware;
+    size_t lattice_width;
+    size_t lattice_height;
+    size_t num_stabilizers;
+    size_t num_plaquettes;
+    size_t num_vertices;
+    StabilizerMeasurement* stabilizers;
+    size_t num_anyons;
+    size_t max_anyons;
+    TopologicalAnyon* anyons;
+    double* syndrome_values;
+    size_t syndrome_size;
+    double* measurement_confidence;
+    size_t confidence_size;
 };
 
 typedef struct circuit_layer_t {

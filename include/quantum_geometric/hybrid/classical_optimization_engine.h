@@ -2,9 +2,9 @@
  * classical_optimization_engine.h -- the natural-gradient solve consumed by
  * the reference's optimiser (reference: src/quantum_geometric/hybrid/
  * classical_optimization_engine.c:613-623, where the GPU variant falls back
- * to the CPU CG).  Here it is an FP64 Cholesky solve of F x = g on the GPU
- * (lambda starts at 0 and grows x10 from 1e-12 * max diag(F) when F is not
- * positive definite).
+ * to the CPU CG of :543-611).  Here the same conjugate-gradient iteration
+ * (x0 = 0, at most 100 steps, stop at |p^T F p| < 1e-15 or |r| < 1e-8) runs
+ * on the GPU in FP64.
  */
 #ifndef QUANTUM_GEOMETRIC_CLASSICAL_OPTIMIZATION_ENGINE_H
 #define QUANTUM_GEOMETRIC_CLASSICAL_OPTIMIZATION_ENGINE_H

@@ -31,9 +31,14 @@ ROTATIONS = (RX, RY, RZ)
 GATE_DTYPE = np.dtype([("type", "<i4"), ("q0", "<i4"), ("q1", "<i4"), ("param", "<i4"), ("angle", "<f8")])
 
 
-def build(quiet: bool = True) -> None:
-    """Compile the oracle (and oracle/_ref when the reference tree exists)."""
-    out = subprocess.run(["make", "-C", HERE, "-j4"], capture_output=True, text=True)
+def build(quiet: bool = True, ref_tree: str | None = None) -> None:
+    """Compile the oracle, and oracle/_ref from the reference tree at ref_tree
+    (or at $QGT_REFERENCE_TREE) when one is given and present."""
+    tree = ref_tree or os.environ.get("QGT_REFERENCE_TREE")
+    cmd = ["make", "-C", HERE, "-j4"]
+    if tree and os.path.isdir(os.path.join(tree, "src", "quantum_geometric")):
+        cmd.append(f"REF={tree}")
+    out = subprocess.run(cmd, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
 
@@ -113,6 +118,15 @@ class Oracle:
         L.or_seed_params.argtypes = [C.c_uint64, i32, vp]
         L.or_berry_phase.argtypes = [vp, sz, sz, vp]
         L.or_berry_flux.argtypes = [i32, vp, i32, vp, i32, i32, i32, i32, i32, f64, f64, f64, f64, i32, vp]
+        L.or_qgt_job_create.argtypes = [i32, vp, i32, vp, i32, i32, f64, f64, f64, vp, vp, vp, vp]
+        L.or_qgt_job_create.restype = vp
+        L.or_qgt_job_slices.argtypes = [vp]
+        L.or_qgt_job_step.argtypes = [vp]
+        L.or_qgt_job_destroy.argtypes = [vp]
+
+    def qgt_job(self, n, gates, theta, nslices, J=1.0, h=1.0, lam=1e-3):
+        """A full QGT step on the CPU cut into nslices calls (QGTJob)."""
+        return QGTJob(self, n, gates, theta, nslices, J, h, lam)
 
     def seed_params(self, seed: int, count: int) -> np.ndarray:
         th = np.zeros(count)
@@ -224,6 +238,48 @@ class Oracle:
         return out
 
 
+class QGTJob:
+    """or_qgt_job: one full QGT step (psi, all derivative states, Gram, projector, TFIM energy and
+    gradient, Cholesky step) whose work is split over `slices` calls of step(); result() after the
+    last one.  Every piece of the work happens exactly once over the slices."""
+
+    def __init__(self, orc, n, gates, theta, nslices, J, h, lam):
+        self.orc, self.n = orc, n
+        self.gates = np.ascontiguousarray(gates)
+        self.theta = np.ascontiguousarray(theta, dtype=np.float64)
+        P = self.theta.shape[0]
+        self.P = P
+        self.Q = np.zeros((P, P), dtype=np.complex128)
+        self.grad = np.zeros(P)
+        self.energy = np.zeros(1)
+        self.natgrad = np.zeros(P)
+        self.h = orc.lib.or_qgt_job_create(n, _p(self.gates), len(self.gates), _p(self.theta), P, nslices, J, h, lam,
+                                           _p(self.Q), _p(self.grad), _p(self.energy), _p(self.natgrad))
+        if not self.h:
+            raise MemoryError("or_qgt_job_create failed")
+        self.slices = orc.lib.or_qgt_job_slices(self.h)
+
+    def step(self) -> int:
+        left = self.orc.lib.or_qgt_job_step(self.h)
+        if left < 0:
+            raise RuntimeError("or_qgt_job_step: no slice left")
+        return left
+
+    def result(self):
+        return {"Q": self.Q, "grad": self.grad, "energy": float(self.energy[0]), "natgrad": self.natgrad}
+
+    def close(self):
+        if self.h:
+            self.orc.lib.or_qgt_job_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Reference:
     """The reference library's own code (compiled from its sources by oracle/Makefile)."""
 
@@ -241,10 +297,20 @@ class Reference:
         L.ref_natural_gradient_cg.argtypes = [vp, vp, vp, sz]
         L.ref_invert_qfim_regularized.argtypes = [vp, vp, sz, C.c_float]
         L.ref_berry_phase.argtypes = [vp, sz, sz, vp]
+        L.ref_matrix_inverse.argtypes = [vp, vp, sz]
+        L.ref_matrix_inverse.restype = i32
 
     @staticmethod
     def available(path: str = REF_SO) -> bool:
         return os.path.exists(path)
+
+    def matrix_inverse(self, M):
+        """matrix_inverse (core/matrix_operations.c:176-217: LU with partial pivoting in ComplexFloat)
+        -> (ok, inverse as complex64)."""
+        a = np.ascontiguousarray(M, dtype=np.complex64)
+        inv = np.zeros_like(a)
+        ok = self.lib.ref_matrix_inverse(_p(a), _p(inv), a.shape[0])
+        return bool(ok), inv
 
     def simulate(self, n, gates, theta):
         G = len(gates)
@@ -349,3 +415,50 @@ def tfim_pauli_strings(n: int, J: float = 1.0, h: float = 1.0):
         s[n - 1 - q] = "X"
         terms.append((-h, "".join(s)))
     return terms
+
+
+# ---------------------------------------------------------------------------
+# natural-gradient configurations of the reference entry points (restated)
+# ---------------------------------------------------------------------------
+
+def condition_number_f32(G):
+    """compute_complex_matrix_condition_number (core/quantum_geometric_gradient.c:2733-2781): the
+    singular values of the ComplexFloat matrix (LAPACK, as the reference's lapack_svd), then
+    sigma_max / sigma_min over the positive ones in float; inf when sigma_min <= 1e-15."""
+    s = np.linalg.svd(np.asarray(G, dtype=np.complex64), compute_uv=False).astype(np.float32)
+    mx = s.max()
+    pos = s[s > 0]
+    mn = pos.min() if pos.size else np.float32(0)
+    return float(np.float32(mx / mn)) if mn > np.float32(1e-15) else math.inf
+
+
+def pseudoinverse_natural_gradient(g, G, cutoff):
+    """compute_pseudoinverse_natural_gradient (core/quantum_geometric_gradient.c:2800-2884):
+    x = V S^+ U^H g with singular values <= cutoff dropped (FP64 here)."""
+    U, s, Vh = np.linalg.svd(np.asarray(G, dtype=np.complex128))
+    t = U.conj().T @ np.asarray(g, dtype=np.complex128)
+    t = np.where(s > cutoff, t / np.where(s > 0, s, 1), 0)
+    return Vh.conj().T @ t
+
+
+def regularized_natural_gradient(ref, g, G, reg=1e-4, threshold=1e8, adaptive=True, pinv=True, cutoff=1e-10):
+    """compute_regularized_natural_gradient (core/quantum_geometric_gradient.c:2887-2964): lambda from
+    the config, raised to 1e-6 sqrt(kappa) when kappa exceeds the threshold; x = (G + lambda I)^-1 g
+    with the reference's own matrix_inverse (ComplexFloat LU); when that reports a singular matrix,
+    the pseudo-inverse of the unregularised G.  -> (x, lambda, kappa, path) with path "lu" / "pinv"."""
+    lam = np.float32(reg)
+    kappa = None
+    if adaptive:
+        kappa = condition_number_f32(G)
+        if kappa > threshold:
+            a = np.float32(1e-6) * np.float32(math.sqrt(np.float32(kappa)))
+            if a > lam:
+                lam = a
+    M = np.array(G, dtype=np.complex64)
+    M[np.diag_indices_from(M)] += lam
+    ok, inv = ref.matrix_inverse(M)
+    if ok:
+        return (inv @ np.asarray(g, dtype=np.complex64)).astype(np.complex128), float(lam), kappa, "lu"
+    if not pinv:
+        return None, float(lam), kappa, "fail"
+    return pseudoinverse_natural_gradient(g, G, cutoff), float(lam), kappa, "pinv"

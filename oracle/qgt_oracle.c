@@ -104,9 +104,13 @@ static void generator_matrix(int type, cd m[4])
     }
 }
 
-static void apply_1q(cd* v, size_t dim, int q, const cd m[4])
+/* The gate loops below run over the amplitudes in parallel when `par` is set
+ * (large vectors, one vector at a time); callers that already run one vector
+ * per thread pass 0.  Every iteration touches its own pair of amplitudes. */
+static void apply_1q_p(cd* v, size_t dim, int q, const cd m[4], int par)
 {
     size_t mask = (size_t)1 << q;
+    #pragma omp parallel for if (par) schedule(static)
     for (size_t i = 0; i < dim; i++) {
         if (i & mask) continue;
         size_t j = i | mask;
@@ -116,27 +120,35 @@ static void apply_1q(cd* v, size_t dim, int q, const cd m[4])
     }
 }
 
-static void apply_gate(cd* v, int n, const og_gate_t* g, const double* theta)
+static void apply_gate_p(cd* v, int n, const og_gate_t* g, const double* theta, int par)
 {
     size_t dim = (size_t)1 << n;
     if (g->type == OG_CNOT) {
         size_t cm = (size_t)1 << g->q0, tm = (size_t)1 << g->q1;
+        #pragma omp parallel for if (par) schedule(static)
         for (size_t i = 0; i < dim; i++)
             if ((i & cm) && !(i & tm)) { cd t = v[i]; v[i] = v[i | tm]; v[i | tm] = t; }
     } else if (g->type == OG_CZ) {
         size_t am = (size_t)1 << g->q0, bm = (size_t)1 << g->q1;
+        #pragma omp parallel for if (par) schedule(static)
         for (size_t i = 0; i < dim; i++)
             if ((i & am) && (i & bm)) { v[i].re = -v[i].re; v[i].im = -v[i].im; }
     } else if (g->type == OG_SWAP) {
         size_t am = (size_t)1 << g->q0, bm = (size_t)1 << g->q1;
+        #pragma omp parallel for if (par) schedule(static)
         for (size_t i = 0; i < dim; i++)
             if ((i & am) && !(i & bm)) { size_t j = (i & ~am) | bm; cd t = v[i]; v[i] = v[j]; v[j] = t; }
     } else {
         cd m[4];
         gate_matrix(g->type, gate_angle(g, theta), m);
-        apply_1q(v, dim, g->q0, m);
+        apply_1q_p(v, dim, g->q0, m, par);
     }
 }
+
+static void apply_gate(cd* v, int n, const og_gate_t* g, const double* theta) { apply_gate_p(v, n, g, theta, 0); }
+
+/* amplitude-parallel loops pay off from this many amplitudes on */
+#define OR_PAR_DIM ((size_t)1 << 16)
 
 static int is_rotation(int t) { return t == OG_RX || t == OG_RY || t == OG_RZ; }
 
@@ -147,7 +159,7 @@ int or_simulate(int n, const og_gate_t* gates, int ngates, const double* theta, 
     cd* v = (cd*)psi;
     memset(v, 0, dim * sizeof(cd));
     v[0].re = 1.0;
-    for (int g = 0; g < ngates; g++) apply_gate(v, n, &gates[g], theta);
+    for (int g = 0; g < ngates; g++) apply_gate_p(v, n, &gates[g], theta, dim >= OR_PAR_DIM);
     return 0;
 }
 
@@ -171,18 +183,25 @@ int or_derivatives(int n, const og_gate_t* gates, int ngates, const double* thet
     int nlive = 0;
     cd* tmp = (cd*)malloc(dim * sizeof(cd));
     if (!tmp) { free(live); free(live_list); return -1; }
+    /* few vectors of many amplitudes: parallel over the amplitudes of each vector; otherwise one
+     * vector per thread */
+    const int big = dim >= OR_PAR_DIM;
     for (int g = 0; g < ngates; g++) {
         const og_gate_t* gt = &gates[g];
-        apply_gate(v, n, gt, theta);
-        #pragma omp parallel for schedule(dynamic, 1)
-        for (int j = 0; j < nlive; j++) apply_gate(d + (size_t)live_list[j] * dim, n, gt, theta);
+        apply_gate_p(v, n, gt, theta, big);
+        if (big) {
+            for (int j = 0; j < nlive; j++) apply_gate_p(d + (size_t)live_list[j] * dim, n, gt, theta, 1);
+        } else {
+            #pragma omp parallel for schedule(dynamic, 1)
+            for (int j = 0; j < nlive; j++) apply_gate(d + (size_t)live_list[j] * dim, n, gt, theta);
+        }
         if (is_rotation(gt->type) && gt->param >= 0) {
             int k = gt->param;
             if (k >= nparams) { free(live); free(live_list); free(tmp); return -1; }
             cd m[4];
             generator_matrix(gt->type, m);
             memcpy(tmp, v, dim * sizeof(cd));
-            apply_1q(tmp, dim, gt->q0, m);
+            apply_1q_p(tmp, dim, gt->q0, m, big);
             cd* row = d + (size_t)k * dim;
             #pragma omp parallel for
             for (size_t i = 0; i < dim; i++) row[i] = cadd(row[i], tmp[i]);
@@ -645,4 +664,208 @@ int or_berry_flux(int n, const og_gate_t* gates, int ngates, const double* theta
     }
     free(st);
     return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* one full QGT step in slices (CPU baseline)                                */
+/* ------------------------------------------------------------------------ */
+
+/* The whole step (psi, every derivative state, Gram, projector, TFIM energy
+ * and gradient, Cholesky natural-gradient solve) cut into `nslices` calls
+ * that together do each piece of work exactly once: slice s carries psi up
+ * to the gate of its last derivative row (spawning its rows on the way, as
+ * or_derivatives does), transports its rows to the end of the circuit, and
+ * adds their Gram rows against every row made so far; the last slice also
+ * finishes psi and forms Q, energy, gradient and natural gradient. */
+struct or_qgt_job {
+    int n, ngates, P, nrows, nslices, next, gpsi;
+    size_t dim;
+    og_gate_t* gates;
+    double* theta;
+    int* row_gate;
+    int* row_param;
+    cd* psi;
+    cd* D;
+    cd* B;            /* nrows x nrows: B[i][j] = <D_i|D_j>, filled for j <= i */
+    double J, h, lambda;
+    double *Q, *grad, *energy, *natgrad;
+};
+
+void or_qgt_job_destroy(or_qgt_job_t* j)
+{
+    if (!j) return;
+    free(j->gates); free(j->theta); free(j->row_gate); free(j->row_param);
+    free(j->psi); free(j->D); free(j->B);
+    free(j);
+}
+
+or_qgt_job_t* or_qgt_job_create(int n, const og_gate_t* gates, int ngates, const double* theta, int P, int nslices,
+                                double J, double h, double lambda, double* Q, double* grad, double* energy,
+                                double* natgrad)
+{
+    if (n < 1 || n > 30 || ngates < 0 || P < 1 || nslices < 1) return NULL;
+    or_qgt_job_t* j = (or_qgt_job_t*)calloc(1, sizeof(*j));
+    if (!j) return NULL;
+    j->n = n;
+    j->dim = (size_t)1 << n;
+    j->ngates = ngates;
+    j->P = P;
+    j->J = J; j->h = h; j->lambda = lambda;
+    j->Q = Q; j->grad = grad; j->energy = energy; j->natgrad = natgrad;
+    j->gates = (og_gate_t*)malloc(sizeof(og_gate_t) * (size_t)(ngates > 0 ? ngates : 1));
+    j->theta = (double*)malloc(sizeof(double) * (size_t)P);
+    j->row_gate = (int*)malloc(sizeof(int) * (size_t)(ngates > 0 ? ngates : 1));
+    j->row_param = (int*)malloc(sizeof(int) * (size_t)(ngates > 0 ? ngates : 1));
+    j->psi = (cd*)malloc(sizeof(cd) * j->dim);
+    if (!j->gates || !j->theta || !j->row_gate || !j->row_param || !j->psi) { or_qgt_job_destroy(j); return NULL; }
+    memcpy(j->gates, gates, sizeof(og_gate_t) * (size_t)ngates);
+    memcpy(j->theta, theta, sizeof(double) * (size_t)P);
+    for (int g = 0; g < ngates; g++)
+        if (is_rotation(gates[g].type) && gates[g].param >= 0) {
+            if (gates[g].param >= P) { or_qgt_job_destroy(j); return NULL; }
+            j->row_gate[j->nrows] = g;
+            j->row_param[j->nrows] = gates[g].param;
+            j->nrows++;
+        }
+    j->nslices = nslices > j->nrows ? (j->nrows > 0 ? j->nrows : 1) : nslices;
+    j->D = (cd*)calloc((size_t)(j->nrows > 0 ? j->nrows : 1) * j->dim, sizeof(cd));
+    j->B = (cd*)calloc((size_t)(j->nrows > 0 ? j->nrows : 1) * (size_t)(j->nrows > 0 ? j->nrows : 1), sizeof(cd));
+    if (!j->D || !j->B) { or_qgt_job_destroy(j); return NULL; }
+    memset(j->psi, 0, sizeof(cd) * j->dim);
+    j->psi[0].re = 1.0;
+    return j;
+}
+
+int or_qgt_job_slices(const or_qgt_job_t* j) { return j ? j->nslices : 0; }
+
+static void job_finish(or_qgt_job_t* j)
+{
+    const size_t dim = j->dim;
+    const int R = j->nrows, P = j->P;
+    for (int g = j->gpsi; g < j->ngates; g++) apply_gate_p(j->psi, j->n, &j->gates[g], j->theta, dim >= OR_PAR_DIM);
+    j->gpsi = j->ngates;
+    cd* v = (cd*)calloc((size_t)(R > 0 ? R : 1), sizeof(cd));
+    double* gr = (double*)calloc((size_t)(R > 0 ? R : 1), sizeof(double));
+    cd* hp = (cd*)malloc(sizeof(cd) * dim);
+    if (!v || !gr || !hp) { free(v); free(gr); free(hp); return; }
+    or_tfim_apply(j->n, j->J, j->h, (const double*)j->psi, (double*)hp);
+    double e = 0;
+    #pragma omp parallel for reduction(+:e) schedule(static)
+    for (size_t k = 0; k < dim; k++) e += j->psi[k].re * hp[k].re + j->psi[k].im * hp[k].im;
+    /* v_i = <D_i|psi>, g_i = 2 Re <D_i|H psi> */
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < R; i++) {
+        const cd* a = j->D + (size_t)i * dim;
+        double vr = 0, vi = 0, g = 0;
+        for (size_t k = 0; k < dim; k++) {
+            vr += a[k].re * j->psi[k].re + a[k].im * j->psi[k].im;
+            vi += a[k].re * j->psi[k].im - a[k].im * j->psi[k].re;
+            g += a[k].re * hp[k].re + a[k].im * hp[k].im;
+        }
+        v[i] = (cd){vr, vi};
+        gr[i] = 2.0 * g;
+    }
+    cd* q = (cd*)j->Q;
+    memset(q, 0, sizeof(cd) * (size_t)P * P);
+    memset(j->grad, 0, sizeof(double) * (size_t)P);
+    for (int a = 0; a < R; a++) {
+        j->grad[j->row_param[a]] += gr[a];
+        for (int b = 0; b < R; b++) {
+            /* <D_a|D_b> from the filled lower part (Hermitian) */
+            cd bab = a >= b ? j->B[(size_t)a * R + b] : (cd){j->B[(size_t)b * R + a].re, -j->B[(size_t)b * R + a].im};
+            cd vv = cmul(v[a], (cd){v[b].re, -v[b].im});
+            cd* t = &q[(size_t)j->row_param[a] * P + j->row_param[b]];
+            t->re += bab.re - vv.re;
+            t->im += bab.im - vv.im;
+        }
+    }
+    *j->energy = e;
+    double* A = (double*)malloc(sizeof(double) * (size_t)P * P);
+    if (A) {
+        for (size_t k = 0; k < (size_t)P * P; k++) A[k] = q[k].re;
+        double used;
+        if (or_cholesky_solve(P, A, j->lambda, j->grad, j->natgrad, &used) != 0)
+            for (int k = 0; k < P; k++) j->natgrad[k] = NAN;
+        free(A);
+    }
+    free(v); free(gr); free(hp);
+}
+
+/* runs the next slice; returns the number of slices left (0 after the last), -1 on error */
+int or_qgt_job_step(or_qgt_job_t* j)
+{
+    if (!j || j->next >= j->nslices) return -1;
+    const int s = j->next;
+    const size_t dim = j->dim;
+    const int R = j->nrows;
+    const int r0 = (int)((int64_t)s * R / j->nslices), r1 = (int)((int64_t)(s + 1) * R / j->nslices);
+    const int big = dim >= OR_PAR_DIM;
+    if (r1 > r0) {
+        /* psi up to the last row's gate, spawning and carrying this slice's rows */
+        const int gl = j->row_gate[r1 - 1];
+        int live0 = r0, live1 = r0;   /* rows [live0, live1) are spawned */
+        for (int g = j->gpsi; g <= gl; g++) {
+            const og_gate_t* gt = &j->gates[g];
+            apply_gate_p(j->psi, j->n, gt, j->theta, big);
+            if (big) {
+                for (int r = live0; r < live1; r++) apply_gate_p(j->D + (size_t)r * dim, j->n, gt, j->theta, 1);
+            } else {
+                #pragma omp parallel for schedule(dynamic, 1)
+                for (int r = live0; r < live1; r++) apply_gate(j->D + (size_t)r * dim, j->n, gt, j->theta);
+            }
+            if (live1 < r1 && j->row_gate[live1] == g) {
+                cd m[4];
+                generator_matrix(gt->type, m);
+                cd* row = j->D + (size_t)live1 * dim;
+                memcpy(row, j->psi, sizeof(cd) * dim);
+                apply_1q_p(row, dim, gt->q0, m, big);
+                live1++;
+            }
+        }
+        j->gpsi = gl + 1;
+        /* the slice's rows to the end of the circuit: one row per thread */
+        #pragma omp parallel for schedule(dynamic, 1)
+        for (int r = r0; r < r1; r++)
+            for (int g = gl + 1; g < j->ngates; g++) apply_gate(j->D + (size_t)r * dim, j->n, &j->gates[g], j->theta);
+        /* Gram rows i in [r0, r1) against j <= i, over amplitude chunks */
+        const int m = r1 - r0;
+        const size_t chunk = 256;
+        const size_t nch = (dim + chunk - 1) / chunk;
+        #pragma omp parallel
+        {
+            cd* acc = (cd*)calloc((size_t)m * (size_t)r1, sizeof(cd));
+            #pragma omp for schedule(static)
+            for (size_t c = 0; c < nch; c++) {
+                const size_t k0 = c * chunk, k1 = k0 + chunk < dim ? k0 + chunk : dim;
+                for (int i = r0; i < r1; i++) {
+                    const cd* a = j->D + (size_t)i * dim;
+                    for (int jj = 0; jj <= i; jj++) {
+                        const cd* b = j->D + (size_t)jj * dim;
+                        double re = 0, im = 0;
+                        for (size_t k = k0; k < k1; k++) {
+                            re += a[k].re * b[k].re + a[k].im * b[k].im;
+                            im += a[k].re * b[k].im - a[k].im * b[k].re;
+                        }
+                        if (acc) {
+                            acc[(size_t)(i - r0) * r1 + jj].re += re;
+                            acc[(size_t)(i - r0) * r1 + jj].im += im;
+                        }
+                    }
+                }
+            }
+            #pragma omp critical
+            {
+                if (acc)
+                    for (int i = r0; i < r1; i++)
+                        for (int jj = 0; jj <= i; jj++) {
+                            j->B[(size_t)i * R + jj].re += acc[(size_t)(i - r0) * r1 + jj].re;
+                            j->B[(size_t)i * R + jj].im += acc[(size_t)(i - r0) * r1 + jj].im;
+                        }
+            }
+            free(acc);
+        }
+    }
+    j->next++;
+    if (j->next == j->nslices) job_finish(j);
+    return j->nslices - j->next;
 }

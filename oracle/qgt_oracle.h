@@ -122,7 +122,22 @@ int or_berry_phase(const double* const* states, size_t n, size_t dim, double* ou
 int or_berry_flux(int n, const og_gate_t* gates, int ngates, const double* theta, int nparams, int pa, int pb,
                   int rows, int cols, double a0, double da, double b0, double db, int periodic, double* flux);
 
+/* One full QGT step (psi, derivative states, Gram, projector, TFIM energy
+ * and gradient, FP64 Cholesky natural-gradient step) done in nslices calls of
+ * or_qgt_job_step, each piece of work exactly once; the outputs (Q: P x P
+ * complex, grad: P, energy: 1, natgrad: P, caller-owned) are written by the
+ * last call.  The CPU baseline of the benchmark. */
+typedef struct or_qgt_job or_qgt_job_t;
+or_qgt_job_t* or_qgt_job_create(int n, const og_gate_t* gates, int ngates, const double* theta, int nparams,
+                                int nslices, double J, double h, double lambda, double* Q, double* grad,
+                                double* energy, double* natgrad);
+int or_qgt_job_slices(const or_qgt_job_t* job);
+int or_qgt_job_step(or_qgt_job_t* job);
+void or_qgt_job_destroy(or_qgt_job_t* job);
+
 #ifdef __cplusplus
 }
 #endif
+
+
 #endif

@@ -110,6 +110,7 @@ def lib() -> C.CDLL:
         L.qgt_plan_device_status.argtypes = [vp, vp]
         L.qgt_cholesky_solve_f64.argtypes = [vp, vp, C.c_double, C.c_int32, vp, vp]
         L.qgt_plan_profile_step.argtypes = [vp, C.POINTER(StepProfile)]
+        L.qgt_plan_test_gram_stall.argtypes = [vp, C.c_int, C.c_int64]
         L.qgt_batch_default_options.argtypes = [C.POINTER(BatchOptions)]
         L.qgt_batch_create.argtypes = [vp, C.c_int32, vp, C.POINTER(BatchOptions), C.POINTER(vp)]
         L.qgt_batch_execute_host.argtypes = [vp, vp, vp, vp]
@@ -274,6 +275,11 @@ class Plan:
 
     def stream(self) -> int:
         return lib().qgt_plan_stream(self.h) or 0
+
+    def test_gram_stall(self, stall: bool, timeout_ns: int = 0):
+        """Fault-injection hook (qgt_plan_test_gram_stall): with stall the digit Gram's
+        bounded waits run out after timeout_ns and the step reports QGT_ERROR_TIMEOUT."""
+        _check(lib().qgt_plan_test_gram_stall(self.h, int(bool(stall)), int(timeout_ns)), "qgt_plan_test_gram_stall")
 
     def close(self):
         if getattr(self, "h", None):

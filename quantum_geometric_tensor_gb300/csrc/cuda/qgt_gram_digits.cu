@@ -63,6 +63,17 @@
 #define DG_ERR_TIMEOUT (-13)
 #define DG_ERR_INEXACT (-24)
 
+// device control block of a Gram: the status word the kernel writes (cleared on the stream before
+// every run) and the wait settings it reads at start.  `stall` and `timeout_ns` exist for the tests of
+// the bounded-wait error path: with stall set, the converter warps wait on an mbarrier that nothing
+// arrives on, so their wait runs out after timeout_ns (0 = DG_TIMEOUT_NS) and the CTA takes its
+// abort path (drain its own loads and MMAs, free TMEM, report DG_ERR_TIMEOUT).
+struct dg_ctl_t {
+    int err;
+    int stall;
+    long long timeout_ns;
+};
+
 struct qgt_dg_gram {
     CUtensorMap tmap;
     const void* V;
@@ -72,7 +83,7 @@ struct qgt_dg_gram {
     int mbits;                 /* digits D in [-2^mbits, 2^mbits] */
     const uint32_t* rowmax;
     float* part;
-    int* err;
+    dg_ctl_t* ctl;
 };
 
 static __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -219,14 +230,16 @@ __constant__ int8_t dg_terms[12][4] = {
 __global__ void __launch_bounds__(DG_THREADS, 1)
     dg_gram_kernel(const __grid_constant__ CUtensorMap tmap, int nbk, int64_t N, int64_t kchunk,
                    const uint32_t* __restrict__ rowmax, int rows, int mbits, float* __restrict__ part,
-                   int* __restrict__ err)
+                   dg_ctl_t* __restrict__ ctl)
 {
+    int* err = &ctl->err;
     extern __shared__ uint8_t dg_smem[];
     __shared__ __align__(8) uint64_t raw_full[DG_RAW_STAGES];
     __shared__ __align__(8) uint64_t raw_empty[DG_RAW_STAGES];
     __shared__ __align__(8) uint64_t pl_full[DG_PL_STAGES];
     __shared__ __align__(8) uint64_t pl_empty[DG_PL_STAGES];
     __shared__ __align__(8) uint64_t done_bar;
+    __shared__ __align__(8) uint64_t never_bar;   // test stall: initialised, never arrived on
     __shared__ uint32_t tmem_sh;
     __shared__ volatile int abort_sh;
     __shared__ float inv_u[2][128];
@@ -249,7 +262,9 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
     int64_t k1 = k0 + kchunk;
     if (k1 > N) k1 = N;
     const int nk = (int)((k1 - k0) / DG_BK);
-    const uint64_t deadline = gtimer() + DG_TIMEOUT_NS;
+    const long long tmo = ctl->timeout_ns;
+    const bool stall = ctl->stall != 0;
+    const uint64_t deadline = gtimer() + (tmo > 0 ? (uint64_t)tmo : DG_TIMEOUT_NS);
     rowmax += (int64_t)blockIdx.z * rows;   // parameter point
     part += (int64_t)blockIdx.z * gridDim.x * (2 * 128 * 128);
 
@@ -271,6 +286,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
             bar_init(smem_u32(&pl_empty[s]), 1);
         }
         bar_init(smem_u32(&done_bar), 1);
+        bar_init(smem_u32(&never_bar), 1);
         abort_sh = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -344,7 +360,8 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
         const int sub = lane >> 3, kp = (lane & 7) * 2;
         for (int kt = 0; kt < nk; kt++) {
             const int rs = kt % DG_RAW_STAGES, ps = kt % DG_PL_STAGES;
-            bool ok = bar_wait(smem_u32(&raw_full[rs]), (kt / DG_RAW_STAGES) & 1, deadline);
+            bool ok = bar_wait(stall ? smem_u32(&never_bar) : smem_u32(&raw_full[rs]), (kt / DG_RAW_STAGES) & 1,
+                               deadline);
             if (ok && kt >= DG_PL_STAGES) ok = bar_wait(smem_u32(&pl_empty[ps]), ((kt / DG_PL_STAGES) & 1) ^ 1, deadline);
             if (!ok) {
                 atomicExch(err, DG_ERR_TIMEOUT);
@@ -599,13 +616,13 @@ extern "C" int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, co
     }
     size_t pbytes = (size_t)npoints * g->nsplit * g->ntp * 2 * 128 * 128 * sizeof(float);
     cudaError_t e = cudaMalloc((void**)&g->part, pbytes);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&g->err, sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(g->err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&g->ctl, sizeof(dg_ctl_t));
+    if (e == cudaSuccess) e = cudaMemset(g->ctl, 0, sizeof(dg_ctl_t));
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(dg_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, DG_SMEM_BYTES);
     if (e != cudaSuccess) {
         cudaFree(g->part);
-        cudaFree(g->err);
+        cudaFree(g->ctl);
         free(g);
         return qgt_set_error(e == cudaErrorMemoryAllocation ? -2 : -6, "digit gram: %s", cudaGetErrorString(e));
     }
@@ -616,8 +633,11 @@ extern "C" int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, co
 extern "C" int qgt_dev_dg_gram_run(qgt_dg_gram_t* g, double* HG, void* stream)
 {
     cudaStream_t s = (cudaStream_t)stream;
+    // the status word describes this run only (a run after a failed one starts clean)
+    cudaError_t e = cudaMemsetAsync(&g->ctl->err, 0, sizeof(int), s);
+    if (e != cudaSuccess) return qgt_set_error(-6, "digit gram: %s", cudaGetErrorString(e));
     dg_gram_kernel<<<dim3((unsigned)(g->ntp * g->nsplit), 1, g->npoints), DG_THREADS, DG_SMEM_BYTES, s>>>(g->tmap, g->nbk, g->N, g->kchunk, g->rowmax,
-                                                                       g->rows, g->mbits, g->part, g->err);
+                                                                       g->rows, g->mbits, g->part, g->ctl);
     int rc = qgt_dev_last_error();
     if (rc) return rc;
     dg_reduce_kernel<<<dim3((unsigned)((g->rows + 31) / 32), (unsigned)g->rows, g->npoints), 256, 0, s>>>(
@@ -625,12 +645,23 @@ extern "C" int qgt_dev_dg_gram_run(qgt_dg_gram_t* g, double* HG, void* stream)
     return qgt_dev_last_error();
 }
 
-extern "C" const int* qgt_dev_dg_gram_err(const qgt_dg_gram_t* g) { return g ? g->err : NULL; }
+extern "C" const int* qgt_dev_dg_gram_err(const qgt_dg_gram_t* g) { return g ? &g->ctl->err : NULL; }
+
+extern "C" int qgt_dev_dg_gram_set_stall(qgt_dg_gram_t* g, int stall, int64_t timeout_ns, void* stream)
+{
+    dg_ctl_t h;
+    h.err = 0;
+    h.stall = stall ? 1 : 0;
+    h.timeout_ns = timeout_ns > 0 ? (long long)timeout_ns : 0;
+    cudaError_t e = cudaMemcpyAsync(g->ctl, &h, sizeof h, cudaMemcpyHostToDevice, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    return e == cudaSuccess ? 0 : qgt_set_error(-6, "digit gram: %s", cudaGetErrorString(e));
+}
 
 extern "C" int qgt_dev_dg_gram_status(qgt_dg_gram_t* g, void* stream)
 {
     int h = 0;
-    cudaError_t e = cudaMemcpyAsync(&h, g->err, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    cudaError_t e = cudaMemcpyAsync(&h, &g->ctl->err, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return qgt_set_error(-6, "digit gram status: %s", cudaGetErrorString(e));
     return h;
@@ -640,7 +671,7 @@ extern "C" void qgt_dev_dg_gram_destroy(qgt_dg_gram_t* g)
 {
     if (!g) return;
     cudaFree(g->part);
-    cudaFree(g->err);
+    cudaFree(g->ctl);
     free(g);
 }
 

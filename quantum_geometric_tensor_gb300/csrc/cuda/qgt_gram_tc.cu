@@ -389,6 +389,9 @@ extern "C" int qgt_dev_tc_gram_create(void* split, int64_t N, int32_t rows, int3
 extern "C" int qgt_dev_tc_gram_run(qgt_tc_gram_t* g, double inv_scale2, double* HG, void* stream)
 {
     cudaStream_t s = (cudaStream_t)stream;
+    // the error word describes this run only (a run after a failed one starts clean)
+    cudaError_t e = cudaMemsetAsync(g->err, 0, sizeof(int), s);
+    if (e != cudaSuccess) return qgt_set_error(-6, "tc gram: %s", cudaGetErrorString(e));
     tc_gram_kernel<<<dim3(g->ntp, g->nsplit), 192, TC_SMEM_BYTES, s>>>(g->tmap, g->nbk, g->N, g->kchunk, g->bf16,
                                                                        g->part, g->err);
     int rc = qgt_dev_last_error();

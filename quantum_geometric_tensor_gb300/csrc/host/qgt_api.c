@@ -27,6 +27,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include "../qgt_internal.h"
 #include "qgt_gb300.h"
@@ -615,6 +616,29 @@ qgt_error_t geometric_clone_metric(quantum_geometric_metric_t** d, const quantum
     return QGT_SUCCESS;
 }
 
+/* The state-space metric of geometric_compute_metric
+ * (src/quantum_geometric/core/quantum_geometric_metric.c:85-189): Euclidean
+ * leaves the components as they are; Fubini-Study writes
+ * M_ij = delta_ij - conj(psi_i) psi_j for the state's amplitudes (computed
+ * on the GPU); other types are not implemented, as in the reference. */
+qgt_error_t geometric_compute_metric(quantum_geometric_metric_t* m, const quantum_state_t* state)
+{
+    CHECK_NULL(m); CHECK_NULL(state);
+    if (m->dimension != state->dimension) return QGT_ERROR_INVALID_ARGUMENT;
+    switch (m->type) {
+    case GEOMETRIC_METRIC_EUCLIDEAN:
+        return QGT_SUCCESS;
+    case GEOMETRIC_METRIC_FUBINI_STUDY:
+        CHECK_NULL(state->coordinates);
+        CHECK_NULL(m->components);
+        if (qgt_dev_fs_metric((const float*)state->coordinates, (int64_t)m->dimension, (float*)m->components) != 0)
+            return QGT_ERROR_COMPUTATION_FAILED;
+        return QGT_SUCCESS;
+    default:
+        return QGT_ERROR_NOT_IMPLEMENTED;
+    }
+}
+
 static qgt_error_t full_q(const quantum_geometric_tensor_network_t* q, size_t P, const double** Q)
 {
     if (!ensure_step(q, 0)) return QGT_ERROR_COMPUTATION_FAILED;
@@ -829,6 +853,69 @@ qgt_error_t geometric_tensor_initialize_zero(quantum_geometric_tensor_t* t)
     return QGT_SUCCESS;
 }
 
+/* uniform double in [0, 1) from a splitmix64 stream (53 random bits) */
+static double tensor_uniform(uint64_t* state)
+{
+    uint64_t z = (*state += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+/* The reference fills from its entropy-seeded QRNG
+ * (src/quantum_geometric/core/quantum_geometric_tensor.c:257-340): every
+ * element (re, im) uniform in [min, max) scaled to unit modulus; a rank-2
+ * Hermitian tensor gets a real uniform diagonal and unit-modulus upper
+ * entries mirrored as conjugates.  Here the stream is splitmix64, seeded
+ * differently on every call (clock and a per-process counter), so the values
+ * are as unrepeatable as the reference's. */
+qgt_error_t geometric_tensor_initialize_random(quantum_geometric_tensor_t* t, float min_val, float max_val)
+{
+    if (!t || !t->components) return QGT_ERROR_INVALID_ARGUMENT;
+    if (!(min_val < max_val)) return QGT_ERROR_INVALID_ARGUMENT;
+    static uint64_t calls = 0;
+    struct timespec ts;
+    clock_gettime(CLOCK_REALTIME, &ts);
+    uint64_t st = ((uint64_t)ts.tv_sec * 1000000007ULL) ^ (uint64_t)ts.tv_nsec ^
+                  (__atomic_add_fetch(&calls, 1, __ATOMIC_RELAXED) * 0xD1B54A32D192ED03ULL) ^ (uint64_t)(uintptr_t)t;
+    const float range = max_val - min_val;
+    ComplexFloat* d = t->components;
+    if (t->type == GEOMETRIC_TENSOR_HERMITIAN && t->rank == 2) {
+        const size_t n = t->dimensions[0];
+        for (size_t i = 0; i < n; i++)
+            for (size_t j = i; j < n; j++) {
+                float re = min_val + (float)tensor_uniform(&st) * range;
+                if (i == j) { d[i * n + i] = (ComplexFloat){re, 0.0f}; continue; }
+                float im = min_val + (float)tensor_uniform(&st) * range;
+                const float m = sqrtf(re * re + im * im);
+                if (m > 0) { re /= m; im /= m; }
+                d[i * n + j] = (ComplexFloat){re, im};
+                d[j * n + i] = (ComplexFloat){re, -im};
+            }
+    } else {
+        for (size_t i = 0; i < t->total_elements; i++) {
+            float re = min_val + (float)tensor_uniform(&st) * range;
+            float im = min_val + (float)tensor_uniform(&st) * range;
+            const float m = sqrtf(re * re + im * im);
+            if (m > 0) { re /= m; im /= m; }
+            d[i] = (ComplexFloat){re, im};
+        }
+    }
+    return QGT_SUCCESS;
+}
+
+/* src/quantum_geometric/core/quantum_geometric_tensor_cpu.c:837-863: square rank-2 tensors only */
+qgt_error_t geometric_tensor_initialize_identity(quantum_geometric_tensor_t* t)
+{
+    if (!t || !t->components || !t->dimensions) return QGT_ERROR_INVALID_ARGUMENT;
+    if (t->rank != 2 || t->dimensions[0] != t->dimensions[1]) return QGT_ERROR_INVALID_DIMENSION;
+    const size_t n = t->dimensions[0];
+    memset(t->components, 0, t->total_elements * sizeof(ComplexFloat));
+    for (size_t i = 0; i < n; i++) t->components[i * n + i] = (ComplexFloat){1.0f, 0.0f};
+    return QGT_SUCCESS;
+}
+
 /* ------------------------------------------------------------------------ */
 /* gradients and natural gradients (quantum_geometric_gradient.c)            */
 /* ------------------------------------------------------------------------ */
@@ -907,157 +994,84 @@ natural_gradient_config_t get_default_natural_gradient_config(void)
     return c;
 }
 
-/* Eigen-decomposition of a Hermitian P x P matrix through its real
- * symmetric 2P x 2P embedding [[Re, -Im], [Im, Re]] (every eigenvalue appears
- * twice), cyclic Jacobi in FP64.  V (optional) receives the eigenvectors as
- * columns.  A host-side dense routine for the diagnostics and the SVD
- * fallback of the reference (LAPACK cgesvd in quantum_geometric_gradient.c:
- * 2733-2884); the natural-gradient step itself is the GPU Cholesky. */
-static int herm_eig(const ComplexFloat* M, size_t P, double* w, double* V)
-{
-    size_t n = 2 * P;
-    double* A = (double*)malloc(sizeof(double) * n * n);
-    if (!A) return -1;
-    for (size_t i = 0; i < P; i++)
-        for (size_t j = 0; j < P; j++) {
-            double re = 0.5 * (M[i * P + j].real + M[j * P + i].real);
-            double im = 0.5 * (M[i * P + j].imag - M[j * P + i].imag);
-            A[i * n + j] = re; A[(i + P) * n + j + P] = re;
-            A[i * n + j + P] = -im; A[(i + P) * n + j] = im;
-        }
-    if (V) for (size_t i = 0; i < n * n; i++) V[i] = (i % (n + 1) == 0) ? 1.0 : 0.0;
-    for (int sweep = 0; sweep < 60; sweep++) {
-        double off = 0, tot = 0;
-        for (size_t i = 0; i < n; i++)
-            for (size_t j = 0; j < n; j++) { double a = A[i * n + j] * A[i * n + j]; tot += a; if (i != j) off += a; }
-        if (off <= 1e-30 * (tot > 0 ? tot : 1)) break;
-        for (size_t p = 0; p < n; p++)
-            for (size_t q = p + 1; q < n; q++) {
-                double apq = A[p * n + q];
-                if (fabs(apq) < 1e-300) continue;
-                double th = (A[q * n + q] - A[p * n + p]) / (2 * apq);
-                double t = (th >= 0 ? 1 : -1) / (fabs(th) + sqrt(th * th + 1));
-                double cs = 1 / sqrt(t * t + 1), sn = t * cs;
-                for (size_t k = 0; k < n; k++) {
-                    double akp = A[k * n + p], akq = A[k * n + q];
-                    A[k * n + p] = cs * akp - sn * akq;
-                    A[k * n + q] = sn * akp + cs * akq;
-                }
-                for (size_t k = 0; k < n; k++) {
-                    double apk = A[p * n + k], aqk = A[q * n + k];
-                    A[p * n + k] = cs * apk - sn * aqk;
-                    A[q * n + k] = sn * apk + cs * aqk;
-                }
-                if (V)
-                    for (size_t k = 0; k < n; k++) {
-                        double vkp = V[k * n + p], vkq = V[k * n + q];
-                        V[k * n + p] = cs * vkp - sn * vkq;
-                        V[k * n + q] = sn * vkp + cs * vkq;
-                    }
-            }
-    }
-    for (size_t i = 0; i < n; i++) w[i] = A[i * n + i];
-    free(A);
-    return 0;
-}
+/* Singular values and the pseudo-inverse come from a one-sided Jacobi SVD of
+ * the general complex matrix on the GPU (qgt_linalg.cu), where the reference
+ * calls LAPACK cgesvd (quantum_geometric_gradient.c:2733-2884); the
+ * regularised step solves (G + lambda I) x = g by LU with partial pivoting on
+ * the GPU with the singularity rule of the reference's matrix_inverse
+ * (matrix_operations.c:55-217).  All three work on G as given (Hermitian or
+ * not), in FP64, and return ComplexFloat as the reference does. */
+#define NG_MAX_SWEEPS 60
 
 bool compute_complex_matrix_condition_number(const ComplexFloat* m, size_t P, float* kappa)
 {
-    if (!m || !kappa || P == 0) return false;
-    double* w = (double*)malloc(sizeof(double) * 2 * P);
-    if (!w || herm_eig(m, P, w, NULL) != 0) { free(w); return false; }
-    double mx = 0, mn = INFINITY;
-    for (size_t i = 0; i < 2 * P; i++) {
-        double a = fabs(w[i]);
-        if (a > mx) mx = a;
-        if (a > 0 && a < mn) mn = a;
-    }
-    free(w);
-    *kappa = (mn > 1e-15) ? (float)(mx / mn) : INFINITY;
-    return true;
-}
-
-/* (G + lambda I) x = g for Hermitian G by the real 2P embedding, FP64
- * Cholesky on the GPU (quantum_geometric_gradient.c:2887-2964 uses a complex
- * inverse; a Hermitian positive-definite system is solved exactly this way). */
-static bool herm_solve(const ComplexFloat* G, const ComplexFloat* g, ComplexFloat* x, size_t P, double lambda,
-                       int retries)
-{
-    size_t n = 2 * P;
-    double* A = (double*)malloc(sizeof(double) * n * n);
-    double* b = (double*)malloc(sizeof(double) * n);
-    double* y = (double*)malloc(sizeof(double) * n);
-    bool ok = A && b && y;
+    if (!m || !kappa || P == 0 || P > 8192) return false;
+    double* s = (double*)malloc(sizeof(double) * P);
+    if (!s) return false;
+    int32_t sweeps = 0;
+    bool ok = qgt_dev_svd_pinv((const float*)m, (int32_t)P, s, NULL, 0.0, NULL, NG_MAX_SWEEPS, &sweeps) == 0;
     if (ok) {
-        for (size_t i = 0; i < P; i++) {
-            for (size_t j = 0; j < P; j++) {
-                double re = 0.5 * (G[i * P + j].real + G[j * P + i].real);
-                double im = 0.5 * (G[i * P + j].imag - G[j * P + i].imag);
-                A[i * n + j] = re; A[(i + P) * n + j + P] = re;
-                A[i * n + j + P] = -im; A[(i + P) * n + j] = im;
-            }
-            b[i] = g[i].real;
-            b[i + P] = g[i].imag;
+        /* sigma_max over sigma_min among the positive values (quantum_geometric_gradient.c:2762-2773) */
+        double mx = s[0], mn = s[0];
+        for (size_t i = 1; i < P; i++) {
+            if (s[i] > mx) mx = s[i];
+            if (s[i] < mn && s[i] > 0) mn = s[i];
         }
-        double used = lambda;
-        ok = qgt_cholesky_solve_f64(A, b, lambda, (int32_t)n, y, &used) == 0;
-        if (ok && !retries && used != lambda) ok = false;
+        *kappa = (mn > 1e-15) ? (float)(mx / mn) : INFINITY;
     }
-    if (ok) for (size_t i = 0; i < P; i++) x[i] = (ComplexFloat){(float)y[i], (float)y[i + P]};
-    free(A); free(b); free(y);
+    free(s);
     return ok;
 }
 
 bool compute_pseudoinverse_natural_gradient(const ComplexFloat* g, const ComplexFloat* G, ComplexFloat* x, size_t P,
                                             float cutoff)
 {
-    if (!g || !G || !x || P == 0) return false;
-    size_t n = 2 * P;
-    double* w = (double*)malloc(sizeof(double) * n);
-    double* V = (double*)malloc(sizeof(double) * n * n);
-    double* b = (double*)malloc(sizeof(double) * n);
-    double* y = (double*)calloc(n, sizeof(double));
-    bool ok = w && V && b && y && herm_eig(G, P, w, V) == 0;
-    if (ok) {
-        for (size_t i = 0; i < P; i++) { b[i] = g[i].real; b[i + P] = g[i].imag; }
-        for (size_t k = 0; k < n; k++) {
-            if (fabs(w[k]) <= cutoff) continue; /* G^+ drops singular values below the cutoff */
-            double c = 0;
-            for (size_t i = 0; i < n; i++) c += V[i * n + k] * b[i];
-            c /= w[k];
-            for (size_t i = 0; i < n; i++) y[i] += c * V[i * n + k];
-        }
-        for (size_t i = 0; i < P; i++) x[i] = (ComplexFloat){(float)y[i], (float)y[i + P]};
-    }
-    free(w); free(V); free(b); free(y);
+    if (!g || !G || !x || P == 0 || P > 8192) return false;
+    double* y = (double*)malloc(sizeof(double) * 2 * P);
+    if (!y) return false;
+    int32_t sweeps = 0;
+    bool ok = qgt_dev_svd_pinv((const float*)G, (int32_t)P, NULL, (const float*)g, (double)cutoff, y, NG_MAX_SWEEPS,
+                               &sweeps) == 0;
+    if (ok) for (size_t i = 0; i < P; i++) x[i] = (ComplexFloat){(float)y[2 * i], (float)y[2 * i + 1]};
+    free(y);
     return ok;
 }
 
 bool compute_regularized_natural_gradient(const ComplexFloat* g, const ComplexFloat* G, ComplexFloat* x, size_t P,
                                           const natural_gradient_config_t* cfg)
 {
-    if (!g || !G || !x || !cfg || P == 0) return false;
-    double lambda = cfg->regularization_param;
+    if (!g || !G || !x || !cfg || P == 0 || P > 8192) return false;
+    /* quantum_geometric_gradient.c:2887-2964: lambda grows to 1e-6 sqrt(kappa) above the threshold */
+    float lambda = cfg->regularization_param;
     if (cfg->use_adaptive_regularization) {
         float kappa;
         if (compute_complex_matrix_condition_number(G, P, &kappa) && kappa > cfg->condition_threshold) {
-            double a = 1e-6 * sqrt((double)kappa);
+            float a = 1e-6f * sqrtf(kappa);
             if (a > lambda) lambda = a;
         }
     }
-    if (herm_solve(G, g, x, P, lambda, 0)) return true;
-    if (cfg->use_pseudoinverse_fallback)
+    double* y = (double*)malloc(sizeof(double) * 2 * P);
+    if (!y) return false;
+    int32_t singular = 1;
+    bool ok = qgt_dev_lu_solve((const float*)G, (int32_t)P, (double)lambda, (const float*)g, y, &singular) == 0;
+    if (ok && !singular) {
+        for (size_t i = 0; i < P; i++) x[i] = (ComplexFloat){(float)y[2 * i], (float)y[2 * i + 1]};
+        free(y);
+        return true;
+    }
+    free(y);
+    if (ok && cfg->use_pseudoinverse_fallback)   /* the fallback uses the unregularised metric, as the reference */
         return compute_pseudoinverse_natural_gradient(g, G, x, P, cfg->singular_value_cutoff);
     return false;
 }
 
+/* The reference's GPU entry point runs its CPU conjugate gradients
+ * (classical_optimization_engine.c:612-623 -> :543-611); here the same
+ * iteration (x0 = 0, <= 100 steps, |p^T F p| < 1e-15 or |r| < 1e-8 stops it)
+ * runs on the GPU in FP64.  On a failure of the device the plain gradient is
+ * returned, as the reference does when its buffers cannot be allocated. */
 void compute_natural_gradient_gpu(const double* F, const double* g, double* x, size_t P)
 {
     if (!F || !g || !x || P == 0) return;
-    double md = 0;
-    for (size_t i = 0; i < P; i++) md = fmax(md, fabs(F[i * P + i]));
-    double used;
-    if (qgt_cholesky_solve_f64(F, g, 0.0, (int32_t)P, x, &used) != 0 &&
-        qgt_cholesky_solve_f64(F, g, 1e-12 * (md > 0 ? md : 1.0), (int32_t)P, x, &used) != 0)
-        memcpy(x, g, sizeof(double) * P); /* the reference returns the plain gradient on failure */
+    if (P > 8192 || qgt_dev_ref_cg(F, g, (int32_t)P, x) != 0) memcpy(x, g, sizeof(double) * P);
 }

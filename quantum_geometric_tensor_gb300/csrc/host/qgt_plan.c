@@ -1920,7 +1920,13 @@ int qgt_plan_execute_host(qgt_plan_t* p, const double* theta, double* Q, double*
                 if (natgrad &&
                     (rc = qgt_dev_memcpy_d2h(p->natgrad_pin, p->natgrad_d, sizeof(double) * B * Pd, p->stream)) != 0)
                     return rc;
+                if ((rc = qgt_dev_memcpy_d2h(p->status_pin, p->status_d, sizeof(double) * 2, p->stream)) != 0)
+                    return rc;
                 if ((rc = qgt_dev_stream_sync(p->stream)) != 0) return rc;
+                if ((int)p->status_pin[0] != 0)
+                    return qgt_set_error((int)p->status_pin[0],
+                                         "cholesky: not positive definite after lambda retries (last lambda %g)",
+                                         p->status_pin[1]);
             }
         } else {
             for (size_t b = 0; b < B; b++)
@@ -2055,6 +2061,18 @@ int qgt_cholesky_solve_f64(const double* A, const double* g, double lambda, int3
     if (lambda_used) *lambda_used = st[1];
     if ((int)st[0]) return qgt_set_error((int)st[0], "cholesky: matrix not positive definite after lambda retries");
     return 0;
+}
+
+int qgt_plan_test_gram_stall(qgt_plan_t* p, int stall, int64_t timeout_ns)
+{
+    if (!p) return qgt_set_error(E_INVAL, "qgt_plan_test_gram_stall: plan is NULL");
+    if (!p->dg) return qgt_set_error(E_STATE, "qgt_plan_test_gram_stall: the plan has no integer-digit Gram");
+    if ((stall && timeout_ns <= 0) || timeout_ns > 4000000000LL)
+        return qgt_set_error(E_INVAL, "qgt_plan_test_gram_stall: timeout %lld ns out of range (a stall needs (0, 4 s])",
+                             (long long)timeout_ns);
+    int rc = qgt_dev_stream_sync(p->stream);
+    if (!rc) rc = qgt_dev_dg_gram_set_stall(p->dg, stall, timeout_ns, p->stream);
+    return rc;
 }
 
 int qgt_plan_enqueue_step(qgt_plan_t* p, void* stream)

@@ -254,6 +254,9 @@ int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, const uint32_
                            int32_t point_rows, qgt_dg_gram_t** g);
 int qgt_dev_dg_gram_run(qgt_dg_gram_t* g, double* HG, void* stream);
 int qgt_dev_dg_gram_status(qgt_dg_gram_t* g, void* stream);
+/* wait settings read by every later run (tests of the bounded-wait error path): stall = 1 makes the
+ * converter warps wait on a barrier nothing arrives on; timeout_ns = each wait's limit (0: 4 s) */
+int qgt_dev_dg_gram_set_stall(qgt_dg_gram_t* g, int stall, int64_t timeout_ns, void* stream);
 /* device address of the kernel's error flag (int; 0 = no error), for a copy queued with others */
 const int* qgt_dev_dg_gram_err(const qgt_dg_gram_t* g);
 void qgt_dev_dg_gram_destroy(qgt_dg_gram_t* g);
@@ -362,6 +365,21 @@ int qgt_dev_pcg(const double* Q, int32_t complex_input, int64_t sys_stride, cons
                 const double* d, const double* U, int32_t r, double tol, int32_t max_iter, double* x, int32_t* iters,
                 double* resid, int32_t nsys, void* stream);
 int qgt_dev_axpy_update(double* theta, const double* x, double eta, int32_t n, void* stream);
+
+/* ---- dense complex linear algebra of the reference entry points (qgt_linalg.cu; host buffers in
+ * and out, P <= 8192) ---- */
+/* singular values of the P x P complex64 matrix G (row-major {re, im} floats) by one-sided Jacobi in
+ * FP64 (sigma: P doubles, NULL allowed); with g (P complex64) also the pseudo-inverse solution
+ * x = V S^+ U^H g, S^+ dropping sigma <= cutoff (x: 2P doubles) */
+int qgt_dev_svd_pinv(const float* G, int32_t P, double* sigma, const float* g, double cutoff, double* x,
+                     int32_t max_sweeps, int32_t* sweeps);
+/* (G + lambda I) x = g by LU with partial pivoting in FP64 (x: 2P doubles); *singular = 1 when a pivot
+ * has |a|^2 < 1e-10 (the last pivot: when it is zero) */
+int qgt_dev_lu_solve(const float* G, int32_t P, double lambda, const float* g, double* x, int32_t* singular);
+/* F x = g by the reference's conjugate gradients (FP64, F real P x P) */
+int qgt_dev_ref_cg(const double* F, const double* g, int32_t P, double* x);
+/* out (dim x dim complex64) = delta_ij - conj(psi_i) psi_j */
+int qgt_dev_fs_metric(const float* psi, int64_t dim, float* out);
 
 /* more plan accessors (device buffers of a plan) */
 double* qgt_plan_dev_grad(struct qgt_plan* p);

@@ -22,10 +22,17 @@ two-parameter lattice and, from diffgeo_compute_berry_phase
              full-state links), the lattice wrapping at its edges
   loop_phase the loop phase of the lattice's first row of sites
 
+The natural-gradient fixture (natgrad/natgrad_reg.npz) holds, per case, a
+metric G and gradient g and the outputs of compute_regularized_natural_gradient
+(core/quantum_geometric_gradient.c:2887-2964) restated in oracle.py around the
+reference's own LU inverse (core/matrix_operations.c:176-217) with LAPACK
+singular values for kappa and the pseudo-inverse, as the reference's lapack_svd.
+
 Only the circuits and seeded angles are chosen here.  Run from the repository
-root in a container that has the reference tree:
-    make -C oracle && python tests/golden/make_golden.py          (all fixtures)
-  make -C oracle && python tests/golden/make_golden.py berry    (Berry-phase fixtures only)
+root in a container that has the reference tree (REF = its path):
+    make -C oracle REF=... && python tests/golden/make_golden.py          (all fixtures)
+    make -C oracle REF=... && python tests/golden/make_golden.py berry    (Berry-phase fixtures only)
+    make -C oracle REF=... && python tests/golden/make_golden.py natgrad  (natural-gradient fixture only)
 """
 import math
 import os
@@ -109,11 +116,85 @@ def berry_main():
         print(f"{name}: {rows}x{cols} sum flux / 2 pi = {flux.sum() / (2 * math.pi):.3e} -> {os.path.relpath(path, ROOT)}")
 
 
+def natgrad_cases():
+    """(name, G, g, config) with config = (reg, threshold, adaptive, pinv, cutoff)."""
+    rng = np.random.default_rng(2029)
+    out = []
+    z = np.load(os.path.join(ROOT, "tests", "golden", "hea_cz_n6_l3_s2.npz"))
+    P = z["Q"].shape[0]
+    g = z["grad"].astype(np.complex128)
+    # a circuit's QGT (Hermitian, positive semi-definite) with the default config
+    out.append(("circuit_qgt_default", z["Q"], g, (1e-4, 1e8, True, True, 1e-10)))
+    # the same with a larger lambda and no adaptive step
+    out.append(("circuit_qgt_lambda", z["Q"], g, (1e-2, 1e8, False, True, 1e-10)))
+    # condition number 1e10 held exactly by ComplexFloat entries (a permuted diagonal with phases: its
+    # singular values are the moduli of the entries): the adaptive lambda 1e-6 sqrt(kappa) = 0.1 takes over
+    P = 24
+    perm = rng.permutation(P)
+    Gd = np.zeros((P, P), dtype=np.complex128)
+    Gd[perm, np.arange(P)] = np.logspace(0, -10, P) * np.exp(1j * rng.uniform(0, 2 * np.pi, P))
+    gh = rng.standard_normal(P) + 1j * rng.standard_normal(P)
+    out.append(("permuted_diagonal_kappa1e10", Gd, gh, (1e-4, 1e8, True, True, 1e-10)))
+    # general (non-Hermitian) complex matrix, well conditioned: LU on G as given
+    Gn = np.eye(P) * 3 + (rng.standard_normal((P, P)) + 1j * rng.standard_normal((P, P))) / np.sqrt(P)
+    out.append(("nonhermitian", Gn, gh, (1e-4, 1e8, True, True, 1e-10)))
+    # G + lambda I singular (a row and column of G equal to -lambda e_k): LU fails, the pseudo-inverse
+    # of the unregularised G answers
+    Gs = np.array(Gn)
+    Gs[5, :] = 0
+    Gs[:, 5] = 0
+    Gs[5, 5] = -np.float32(1e-4)
+    out.append(("singular_after_lambda", Gs, gh, (1e-4, 1e8, False, True, 1e-10)))
+    # rank-deficient PSD matrix through the pseudo-inverse path with a cutoff that drops the null space
+    B = rng.standard_normal((P, 16)) + 1j * rng.standard_normal((P, 16))
+    Gr = B @ B.conj().T / 16
+    out.append(("rank16_pinv_only", Gr, gh, None))
+    return out
+
+
+def natgrad_main():
+    ref = O.Reference()
+    arrays = {}
+    for name, G, g, cfg in natgrad_cases():
+        G32 = np.asarray(G, dtype=np.complex64)
+        g32 = np.asarray(g, dtype=np.complex64)
+        arrays[f"{name}__G"] = G32
+        arrays[f"{name}__g"] = g32
+        arrays[f"{name}__kappa"] = np.float64(O.condition_number_f32(G32))
+        if cfg is None:
+            x = O.pseudoinverse_natural_gradient(g32, G32, 1e-6)
+            arrays[f"{name}__pinv_x"] = x
+            print(f"{name}: pinv |x| = {np.linalg.norm(x):.4e}")
+            continue
+        x, lam, kappa, path = O.regularized_natural_gradient(ref, g32, G32, *cfg)
+        arrays[f"{name}__cfg"] = np.array([cfg[0], cfg[1], float(cfg[2]), float(cfg[3]), cfg[4]])
+        arrays[f"{name}__x"] = x
+        arrays[f"{name}__lambda"] = np.float64(lam)
+        arrays[f"{name}__path"] = np.array(path)
+        print(f"{name}: kappa {arrays[f'{name}__kappa']:.3e} lambda {lam:.3e} path {path} |x| {np.linalg.norm(x):.4e}")
+    # the reference CG (compute_natural_gradient_cpu) on a rank-deficient Fisher matrix (no lambda)
+    rng = np.random.default_rng(2030)
+    B = rng.standard_normal((40, 12))
+    F = B @ B.T / 12
+    gF = B @ rng.standard_normal(12)   # in the range of F: CG converges inside it
+    arrays["cg_rankdef__F"] = F
+    arrays["cg_rankdef__g"] = gF
+    arrays["cg_rankdef__x"] = ref.natural_gradient_cg(F, gF)
+    print(f"cg_rankdef: |x| = {np.linalg.norm(arrays['cg_rankdef__x']):.4e}")
+    d = os.path.join(ROOT, "tests", "golden", "natgrad")
+    os.makedirs(d, exist_ok=True)
+    np.savez_compressed(os.path.join(d, "natgrad_reg.npz"), **arrays)
+
+
 def main():
     if sys.argv[1:] == ["berry"]:
         berry_main()
         return
+    if sys.argv[1:] == ["natgrad"]:
+        natgrad_main()
+        return
     berry_main()
+    natgrad_main()
     ref = O.Reference()
     for name, n, gates, theta in cases():
         psi = ref.simulate(n, gates, theta)

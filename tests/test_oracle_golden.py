@@ -181,3 +181,29 @@ def test_small_plaquette_flux_is_twice_curvature(orc):
     psi, D = orc.derivatives(n, g, th)
     Q = orc.qgt_from_states(psi, D)
     assert abs(F[0, 0] / h ** 2 - 2 * Q[pa, pb].imag) < 1e-5
+
+
+@pytest.mark.parametrize("slices", [1, 3, 7, 1000])
+def test_sliced_qgt_job_equals_one_shot(orc, slices):
+    """The CPU baseline's sliced full step gives the one-shot oracle's Q, energy, gradient and step."""
+    n, L = 8, 3
+    g = O.ansatz(n, L, "cz")
+    P = O.num_params(g)
+    th = O.splitmix64_params(12, P)
+    psi, D = orc.derivatives(n, g, th)
+    Qref = orc.qgt_from_states(psi, D)
+    hp = orc.tfim_apply(n, psi)
+    gref = orc.energy_grad(D, hp)
+    eref = float(np.vdot(psi, hp).real)
+    xref, _ = orc.cholesky_solve(Qref.real, gref, 1e-3)
+    job = orc.qgt_job(n, g, th, slices)
+    k = 0
+    while job.step() > 0:
+        k += 1
+    assert k + 1 == min(slices, P)
+    r = job.result()
+    assert np.linalg.norm(r["Q"] - Qref) < 1e-12 * np.linalg.norm(Qref)
+    assert np.linalg.norm(r["grad"] - gref) < 1e-12 * np.linalg.norm(gref)
+    assert abs(r["energy"] - eref) < 1e-12
+    assert np.linalg.norm(r["natgrad"] - xref) < 1e-9 * np.linalg.norm(xref)
+    job.close()
