@@ -225,7 +225,9 @@ def run_gb300(args, ws, rank, local):
     gates = Q.ansatz_gates(nq, nl, ENT)
     P = 2 * nq * nl
     theta = O.splitmix64_params(SEED + rank, P)
+    t0 = time.perf_counter()
     plan = Q.Plan(nq, gates, P, precision=Q.MIXED, lam=LAMBDA, device=dev)
+    t_create = time.perf_counter() - t0
     info = plan.info()
     th_d = torch.tensor(theta, dtype=torch.float64, device=f"cuda:{dev}")
     Q_d = torch.zeros((P, P, 2), dtype=torch.float64, device=f"cuda:{dev}")
@@ -360,7 +362,8 @@ def run_gb300(args, ws, rank, local):
             "gate_hbm_gbs": gate_gbs,
             "gram_tflops_algorithmic": gram_tf,
             "plan": {"passes": info.num_passes, "vector_passes": info.vector_passes, "tile_bits": info.tile_bits,
-                     "device_gb": info.device_bytes / 1e9},
+                     "device_gb": info.device_bytes / 1e9, "compiled_passes": info.jit_passes,
+                     "create_s": t_create},
             "fp64_gpu": fp64,
             "clocks": clk.summary(),
             "cpu_baseline": cb}

@@ -128,6 +128,7 @@ typedef struct {
     int64_t device_bytes;                                  /* device memory held by the plan */
     int32_t batch, num_deriv_params;                       /* points per step; output width Pd */
     int32_t meet_in_middle, cut_gate;                      /* transport used; first gate of the backward half */
+    int32_t jit_passes;                                    /* passes running as compiled straight-line kernels */
 } qgt_plan_info_t;
 
 /* Default options: MIXED, TFIM J = h = 1, lambda = 1e-3, device 0, graph on. */

@@ -43,7 +43,8 @@ class PlanInfo(C.Structure):
                 ("num_rows", C.c_int32), ("num_passes", C.c_int32), ("num_launches", C.c_int32),
                 ("tile_bits", C.c_int32), ("vector_passes", C.c_int64), ("gate_bytes", C.c_int64),
                 ("gram_flops", C.c_int64), ("device_bytes", C.c_int64), ("batch", C.c_int32),
-                ("num_deriv_params", C.c_int32), ("meet_in_middle", C.c_int32), ("cut_gate", C.c_int32)]
+                ("num_deriv_params", C.c_int32), ("meet_in_middle", C.c_int32), ("cut_gate", C.c_int32),
+                ("jit_passes", C.c_int32)]
 
 
 class BatchOptions(C.Structure):

@@ -24,298 +24,7 @@
 
 #include "../qgt_internal.h"
 
-template <typename R> struct v2of;
-template <> struct v2of<float> { typedef float2 T; };
-template <> struct v2of<double> { typedef double2 T; };
-
-// role-encoded bit: 0..4 lane bit, 8 + i reg bit i, 16 + w warp bit w, 32 outside the tile (physical qubit q)
-#define RL_REG 8
-#define RL_WARP 16
-#define RL_OUT 32
-
-template <typename T, typename R>
-struct Cf {
-    R m[8];
-};
-
-template <typename R>
-__device__ __forceinline__ void load_coef(const void* tab, int idx, R* m)
-{
-    const R* t = reinterpret_cast<const R*>(tab) + 8 * idx;
-#pragma unroll
-    for (int i = 0; i < 8; i++) m[i] = __ldg(t + i);
-}
-
-template <typename T, typename R>
-__device__ __forceinline__ T cm(R ar, R ai, T x)
-{
-    T o;
-    o.x = ar * x.x - ai * x.y;
-    o.y = ar * x.y + ai * x.x;
-    return o;
-}
-
-template <typename T, typename R>
-__device__ __forceinline__ T cmad2(const R* m, T x, T y)  // (m0 + i m1) x + (m2 + i m3) y
-{
-    T o;
-    o.x = m[0] * x.x - m[1] * x.y + m[2] * y.x - m[3] * y.y;
-    o.y = m[0] * x.y + m[1] * x.x + m[2] * y.y + m[3] * y.x;
-    return o;
-}
-
-template <typename T, typename R>
-__device__ __forceinline__ T rmad2(R a, T x, R b, T y)  // real a x + b y
-{
-    T o;
-    o.x = a * x.x + b * y.x;
-    o.y = a * x.y + b * y.y;
-    return o;
-}
-
-// complex64: packed FP32x2 arithmetic (one instruction per two lanes of a
-// complex number); per component the same rounding as fmaf
-template <>
-__device__ __forceinline__ float2 rmad2<float2, float>(float a, float2 x, float b, float2 y)
-{
-    return __ffma2_rn(make_float2(a, a), x, __fmul2_rn(make_float2(b, b), y));
-}
-
-template <>
-__device__ __forceinline__ float2 cmad2<float2, float>(const float* m, float2 x, float2 y)
-{
-    // (m0 + i m1) x + (m2 + i m3) y with i z = (-z.y, z.x)
-    const float2 xs = make_float2(-x.y, x.x), ys = make_float2(-y.y, y.x);
-    float2 o = __fmul2_rn(make_float2(m[3], m[3]), ys);
-    o = __ffma2_rn(make_float2(m[2], m[2]), y, o);
-    o = __ffma2_rn(make_float2(m[1], m[1]), xs, o);
-    return __ffma2_rn(make_float2(m[0], m[0]), x, o);
-}
-
-// real a x + y
-template <typename T, typename R>
-__device__ __forceinline__ T fma_s(R a, T x, T y)
-{
-    T o;
-    o.x = a * x.x + y.x;
-    o.y = a * x.y + y.y;
-    return o;
-}
-template <>
-__device__ __forceinline__ float2 fma_s<float2, float>(float a, float2 x, float2 y)
-{
-    return __ffma2_rn(make_float2(a, a), x, y);
-}
-
-// (pr + i pi) x
-template <typename T, typename R>
-__device__ __forceinline__ T cmul_s(R pr, R pi, T x)
-{
-    T o;
-    o.x = pr * x.x - pi * x.y;
-    o.y = pr * x.y + pi * x.x;
-    return o;
-}
-template <>
-__device__ __forceinline__ float2 cmul_s<float2, float>(float pr, float pi, float2 x)
-{
-    return __ffma2_rn(make_float2(pr, pr), x, __fmul2_rn(make_float2(pi, pi), make_float2(-x.y, x.x)));
-}
-
-template <typename T>
-__device__ __forceinline__ T shfl_x(T v, int mask);
-template <>
-__device__ __forceinline__ float2 shfl_x<float2>(float2 v, int mask)
-{
-    return make_float2(__shfl_xor_sync(0xffffffffu, v.x, mask), __shfl_xor_sync(0xffffffffu, v.y, mask));
-}
-template <>
-__device__ __forceinline__ double2 shfl_x<double2>(double2 v, int mask)
-{
-    return make_double2(__shfl_xor_sync(0xffffffffu, v.x, mask), __shfl_xor_sync(0xffffffffu, v.y, mask));
-}
-
-// ---- butterflies on a register bit ----
-template <int RI, int NR, bool real, typename T, typename R>
-__device__ __forceinline__ void u_reg(T* v, const R* m)
-{
-#pragma unroll
-    for (int j = 0; j < NR; j++) {
-        if (j & (1 << RI)) continue;
-        const int k = j | (1 << RI);
-        T a0 = v[j], a1 = v[k];
-        if (real) {
-            v[j] = rmad2<T, R>(m[0], a0, m[2], a1);
-            v[k] = rmad2<T, R>(m[4], a0, m[6], a1);
-        } else {
-            v[j] = cmad2<T, R>(m, a0, a1);
-            v[k] = cmad2<T, R>(m + 4, a0, a1);
-        }
-    }
-}
-
-// tangent-form rotation [[1, m2], [m4, 1]]: one multiply-add per component
-template <int RI, int NR, typename T, typename R>
-__device__ __forceinline__ void tan_reg(T* v, R m2, R m4)
-{
-#pragma unroll
-    for (int j = 0; j < NR; j++) {
-        if (j & (1 << RI)) continue;
-        const int k = j | (1 << RI);
-        const T a0 = v[j], a1 = v[k];
-        v[j] = fma_s<T, R>(m2, a1, a0);
-        v[k] = fma_s<T, R>(m4, a0, a1);
-    }
-}
-
-// cotangent form [[m0, -SG], [SG, m6]], SG = +1 or -1
-template <int RI, int NR, int SG, typename T, typename R>
-__device__ __forceinline__ void cot_reg(T* v, R m0, R m6)
-{
-#pragma unroll
-    for (int j = 0; j < NR; j++) {
-        if (j & (1 << RI)) continue;
-        const int k = j | (1 << RI);
-        const T a0 = v[j], a1 = v[k];
-        T n;
-        if (SG > 0) {
-            n.x = -a1.x;
-            n.y = -a1.y;
-            v[j] = fma_s<T, R>(m0, a0, n);
-            v[k] = fma_s<T, R>(m6, a1, a0);
-        } else {
-            n.x = -a0.x;
-            n.y = -a0.y;
-            v[j] = fma_s<T, R>(m0, a0, a1);
-            v[k] = fma_s<T, R>(m6, a1, n);
-        }
-    }
-}
-
-template <int RI, int NR, typename T, typename R>
-__device__ __forceinline__ void phase_reg(T* v, const R* m)
-{
-#pragma unroll
-    for (int j = 0; j < NR; j++) v[j] = (j & (1 << RI)) ? cm<T, R>(m[6], m[7], v[j]) : cm<T, R>(m[0], m[1], v[j]);
-}
-
-// CNOT with reg target RI, control given by a per-register predicate mask (bit j of cmask)
-template <int RI, int NR, typename T>
-__device__ __forceinline__ void cnot_reg(T* v, uint32_t cmask)
-{
-#pragma unroll
-    for (int j = 0; j < NR; j++) {
-        if (j & (1 << RI)) continue;
-        const int k = j | (1 << RI);
-        if ((cmask >> j) & 1u) { T t = v[j]; v[j] = v[k]; v[k] = t; }
-    }
-}
-
-// (-i/2) X or (-i/2) Y on reg bit RI (exact)
-template <int RI, int NR, typename T, typename R>
-__device__ __forceinline__ void gen_reg(T* v, int gen)
-{
-    const R h = (R)0.5;
-#pragma unroll
-    for (int j = 0; j < NR; j++) {
-        if (j & (1 << RI)) continue;
-        const int k = j | (1 << RI);
-        T a0 = v[j], a1 = v[k], o0, o1;
-        if (gen == QGEN_X) { o0.x = h * a1.y; o0.y = -h * a1.x; o1.x = h * a0.y; o1.y = -h * a0.x; }
-        else { o0.x = -h * a1.x; o0.y = -h * a1.y; o1.x = h * a0.x; o1.y = h * a0.y; }
-        v[j] = o0;
-        v[k] = o1;
-    }
-}
-
-#define RB_SWITCH(ri, CALL)                         \
-    switch (ri) {                                   \
-    case 0: CALL(0); break;                         \
-    case 1: CALL(1); break;                         \
-    case 2: CALL(2); break;                         \
-    case 3: CALL(3); break;                         \
-    default: if (RB > 4) { CALL(4 % RB); } break;   \
-    }
-
-// one single-qubit gate on register bit RI; real rotations in tangent form
-// [[1, -t], [t, 1]] or [[k, -g], [g, k]] (g = +-1) take the one-multiply-add
-// paths (the form is uniform per CTA: one coefficient table per point)
-template <int RI, int NR, typename T, typename R>
-__device__ __forceinline__ void gate_reg(T* v, const R* m, bool real)
-{
-    const bool tanf = real && m[0] == (R)1 && m[6] == (R)1;
-    const bool cotf = real && !tanf && m[2] == -m[4] && (m[4] == (R)1 || m[4] == (R)-1);
-    if (tanf) tan_reg<RI, NR, T, R>(v, m[2], m[4]);
-    else if (cotf && m[4] > (R)0) cot_reg<RI, NR, 1, T, R>(v, m[0], m[6]);
-    else if (cotf) cot_reg<RI, NR, -1, T, R>(v, m[0], m[6]);
-    else if (real) u_reg<RI, NR, true, T, R>(v, m);
-    else u_reg<RI, NR, false, T, R>(v, m);
-}
-
-// the same on lane bit b: v' = c_self v + c_partner w (w = the partner lane's
-// amplitude); row 1 of the matrix for the upper lane, row 0 for the lower one
-template <int NR, typename T, typename R>
-__device__ __forceinline__ void gate_lane(T* v, const R* m, bool real, int b, int lane)
-{
-    const bool tanf = real && m[0] == (R)1 && m[6] == (R)1;
-    const bool cotf = real && !tanf && m[2] == -m[4] && (m[4] == (R)1 || m[4] == (R)-1);
-    const int hi = (lane >> b) & 1;
-    const R cs0 = hi ? m[6] : m[0], cs1 = hi ? m[7] : m[1];
-    const R cp0 = hi ? m[4] : m[2], cp1 = hi ? m[5] : m[3];
-    if (tanf) {
-        // own + c w
-#pragma unroll
-        for (int j = 0; j < NR; j++) {
-            const T w = shfl_x<T>(v[j], 1 << b);
-            v[j] = fma_s<T, R>(cp0, w, v[j]);
-        }
-    } else if (cotf) {
-        // k own + c w with c = -g (lower lane) or +g (upper lane)
-#pragma unroll
-        for (int j = 0; j < NR; j++) {
-            T w = shfl_x<T>(v[j], 1 << b);
-            w.x *= cp0;
-            w.y *= cp0;
-            v[j] = fma_s<T, R>(cs0, v[j], w);
-        }
-    } else if (real) {
-#pragma unroll
-        for (int j = 0; j < NR; j++) {
-            const T w = shfl_x<T>(v[j], 1 << b);
-            v[j] = rmad2<T, R>(cs0, v[j], cp0, w);
-        }
-    } else {
-        const R mm[4] = {cs0, cs1, cp0, cp1};
-#pragma unroll
-        for (int j = 0; j < NR; j++) {
-            const T w = shfl_x<T>(v[j], 1 << b);
-            v[j] = cmad2<T, R>(mm, v[j], w);
-        }
-    }
-}
-
-// bit value of a non-register role for this thread
-__device__ __forceinline__ int role_bit(int role, int q, int lane, int warp, uint64_t base)
-{
-    if (role < RL_REG) return (lane >> role) & 1;
-    if (role < RL_OUT) return (warp >> (role - RL_WARP)) & 1;
-    return (int)((base >> q) & 1);
-}
-
-// per-register mask of "bit is 1" for any role: reg -> pattern over j; other -> all or nothing
-template <int NR>
-__device__ __forceinline__ uint32_t role_mask(int role, int q, int lane, int warp, uint64_t base)
-{
-    const uint32_t all = (NR == 32) ? 0xffffffffu : ((1u << NR) - 1u);
-    if (role >= RL_REG && role < RL_WARP) {
-        const int ri = role - RL_REG;
-        uint32_t m = 0;
-#pragma unroll
-        for (int j = 0; j < NR; j++) m |= (uint32_t)((j >> ri) & 1) << j;
-        return m;
-    }
-    return role_bit(role, q, lane, warp, base) ? all : 0u;
-}
+#include "qgt_pass2_ops.cuh"
 
 // CKPT: the launch's entries also store their state before every Q2_SEG op whose slot is >= 0 (the
 // checkpoint writers of a pass; spawns then run the program from that segment on)

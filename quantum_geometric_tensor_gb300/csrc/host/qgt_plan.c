@@ -27,6 +27,7 @@
  * functions of the same Pauli (Z-type, X-type or Y-type).
  */
 #include <math.h>
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -72,6 +73,7 @@ typedef struct {
     int tile_bits;
     uint32_t tile_mask;
     int8_t l2p[16];
+    qgt_jit_kernel_t* jit[2];     /* the pass program as straight-line kernels: [0] entries, [1] checkpoint writer */
 } spass_t;
 
 struct qgt_plan {
@@ -159,6 +161,7 @@ struct qgt_plan {
     int64_t device_bytes;
     int64_t vector_passes, gate_bytes;
     int wide;                     /* complex64 passes on 14-bit tiles (choose_tile) */
+    int njit;                     /* passes running as compiled straight-line kernels */
     int launches;
     int has_run;
     void* prof_ev[7];             /* phase events of qgt_plan_profile_step (NULL otherwise) */
@@ -1233,6 +1236,144 @@ static int fold_diagonal_runs(qgt_plan_t* p)
 
 static int run_step(qgt_plan_t* p);
 
+/* Straight-line pass kernels (qgt_jit.c): complex64 plans of MIXED precision
+ * whose passes run on 13- or 14-qubit register tiles, from 16 qubits on (or
+ * for every such plan with QGT_PASS_JIT=1; QGT_PASS_JIT=0 keeps the
+ * interpreter).  The kernels of one plan compile in parallel. */
+typedef struct {
+    qgt_jit_pass_desc_t d;
+    char* src;
+    int32_t smem, device;
+    qgt_jit_kernel_t* out;
+    int rc;
+    char err[256];
+} jit_job_t;
+
+static void* jit_worker(void* arg)
+{
+    jit_job_t* j = (jit_job_t*)arg;
+    j->rc = qgt_dev_jit_compile(j->src, j->d.kname, j->smem, j->device, &j->out);
+    if (j->rc) snprintf(j->err, sizeof j->err, "%s", qgt_last_error());
+    return NULL;
+}
+
+static int jit_wanted(const qgt_plan_t* p)
+{
+    const char* env = getenv("QGT_PASS_JIT");
+    if (p->fp64 || p->opt.precision != QGT_PRECISION_MIXED) return 0;
+    if (env && env[0] == '0') return 0;
+    if (env && env[0] == '1') return 1;
+    return p->n >= 16;
+}
+
+/* the sources of every compiled pass kernel of the plan (host only) */
+typedef struct {
+    jit_job_t* jobs;
+    int nj;
+    int32_t* starts;
+    int8_t* start_zero;
+    char (*names)[48];
+} jit_set_t;
+
+static void jit_set_free(jit_set_t* js)
+{
+    for (int i = 0; i < js->nj; i++) free(js->jobs[i].src);
+    free(js->jobs);
+    free(js->starts);
+    free(js->start_zero);
+    free(js->names);
+    memset(js, 0, sizeof *js);
+}
+
+static int jit_prepare(qgt_plan_t* p, jit_set_t* js)
+{
+    memset(js, 0, sizeof *js);
+    js->jobs = (jit_job_t*)calloc((size_t)2 * p->npasses + 1, sizeof(jit_job_t));
+    js->starts = (int32_t*)malloc(sizeof(int32_t) * ((size_t)p->nents + 2 * p->npasses + 1));
+    js->start_zero = (int8_t*)calloc((size_t)p->nents + 2 * p->npasses + 1, 1);
+    js->names = (char (*)[48])calloc((size_t)2 * p->npasses + 1, 48);
+    if (!js->jobs || !js->starts || !js->start_zero || !js->names) { jit_set_free(js); return qgt_set_error(E_NOMEM, "jit: oom"); }
+    int at = 0;
+    for (int k = 0; k < p->npasses; k++) {
+        spass_t* ps = &p->passes[k];
+        if (ps->prog_count <= 0 || (ps->tile_bits != QGT_TILE_MAX_F32 && ps->tile_bits != QGT_TILE_WIDE_F32)) continue;
+        for (int ck = 0; ck <= (ps->ckpt_writer ? 1 : 0); ck++) {
+            /* the starts of the entries this kernel runs: all of the pass (ck = 0), the writer (ck = 1) */
+            int32_t* st = js->starts + at;
+            int8_t* sz = js->start_zero + at;
+            int ns = 0;
+            const int e0 = ps->ent_begin, e1 = ck ? ps->ent_begin + 1 : ps->ent_begin + ps->ent_count;
+            for (int i = e0; i < e1; i++) {
+                int t = 0;
+                while (t < ns && st[t] != p->ents_h[i].start_op) t++;
+                if (t == ns) { st[ns] = p->ents_h[i].start_op; sz[ns] = 0; ns++; }
+                if (p->ents_h[i].flags & QENT_SRC_ZERO) sz[t] = 1;
+            }
+            at += ns;
+            jit_job_t* j = &js->jobs[js->nj];
+            snprintf(js->names[js->nj], 48, "qgt_pass%d_%s", k, ck ? "ckpt" : "run");
+            j->d.prog = p->prog_h + ps->prog_begin;
+            j->d.nops = ps->prog_count;
+            j->d.segs = p->segs_h;
+            j->d.l2p = ps->l2p;
+            j->d.n = p->n;
+            j->d.tile_bits = ps->tile_bits;
+            j->d.RB = reg_bits(p);
+            j->d.WB = ps->tile_bits - 5 - j->d.RB;
+            j->d.tile_mask = ps->tile_mask;
+            j->d.ckpt = ck;
+            j->d.starts = st;
+            j->d.start_zero = sz;
+            j->d.nstarts = ns;
+            j->d.kname = js->names[js->nj];
+            j->smem = (int32_t)(8 << ps->tile_bits);
+            j->device = p->opt.device;
+            j->src = qgt_jit_pass_source(&j->d);
+            if (!j->src) { int rc = qgt_last_error()[0] ? -1 : E_NOMEM; jit_set_free(js); return rc; }
+            js->nj++;
+        }
+    }
+    return 0;
+}
+
+static int build_jit(qgt_plan_t* p)
+{
+    p->njit = 0;
+    if (!jit_wanted(p)) return 0;
+    jit_set_t js;
+    int rc = jit_prepare(p, &js);
+    if (rc) return rc;
+    jit_job_t* jobs = js.jobs;
+    const int nj = js.nj;
+    if (nj) {
+        pthread_t* th = (pthread_t*)calloc((size_t)nj, sizeof(pthread_t));
+        int* started = (int*)calloc((size_t)nj, sizeof(int));
+        if (!th || !started) rc = qgt_set_error(E_NOMEM, "jit: oom");
+        for (int i = 0; !rc && i < nj; i++) started[i] = pthread_create(&th[i], NULL, jit_worker, &jobs[i]) == 0;
+        for (int i = 0; !rc && i < nj; i++) {
+            if (started[i]) pthread_join(th[i], NULL);
+            else jit_worker(&jobs[i]);
+        }
+        free(th);
+        free(started);
+        for (int i = 0; !rc && i < nj; i++)
+            if (jobs[i].rc) rc = qgt_set_error(jobs[i].rc, "%s", jobs[i].err);
+    }
+    if (!rc) {
+        int i = 0;
+        for (int k = 0; k < p->npasses && i < nj; k++) {
+            spass_t* ps = &p->passes[k];
+            if (jobs[i].d.prog != p->prog_h + ps->prog_begin) continue;
+            ps->jit[0] = jobs[i++].out;
+            if (ps->ckpt_writer && i < nj) ps->jit[1] = jobs[i++].out;
+            p->njit++;
+        }
+    }
+    jit_set_free(&js);
+    if (rc) { for (int k = 0; k < p->npasses; k++) p->passes[k].jit[0] = p->passes[k].jit[1] = NULL; p->njit = 0; }
+    return rc;
+}
+
 static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, qgt_plan_t** out, int host_only);
 
 int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, qgt_plan_t** out)
@@ -1240,6 +1381,8 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
     return plan_create(c, opt, out, 0);
 }
 
+/* host_only: 0 a full plan; 1 the schedule without checkpoints (qgt_plan_schedule_dump); 2 the
+ * schedule with checkpoints (qgt_plan_jit_check); 1 and 2 hold no device resources */
 static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, qgt_plan_t** out, int host_only)
 {
     int rc = 0;
@@ -1324,7 +1467,7 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
     if ((rc = build_programs(p)) != 0) goto fail;
     if ((rc = fold_diagonal_runs(p)) != 0) goto fail;
     if ((rc = build_renorm(p)) != 0) goto fail;
-    if (!host_only && (rc = build_checkpoints(p)) != 0) goto fail;
+    if (host_only != 1 && (rc = build_checkpoints(p)) != 0) goto fail;
     if (p->opt.hamiltonian == QGT_HAMILTONIAN_PAULI) {
         /* parse the strings: character [n-1-q] acts on qubit q */
         const int T = p->opt.num_pauli_terms;
@@ -1502,6 +1645,7 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
         if ((rc = qgt_dev_host_alloc((void**)&p->gerr_pin, sizeof(int) * 4)) != 0) goto fail;
     }
     if ((rc = qgt_dev_stream_sync(p->stream)) != 0) goto fail;
+    if ((rc = build_jit(p)) != 0) goto fail;
     /* first step eagerly (sets kernel attributes, validates), then capture */
     if ((rc = run_step(p)) != 0) goto fail;
     if ((rc = qgt_dev_stream_sync(p->stream)) != 0) goto fail;
@@ -1586,6 +1730,7 @@ int qgt_plan_get_info(const qgt_plan_t* p, qgt_plan_info_t* info)
     info->num_deriv_params = p->Pd;
     info->meet_in_middle = p->mitm;
     info->cut_gate = p->mitm ? p->cut : -1;
+    info->jit_passes = p->njit;
     info->device_bytes = p->device_bytes;
     return 0;
 }
@@ -1619,6 +1764,14 @@ static int apply_hamiltonian(qgt_plan_t* p, int* launches)
         (*launches)++;
     }
     return 0;
+}
+
+/* one register-resident launch: the pass's compiled kernel when it has one, else the interpreter */
+static int pass2_launch(const spass_t* ps, const qgt_dev_pass2_args_t* b, int fp64, void* stream)
+{
+    const qgt_jit_kernel_t* k = ps->jit[b->ckpt ? 1 : 0];
+    if (k) return qgt_dev_jit_launch(k, b, stream);
+    return qgt_dev_pass2(b, fp64, stream);
 }
 
 static int run_step(qgt_plan_t* p)
@@ -1721,23 +1874,23 @@ static int run_step(qgt_plan_t* p)
                 if ((rc = qgt_dev_stream_wait_event(p->aux_stream, p->ev_fork)) != 0) return rc;
                 b.nentries = 1;
                 b.ckpt = 1;
-                if ((rc = qgt_dev_pass2(&b, p->fp64, p->aux_stream)) != 0) return rc;
+                if ((rc = pass2_launch(ps, &b, p->fp64, p->aux_stream)) != 0) return rc;
                 b.ckpt = 0;
                 if (c0 < nall) {
                     b.entries = a.entries + c0;
                     b.nentries = nall - c0;
-                    if ((rc = qgt_dev_pass2(&b, p->fp64, p->aux_stream)) != 0) return rc;
+                    if ((rc = pass2_launch(ps, &b, p->fp64, p->aux_stream)) != 0) return rc;
                     launches++;
                 }
                 if (c0 > 1) {
                     b.entries = a.entries + 1;
                     b.nentries = c0 - 1;
-                    if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) return rc;
+                    if ((rc = pass2_launch(ps, &b, p->fp64, p->stream)) != 0) return rc;
                     launches++;
                 }
                 if ((rc = qgt_dev_event_record(p->ev_join, p->aux_stream)) != 0) return rc;
                 if ((rc = qgt_dev_stream_wait_event(p->stream, p->ev_join)) != 0) return rc;
-            } else if ((rc = qgt_dev_pass2(&b, p->fp64, p->stream)) != 0) {
+            } else if ((rc = pass2_launch(ps, &b, p->fp64, p->stream)) != 0) {
                 return rc;
             }
         } else if ((rc = qgt_dev_pass(&a, p->fp64, p->stream)) != 0) {
@@ -1905,6 +2058,9 @@ int qgt_plan_execute_host(qgt_plan_t* p, const double* theta, double* Q, double*
     if (energy && (rc = qgt_dev_memcpy_d2h(p->energy_pin, p->energy_d, sizeof(double) * B, p->stream)) != 0) return rc;
     if (natgrad && (rc = qgt_dev_memcpy_d2h(p->natgrad_pin, p->natgrad_d, sizeof(double) * B * Pd, p->stream)) != 0) return rc;
     if ((rc = qgt_dev_stream_sync(p->stream)) != 0) return rc;
+    /* a failed Gram invalidates everything after it: report it first */
+    if (gerr && p->gerr_pin[0])
+        return qgt_set_error(p->gerr_pin[0], "tensor-core Gram reported device status %d", p->gerr_pin[0]);
     if (need_status) {
         if (B == 1) {
             /* the graph's blocked solve has no retries: on a non-positive pivot
@@ -1938,8 +2094,6 @@ int qgt_plan_execute_host(qgt_plan_t* p, const double* theta, double* Q, double*
     if (grad) memcpy(grad, p->grad_pin, sizeof(double) * B * Pd);
     if (energy) memcpy(energy, p->energy_pin, sizeof(double) * B);
     if (natgrad) memcpy(natgrad, p->natgrad_pin, sizeof(double) * B * Pd);
-    if (gerr && p->gerr_pin[0])
-        return qgt_set_error(p->gerr_pin[0], "tensor-core Gram reported device status %d", p->gerr_pin[0]);
     return 0;
 }
 
@@ -2000,10 +2154,11 @@ int qgt_plan_device_status(qgt_plan_t* p, double* lambda_used)
     if (!rc) rc = qgt_dev_stream_sync(p->stream);
     if (rc) return rc;
     if (lambda_used) *lambda_used = p->status_pin[1];
+    /* the Gram's status first: a failed Gram makes the solve's status meaningless */
     int st = 0;
-    for (int b = 0; b < p->B && !st; b++) st = (int)p->status_pin[2 * b];
-    if (!st && p->tc) st = qgt_dev_tc_gram_status(p->tc, p->stream);
+    if (p->tc) st = qgt_dev_tc_gram_status(p->tc, p->stream);
     if (!st && p->dg) st = qgt_dev_dg_gram_status(p->dg, p->stream);
+    for (int b = 0; b < p->B && !st; b++) st = (int)p->status_pin[2 * b];
     return st;
 }
 
@@ -2073,6 +2228,40 @@ int qgt_plan_test_gram_stall(qgt_plan_t* p, int stall, int64_t timeout_ns)
     int rc = qgt_dev_stream_sync(p->stream);
     if (!rc) rc = qgt_dev_dg_gram_set_stall(p->dg, stall, timeout_ns, p->stream);
     return rc;
+}
+
+/* The compiled pass kernels of a plan without a device: the schedule (with
+ * checkpoints), every pass's generated source (written to dump_dir when given)
+ * and, with compile = 1, each source through the compiler (no load).  Returns
+ * the number of kernels (or a negative error); *seconds = compile time. */
+int qgt_plan_jit_check(const void* circuit, const void* options, const char* dump_dir, int compile, double* seconds)
+{
+    qgt_plan_t* p = NULL;
+    int rc = plan_create((const qgt_circuit_desc_t*)circuit, (const qgt_plan_options_t*)options, &p, 2);
+    if (rc) return rc;
+    jit_set_t js;
+    if ((rc = jit_prepare(p, &js)) != 0) { qgt_plan_destroy(p); return rc; }
+    double tot = 0;
+    for (int i = 0; i < js.nj && !rc; i++) {
+        if (dump_dir) {
+            char path[1024];
+            snprintf(path, sizeof path, "%s/%s.cu", dump_dir, js.jobs[i].d.kname);
+            FILE* f = fopen(path, "w");
+            if (!f) { rc = qgt_set_error(E_INVAL, "qgt_plan_jit_check: cannot write %s", path); break; }
+            fputs(js.jobs[i].src, f);
+            fclose(f);
+        }
+        if (compile) {
+            double t = 0;
+            rc = qgt_jit_nvrtc_check(js.jobs[i].src, &t);
+            tot += t;
+        }
+    }
+    const int n = js.nj;
+    jit_set_free(&js);
+    qgt_plan_destroy(p);
+    if (seconds) *seconds = tot;
+    return rc ? rc : n;
 }
 
 int qgt_plan_enqueue_step(qgt_plan_t* p, void* stream)

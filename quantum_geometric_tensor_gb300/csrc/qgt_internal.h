@@ -162,6 +162,35 @@ typedef struct {
                                        into row slot (checkpoints for spawns that start at that segment) */
 } qgt_dev_pass2_args_t;
 int qgt_dev_pass2(const qgt_dev_pass2_args_t* args, int fp64, void* stream);
+
+/* ---- pass programs compiled to straight-line kernels (qgt_jit.c, qgt_jit_rt.cu) ---- */
+typedef struct {
+    const qgt_dev_op2_t* prog;  /* the pass program (prog[0] is its initial Q2_SEG) */
+    int32_t nops;
+    const int8_t* segs;         /* layouts, 16 per index (as qgt_dev_pass2_args_t.segs) */
+    const int8_t* l2p;          /* local bit -> physical qubit of the pass's tile */
+    int32_t n, tile_bits, RB, WB;
+    uint32_t tile_mask;
+    int32_t ckpt;               /* 1: entries store checkpoints before Q2_SEG ops with slot >= 0 */
+    const int32_t* starts;      /* program indices at which the launched entries start */
+    const int8_t* start_zero;   /* per start: 1 if an entry starting there reads |0...0> (QENT_SRC_ZERO) */
+    int32_t nstarts;
+    const char* kname;          /* kernel name */
+} qgt_jit_pass_desc_t;
+/* CUDA source of one pass program (malloc'd; NULL and an error message on failure) */
+char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d);
+typedef struct qgt_jit_kernel qgt_jit_kernel_t;
+/* compile (or take from the process / disk cache) and load for `device`; smem = dynamic shared bytes */
+int qgt_dev_jit_compile(const char* body, const char* kname, int32_t smem, int32_t device, qgt_jit_kernel_t** out);
+/* launch over the entries of a, as qgt_dev_pass2 (complex64 register tiles only) */
+int qgt_dev_jit_launch(const qgt_jit_kernel_t* k, const qgt_dev_pass2_args_t* a, void* stream);
+/* seconds spent in the compiler by this process (cache hits cost nothing) */
+double qgt_dev_jit_compile_seconds(void);
+/* compile a pass kernel body without loading it (no device needed); *seconds = compile time */
+int qgt_jit_nvrtc_check(const char* body, double* seconds);
+/* every compiled pass kernel of a plan, without a device (qgt_plan.c): sources to dump_dir (NULL:
+ * none), compile = 1 also runs each through the compiler; returns the kernel count or an error */
+int qgt_plan_jit_check(const void* circuit, const void* options, const char* dump_dir, int compile, double* seconds);
 /* rho[point][m] = product over groups 0..m of the amplitude scales |column 0|
  * of the complex64 coefficient entries src[ptr[g] .. ptr[g+1]) */
 /* per pass and point: multiply the pass's designated entry ren[pass] by 1 / prod of the scales
