@@ -378,3 +378,91 @@ extern "C" int qgt_dev_overlaps(const void* V, int32_t fp64, int64_t N, const in
     else overlap_kernel<float2><<<grid, 256, 0, s>>>((const float2*)V, N, len, nchunk, a_off, b_off, (double2*)part);
     return qgt_dev_last_error();
 }
+
+// ---------------------------------------------------------------------------
+// Closed-form Berry map.  With theta_a and theta_b each driving one rotation
+// R(t) = cos(t/2) I - i sin(t/2) G (G^2 = I), the circuit's state is
+//     psi(ta, tb) = sum_{r,s in {0,1}} c_r(ta) c_s(tb) v_rs,  c(t) = (cos(t/2), -i sin(t/2)),
+// v_rs the circuit with G_a^r, G_b^s in place of the two rotations; so every
+// inner product among psi, d_a psi, d_b psi is a bilinear form in the 4 x 4
+// Gram K = <v|v>, and the whole G x G lattice of Omega_ab = Im Q_ab follows
+// from K.  The four v_rs come from the states at (ta, tb) in {0, pi}^2:
+//     psi(0,0) = v_00, psi(pi,0) = -i v_10, psi(0,pi) = -i v_01, psi(pi,pi) = -v_11.
+// part holds, per circuit, the partial sums of the 10 overlaps <psi_i|psi_j>
+// (i <= j, in the order (0,0) (0,1) (0,2) (0,3) (1,1) (1,2) (1,3) (2,2) (2,3)
+// (3,3)) over nchunk ranges; maps[circuit][x][y] = Omega at
+// (2 pi x / G, 2 pi y / G).  One CTA per circuit.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) berry_closed_kernel(const double2* __restrict__ part, int nchunk, int G,
+                                                           double* __restrict__ maps)
+{
+    __shared__ double Kr[4][4], Ki[4][4];
+    const int m = blockIdx.x;
+    if (threadIdx.x < 10) {
+        const int pr = threadIdx.x;
+        const int ii[10] = {0, 0, 0, 0, 1, 1, 1, 2, 2, 3}, jj[10] = {0, 1, 2, 3, 1, 2, 3, 2, 3, 3};
+        const double2* pp = part + ((int64_t)m * 10 + pr) * nchunk;
+        double re = 0, im = 0;
+        for (int c = 0; c < nchunk; c++) { re += pp[c].x; im += pp[c].y; }
+        // <v_i|v_j> = conj(f_i) f_j <psi_i|psi_j> with v_i = f_i psi_i, f = (1, i, i, -1)
+        const double fr[4] = {1, 0, 0, -1}, fi[4] = {0, 1, 1, 0};
+        const int i = ii[pr], j = jj[pr];
+        const double ar = fr[i] * fr[j] + fi[i] * fi[j], ai = fr[i] * fi[j] - fi[i] * fr[j];   // conj(f_i) f_j
+        const double kr = ar * re - ai * im, ki = ar * im + ai * re;
+        Kr[i][j] = kr; Ki[i][j] = ki;
+        Kr[j][i] = kr; Ki[j][i] = -ki;
+    }
+    __syncthreads();
+    const double step = 6.283185307179586476925 / (double)G;
+    for (int t = threadIdx.x; t < G * G; t += blockDim.x) {
+        const int x = t / G, y = t % G;
+        double sa, ca, sb, cb;
+        sincos(0.5 * step * x, &sa, &ca);
+        sincos(0.5 * step * y, &sb, &cb);
+        // coefficient vectors over (r, s), index r + 2 s: c = (cos, -i sin), c' = (-sin / 2, -i cos / 2)
+        const double car[2] = {ca, 0}, cai[2] = {0, -sa}, dar[2] = {-0.5 * sa, 0}, dai[2] = {0, -0.5 * ca};
+        const double cbr[2] = {cb, 0}, cbi[2] = {0, -sb}, dbr[2] = {-0.5 * sb, 0}, dbi[2] = {0, -0.5 * cb};
+        double pr_[4], pi_[4], qr[4], qi[4], wr[4], wi[4];   // psi, d_a psi, d_b psi coefficients
+        for (int k = 0; k < 4; k++) {
+            const int r = k & 1, s = k >> 1;
+            pr_[k] = car[r] * cbr[s] - cai[r] * cbi[s];
+            pi_[k] = car[r] * cbi[s] + cai[r] * cbr[s];
+            qr[k] = dar[r] * cbr[s] - dai[r] * cbi[s];
+            qi[k] = dar[r] * cbi[s] + dai[r] * cbr[s];
+            wr[k] = car[r] * dbr[s] - cai[r] * dbi[s];
+            wi[k] = car[r] * dbi[s] + cai[r] * dbr[s];
+        }
+        // x^H K y
+        auto form = [&](const double* xr, const double* xi, const double* yr, const double* yi, double* outr, double* outi) {
+            double sr = 0, si = 0;
+            for (int i = 0; i < 4; i++) {
+                double tr = 0, ti = 0;   // (K y)_i
+                for (int j = 0; j < 4; j++) {
+                    tr += Kr[i][j] * yr[j] - Ki[i][j] * yi[j];
+                    ti += Kr[i][j] * yi[j] + Ki[i][j] * yr[j];
+                }
+                sr += xr[i] * tr + xi[i] * ti;   // conj(x_i) (K y)_i
+                si += xr[i] * ti - xi[i] * tr;
+            }
+            *outr = sr;
+            *outi = si;
+        };
+        double sn, sni, Ar, Ai, Br, Bi, Cr, Ci;
+        form(pr_, pi_, pr_, pi_, &sn, &sni);
+        form(qr, qi, wr, wi, &Ar, &Ai);     // <d_a psi|d_b psi>
+        form(qr, qi, pr_, pi_, &Br, &Bi);   // <d_a psi|psi>
+        form(pr_, pi_, wr, wi, &Cr, &Ci);   // <psi|d_b psi>
+        const double inv = 1.0 / sn;
+        // Im(A / s - B C / s^2)
+        maps[(int64_t)m * G * G + t] = Ai * inv - (Br * Ci + Bi * Cr) * inv * inv;
+    }
+}
+
+extern "C" int qgt_dev_berry_closed(const double* part, int32_t nchunk, int32_t ncirc, int32_t G, double* maps,
+                                    void* stream)
+{
+    if (ncirc <= 0) return 0;
+    if (G < 1 || G > 1024 || nchunk < 1) return qgt_set_error(-1, "berry closed form: grid %d, %d chunks", G, nchunk);
+    berry_closed_kernel<<<ncirc, 256, 0, (cudaStream_t)stream>>>((const double2*)part, nchunk, G, maps);
+    return qgt_dev_last_error();
+}

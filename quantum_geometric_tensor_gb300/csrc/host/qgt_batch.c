@@ -18,11 +18,15 @@
  *   - all plans, with the uploads of theta and downloads of Q, are captured
  *     into one CUDA graph over a few streams (independent groups overlap).
  *
- * Exact reduction used for the maps: when a and b each drive one gate and a's
- * gate comes first, Q_ab does not depend on theta_b (R_b commutes with its
- * generator and is unitary on both derivative states), so the lattice needs
- * G points, one per theta_a, and column j repeats them; likewise with the
- * roles swapped.  Parameters shared by several gates get all G^2 points.
+ * Closed form used for the maps: when a and b each drive one rotation
+ * R(t) = cos(t/2) I - i sin(t/2) G, the truncated circuit's state is
+ * sum_{r,s} c_r(ta) c_s(tb) v_rs with v_rs the circuit with G_a^r, G_b^s in
+ * place of the rotations, so psi, d_a psi and d_b psi at every lattice point
+ * are combinations of four vectors: the plan evaluates the states at
+ * (ta, tb) in {0, pi}^2 (v_rs up to phases), one overlap kernel forms their
+ * 4 x 4 Gram and one kernel evaluates Omega_ab at all G^2 points from it
+ * (qgt_dev_berry_closed).  Parameters shared by several gates get all G^2
+ * points as separate 2 x 2 QGTs.
  */
 #include <math.h>
 #include <stdio.h>
@@ -48,6 +52,12 @@ typedef struct {
     int* perm;              /* circuit parameter k -> plan parameter perm[k], k < nperm */
     int nperm;
     size_t th_off, out_off; /* doubles into the pinned staging buffers */
+    /* closed form (compact pairs): 4 points per circuit, (theta_a, theta_b) in {0, pi}^2; their 10
+     * overlaps per circuit (offsets off_d: a then b, 10 nmem each) -> partial sums part_d -> maps_d */
+    int64_t* off_d;
+    double* part_d;
+    double* maps_d;
+    int nchunk;
 } bplan_t;
 
 struct qgt_batch {
@@ -126,6 +136,9 @@ void qgt_batch_destroy(qgt_batch_t* b)
         qgt_plan_destroy(b->bp[i].plan);
         free(b->bp[i].mem);
         free(b->bp[i].perm);
+        qgt_dev_free(b->bp[i].off_d);
+        qgt_dev_free(b->bp[i].part_d);
+        qgt_dev_free(b->bp[i].maps_d);
     }
     for (int k = 0; k < MAX_STREAMS; k++) if (b->s[k]) qgt_dev_stream_destroy(b->s[k]);
     for (int k = 0; k <= MAX_STREAMS; k++) if (b->ev[k]) qgt_dev_event_destroy(b->ev[k]);
@@ -241,9 +254,10 @@ int qgt_batch_create(const qgt_circuit_desc_t* circuits, int32_t count, const in
             int glast = -1;
             for (int g = 0; g < cc->num_gates; g++)
                 if (cc->gates[g].param == pa || cc->gates[g].param == pb) glast = g;
+            /* one gate each: the closed form over the states at (theta_a, theta_b) in {0, pi}^2 */
             bp->compact = (na == 1 && nb == 1);
             bp->early_is_a = ga < gb;
-            bp->per = bp->compact ? b->G : b->G * b->G;
+            bp->per = bp->compact ? 4 : b->G * b->G;
             bp->nperm = cc->num_params;   /* members with more parameters map the rest beyond bp->P */
             for (int k = 0, nxt = 2; k < cc->num_params; k++)
                 bp->perm[k] = (k == pa) ? 0 : (k == pb) ? 1 : nxt++;
@@ -264,6 +278,29 @@ int qgt_batch_create(const qgt_circuit_desc_t* circuits, int32_t count, const in
             free(tg);
             tg = NULL;
             b->nberry++;
+            if (!rc && bp->compact) {
+                /* offsets of the 10 state pairs of every member (points m 4 + t, row 0 = psi) */
+                int64_t pstride = 0;
+                int32_t f64 = 0;
+                (void)qgt_plan_dev_V(bp->plan, &pstride, &f64);
+                const int npair = 10 * bp->nmem;
+                int64_t* off = (int64_t*)malloc(sizeof(int64_t) * 2 * (size_t)npair);
+                if (!off) { rc = qgt_set_error(E_NOMEM, "qgt_batch_create: oom"); break; }
+                static const int pi_[10] = {0, 0, 0, 0, 1, 1, 1, 2, 2, 3}, pj_[10] = {0, 1, 2, 3, 1, 2, 3, 2, 3, 3};
+                for (int m = 0; m < bp->nmem; m++)
+                    for (int k = 0; k < 10; k++) {
+                        off[m * 10 + k] = (int64_t)(4 * m + pi_[k]) * pstride;
+                        off[npair + m * 10 + k] = (int64_t)(4 * m + pj_[k]) * pstride;
+                    }
+                const int64_t N = (int64_t)1 << cc->num_qubits;
+                bp->nchunk = qgt_overlap_chunks(N, npair);
+                rc = qgt_dev_malloc((void**)&bp->off_d, sizeof(int64_t) * 2 * (size_t)npair);
+                if (!rc) rc = qgt_dev_memcpy_h2d(bp->off_d, off, sizeof(int64_t) * 2 * (size_t)npair, NULL);
+                if (!rc) rc = qgt_dev_malloc((void**)&bp->part_d, sizeof(double) * 2 * (size_t)npair * bp->nchunk);
+                if (!rc) rc = qgt_dev_malloc((void**)&bp->maps_d, sizeof(double) * (size_t)bp->nmem * b->G * b->G);
+                if (!rc) rc = qgt_dev_stream_sync(NULL);
+                free(off);
+            }
         }
         free(tg);
         free(done);
@@ -278,7 +315,8 @@ int qgt_batch_create(const qgt_circuit_desc_t* circuits, int32_t count, const in
         bp->th_off = b->th_len;
         bp->out_off = b->out_len;
         b->th_len += pts * (size_t)bp->P;
-        b->out_len += pts * 2 * (size_t)bp->Pd * bp->Pd;
+        if (bp->berry && bp->compact) b->out_len += (size_t)bp->nmem * b->G * b->G;   /* the maps */
+        else b->out_len += pts * 2 * (size_t)bp->Pd * bp->Pd;
         qgt_plan_info_t in;
         if (qgt_plan_get_info(bp->plan, &in) == 0) b->device_bytes += in.device_bytes;
     }
@@ -303,9 +341,22 @@ int qgt_batch_create(const qgt_circuit_desc_t* circuits, int32_t count, const in
                 cr = qgt_dev_memcpy_h2d(qgt_plan_dev_theta(bp->plan), b->th_pin + bp->th_off,
                                         sizeof(double) * pts * (size_t)bp->P, st);
             if (!cr) cr = qgt_plan_enqueue_step(bp->plan, st);
-            if (!cr && bp->Pd > 0)
+            if (!cr && bp->berry && bp->compact) {
+                int64_t pstride = 0;
+                int32_t f64 = 0;
+                const void* V = qgt_plan_dev_V(bp->plan, &pstride, &f64);
+                const int npair = 10 * bp->nmem;
+                const int64_t N = (int64_t)1 << circuits[bp->mem[0]].num_qubits;
+                cr = qgt_dev_overlaps(V, f64, N, bp->off_d, bp->off_d + npair, npair, bp->nchunk, bp->part_d, st);
+                if (!cr) cr = qgt_dev_berry_closed(bp->part_d, bp->nchunk, bp->nmem, b->G, bp->maps_d, st);
+                if (!cr)
+                    cr = qgt_dev_memcpy_d2h(b->out_pin + bp->out_off, bp->maps_d,
+                                            sizeof(double) * (size_t)bp->nmem * b->G * b->G, st);
+                b->nodes += 2;
+            } else if (!cr && bp->Pd > 0) {
                 cr = qgt_dev_memcpy_d2h(b->out_pin + bp->out_off, qgt_plan_dev_Q(bp->plan),
                                         sizeof(double) * pts * 2 * (size_t)bp->Pd * bp->Pd, st);
+            }
             b->nodes += qgt_plan_launches(bp->plan) + 2;
         }
         for (int k = 1; k < K && !cr; k++) {
@@ -343,8 +394,8 @@ int qgt_batch_execute_host(qgt_batch_t* b, const double* theta, double* Q, doubl
                 for (int k = 0; k < np; k++)
                     if (bp->perm[k] < bp->P) dst[bp->perm[k]] = th[k];
                 if (bp->compact) {
-                    dst[0] = bp->early_is_a ? step * t : 0.0;
-                    dst[1] = bp->early_is_a ? 0.0 : step * t;
+                    dst[0] = (t & 1) ? M_PI : 0.0;   /* the closed form's four states */
+                    dst[1] = (t & 2) ? M_PI : 0.0;
                 } else {
                     dst[0] = step * (t / b->G);
                     dst[1] = step * (t % b->G);
@@ -372,12 +423,13 @@ int qgt_batch_execute_host(qgt_batch_t* b, const double* theta, double* Q, doubl
             }
             if (!berry) continue;
             double* map = berry + (size_t)c * G * G;
+            if (bp->compact) {   /* maps formed on the device from the closed form */
+                memcpy(map, b->out_pin + bp->out_off + (size_t)m * G * G, sizeof(double) * G * G);
+                continue;
+            }
             /* Omega_ab = Im Q_01 of the 2 x 2 block (imaginary part at double index 3) */
             for (size_t x = 0; x < G; x++)
-                for (size_t y = 0; y < G; y++) {
-                    size_t t = bp->compact ? (bp->early_is_a ? x : y) : x * G + y;
-                    map[x * G + y] = src[t * blk + 3];
-                }
+                for (size_t y = 0; y < G; y++) map[x * G + y] = src[(x * G + y) * blk + 3];
         }
     }
     return 0;

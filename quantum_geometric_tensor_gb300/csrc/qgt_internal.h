@@ -368,6 +368,10 @@ int qgt_dev_overlaps(const void* V, int32_t fp64, int64_t N, const int64_t* a_of
                      int32_t nchunk, double* part, void* stream);
 /* chunks per pair that fill the GPU for n pairs of N amplitudes */
 int32_t qgt_overlap_chunks(int64_t N, int32_t n);
+/* the G x G Berry maps of ncirc circuits from the overlaps of their states at (theta_a, theta_b) in
+ * {0, pi}^2 (part: per circuit 10 pairs x nchunk partial sums, qgt_dev_overlaps layout); maps: ncirc
+ * x G x G doubles (qgt_gram_f64.cu) */
+int qgt_dev_berry_closed(const double* part, int32_t nchunk, int32_t ncirc, int32_t G, double* maps, void* stream);
 /* the device vector buffer of a plan and the amplitudes between its points */
 const void* qgt_plan_dev_V(struct qgt_plan* p, int64_t* point_stride, int32_t* fp64);
 

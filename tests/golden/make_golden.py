@@ -135,6 +135,9 @@ def natgrad_cases():
     Gd[perm, np.arange(P)] = np.logspace(0, -10, P) * np.exp(1j * rng.uniform(0, 2 * np.pi, P))
     gh = rng.standard_normal(P) + 1j * rng.standard_normal(P)
     out.append(("permuted_diagonal_kappa1e10", Gd, gh, (1e-4, 1e8, True, True, 1e-10)))
+    # the same without the permutation: the reference's LU needs no row swap, so its output is right
+    Gdd = np.diag(np.logspace(0, -10, P) * np.exp(1j * rng.uniform(0, 2 * np.pi, P)))
+    out.append(("diagonal_kappa1e10", Gdd, gh, (1e-4, 1e8, True, True, 1e-10)))
     # general (non-Hermitian) complex matrix, well conditioned: LU on G as given
     Gn = np.eye(P) * 3 + (rng.standard_normal((P, P)) + 1j * rng.standard_normal((P, P))) / np.sqrt(P)
     out.append(("nonhermitian", Gn, gh, (1e-4, 1e8, True, True, 1e-10)))
@@ -167,6 +170,13 @@ def natgrad_main():
             print(f"{name}: pinv |x| = {np.linalg.norm(x):.4e}")
             continue
         x, lam, kappa, path = O.regularized_natural_gradient(ref, g32, G32, *cfg)
+        # the reference's LU inverse solves each column with b and x in one buffer, so its row
+        # permutation overwrites entries it still reads (core/matrix_operations.c:145-147, 204):
+        # its inverse is wrong whenever pivoting swaps rows; record how wrong
+        Mr = G32.copy()
+        Mr[np.diag_indices_from(Mr)] += np.float32(lam)
+        okr, invr = ref.matrix_inverse(Mr)
+        arrays[f"{name}__ref_inverse_residual"] = np.float64(np.abs(invr @ Mr - np.eye(len(Mr))).max()) if okr else np.inf
         arrays[f"{name}__cfg"] = np.array([cfg[0], cfg[1], float(cfg[2]), float(cfg[3]), cfg[4]])
         arrays[f"{name}__x"] = x
         arrays[f"{name}__lambda"] = np.float64(lam)

@@ -11,6 +11,10 @@ FP64 numpy solve of the same ComplexFloat input.
 Tolerances: the library computes in FP64 and returns ComplexFloat, so against
 the FP64 solve 1e-6 relative; the reference computes in FP32, so against its
 fixture 1e-3 relative (its LU and inverse-times-gradient rounding).  The
+reference's matrix_inverse solves each column in place over its right-hand
+side, so any row swap of its pivoting corrupts the inverse
+(core/matrix_operations.c:145-147, 204); the fixture records that residual and
+the comparison with the reference's output is made where it is small.  The
 condition number of a matrix whose smallest singular values sit below FP32
 resolution depends on rounding (the circuit QGT with the default
 configuration): there the check is against the FP64 singular values of the
@@ -124,7 +128,10 @@ def test_regularized_natural_gradient(L, case):
     assert rel(x, x64) < 1e-6, rel(x, x64)
     if case != "circuit_qgt_default":   # kappa (and so lambda) of that case is set by FP32 rounding
         assert float(Z[f"{case}__lambda"]) == pytest.approx(float(lam), rel=1e-6)
-        assert rel(x, Z[f"{case}__x"]) < 1e-3, rel(x, Z[f"{case}__x"])
+        # the reference's own LU inverse is only right when no pivot swaps rows (its permutation
+        # runs in place over the right-hand side it reads): compare where its residual is small
+        if path == "pinv" or float(Z[f"{case}__ref_inverse_residual"]) < 1e-4:
+            assert rel(x, Z[f"{case}__x"]) < 1e-3, rel(x, Z[f"{case}__x"])
 
 
 def test_regularized_without_fallback_fails_on_singular(L):
