@@ -113,8 +113,17 @@ typedef struct {
      * the inverse gates; inner products are unchanged by the common unitary,
      * so Q is the same with about half the gate work) */
     int32_t transport;
+    /* register tile of complex64 plans from 14 qubits: 0 = automatic (14 qubits when that saves at
+     * least 8 % of the vector passes, else 13), 13 or 14 */
+    int32_t tile_bits;
+    /* pass kernels of complex64 plans on 13- / 14-qubit tiles: QGT_PASS_AUTO (each pass program
+     * compiled into its own straight-line kernel at plan creation from 16 qubits, the program
+     * interpreter below), QGT_PASS_INTERPRET, QGT_PASS_COMPILED; the environment variable
+     * QGT_PASS_JIT=0 / 1 overrides it */
+    int32_t pass_kernels;
 } qgt_plan_options_t;
 enum { QGT_TRANSPORT_AUTO = 0, QGT_TRANSPORT_FORWARD = 1, QGT_TRANSPORT_MEET = 2 };
+enum { QGT_PASS_AUTO = 0, QGT_PASS_INTERPRET = 1, QGT_PASS_COMPILED = 2 };
 
 typedef struct qgt_plan qgt_plan_t;
 
@@ -208,6 +217,9 @@ typedef struct {
     int32_t berry_grid;         /* G (0 = no maps; default 32) */
     int32_t device;
     int32_t streams;            /* concurrent branches inside the graph (default 4, max 16) */
+    /* autotuning cache (qgt_plan_autotune): each structural group's plan takes the fastest
+     * configuration found for it, timing the groups not in the file yet; NULL = no tuning */
+    const char* tune_cache;
 } qgt_batch_options_t;
 
 typedef struct {
@@ -382,6 +394,18 @@ int qgt_cholesky_solve_f64_noalloc(const double* A, const double* g, double lamb
  * timeout_ns = 0 restore the default (no stall, 4 s limit).  Plans of
  * MIXED precision with more than 8 rows only; no GPU fault is involved. */
 int qgt_plan_test_gram_stall(qgt_plan_t* plan, int stall, int64_t timeout_ns);
+
+/* ---- autotuning --------------------------------------------------------
+ * Times the candidate configurations of a circuit's plan on the GPU (the
+ * register tile, 13 or 14 qubits; interpreted or compiled pass kernels) for
+ * the given base options (precision, batch, derivative parameters,
+ * Hamiltonian), each over `steps` graph launches after two warm-up steps,
+ * and returns the fastest as *tuned (base with tile_bits and pass_kernels
+ * set) and its time per step.  Results are kept in the text file cache_path
+ * (one line per circuit structure and base options; NULL: no file): a circuit
+ * already in the file is not timed again.  No reference counterpart. */
+int qgt_plan_autotune(const qgt_circuit_desc_t* circuit, const qgt_plan_options_t* base, const char* cache_path,
+                      int32_t steps, qgt_plan_options_t* tuned, double* best_ms);
 
 /* Thread-local text of the last error. */
 const char* qgt_last_error(void);

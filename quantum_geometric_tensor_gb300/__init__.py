@@ -20,6 +20,7 @@ I, X, Y, Z, H, S, T, RX, RY, RZ, CNOT, CZ, SWAP = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 
 FP64, MIXED, MIXED_BF16X3 = 0, 1, 2
 HAM_NONE, HAM_TFIM, HAM_PAULI = 0, 1, 2
 TRANSPORT_AUTO, TRANSPORT_FORWARD, TRANSPORT_MEET = 0, 1, 2
+PASS_AUTO, PASS_INTERPRET, PASS_COMPILED = 0, 1, 2
 
 
 class GateDesc(C.Structure):
@@ -35,7 +36,8 @@ class PlanOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("hamiltonian", C.c_int), ("tfim_J", C.c_double), ("tfim_h", C.c_double),
                 ("lambda_", C.c_double), ("device", C.c_int32), ("use_graph", C.c_int32), ("batch", C.c_int32),
                 ("num_deriv_params", C.c_int32), ("num_pauli_terms", C.c_int32), ("pauli_strings", C.c_char_p),
-                ("pauli_coeffs", C.c_void_p), ("transport", C.c_int32)]
+                ("pauli_coeffs", C.c_void_p), ("transport", C.c_int32), ("tile_bits", C.c_int32),
+                ("pass_kernels", C.c_int32)]
 
 
 class PlanInfo(C.Structure):
@@ -48,7 +50,8 @@ class PlanInfo(C.Structure):
 
 
 class BatchOptions(C.Structure):
-    _fields_ = [("precision", C.c_int), ("berry_grid", C.c_int32), ("device", C.c_int32), ("streams", C.c_int32)]
+    _fields_ = [("precision", C.c_int), ("berry_grid", C.c_int32), ("device", C.c_int32), ("streams", C.c_int32),
+                ("tune_cache", C.c_char_p)]
 
 
 class BatchInfo(C.Structure):
@@ -197,7 +200,8 @@ class Plan:
     """A compiled circuit plan (qgt_plan_t)."""
 
     def __init__(self, n, gates, num_params=None, precision=MIXED, hamiltonian=HAM_TFIM, J=1.0, h=1.0,
-                 lam=1e-3, device=0, use_graph=True, batch=1, deriv_params=0, pauli=None, transport=0):
+                 lam=1e-3, device=0, use_graph=True, batch=1, deriv_params=0, pauli=None, transport=0,
+                 tile_bits=0, pass_kernels=0):
         """pauli: [(coeff, "XZIY..."), ...] selects the Pauli-sum Hamiltonian (character n-1-q acts on qubit q)."""
         L = lib()
         self.desc = circuit_desc(n, gates, num_params)
@@ -214,6 +218,7 @@ class Plan:
             o.pauli_coeffs = self._pauli[1].ctypes.data
         o.lambda_, o.device, o.use_graph = lam, device, int(use_graph)
         o.batch, o.num_deriv_params, o.transport = int(batch), int(deriv_params), int(transport)
+        o.tile_bits, o.pass_kernels = int(tile_bits), int(pass_kernels)
         self.opt = o
         h_ = C.c_void_p()
         _check(L.qgt_plan_create(C.byref(self.desc), C.byref(o), C.byref(h_)), "qgt_plan_create")
@@ -304,7 +309,7 @@ class Batch:
     """A ragged batch (qgt_batch_t): circuits = [(n, gates, num_params), ...];
     berry_params = [(a, b), ...] per circuit when grid > 0."""
 
-    def __init__(self, circuits, berry_params=None, precision=MIXED, grid=32, device=0, streams=4):
+    def __init__(self, circuits, berry_params=None, precision=MIXED, grid=32, device=0, streams=4, tune_cache=None):
         L = lib()
         self.descs = [circuit_desc(n, g, P) for (n, g, P) in circuits]
         arr = (CircuitDesc * len(self.descs))(*self.descs)
@@ -313,6 +318,8 @@ class Batch:
         o = BatchOptions()
         L.qgt_batch_default_options(C.byref(o))
         o.precision, o.berry_grid, o.device, o.streams = precision, int(grid), device, int(streams)
+        self._tune = None if tune_cache is None else str(tune_cache).encode()
+        o.tune_cache = self._tune
         self.G = int(grid)
         bp = None
         if grid > 0:
@@ -540,3 +547,21 @@ def berry_phase(states):
     finally:
         L.diffgeo_engine_destroy(e)
     return complex(r.real, r.imag)
+
+
+def autotune(n, gates, num_params=None, precision=MIXED, hamiltonian=HAM_TFIM, batch=1, deriv_params=0, lam=1e-3,
+             device=0, cache=None, steps=5):
+    """qgt_plan_autotune -> (tile_bits, pass_kernels, ms per step) of the fastest configuration."""
+    L = lib()
+    L.qgt_plan_autotune.argtypes = [C.POINTER(CircuitDesc), C.POINTER(PlanOptions), C.c_char_p, C.c_int32,
+                                    C.POINTER(PlanOptions), C.POINTER(C.c_double)]
+    d = circuit_desc(n, gates, num_params)
+    o = PlanOptions()
+    L.qgt_plan_default_options(C.byref(o))
+    o.precision, o.hamiltonian, o.batch, o.num_deriv_params = precision, hamiltonian, int(batch), int(deriv_params)
+    o.lambda_, o.device = lam, device
+    t = PlanOptions()
+    ms = C.c_double()
+    _check(L.qgt_plan_autotune(C.byref(d), C.byref(o), None if cache is None else str(cache).encode(), int(steps),
+                               C.byref(t), C.byref(ms)), "qgt_plan_autotune")
+    return int(t.tile_bits), int(t.pass_kernels), float(ms.value)

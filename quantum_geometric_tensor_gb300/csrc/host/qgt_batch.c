@@ -124,6 +124,14 @@ static int make_plan(const qgt_circuit_desc_t* c, const qgt_batch_options_t* bo,
     o.use_graph = 0;
     o.batch = batch;
     o.num_deriv_params = Pd;
+    if (bo->tune_cache) {
+        /* the fastest measured configuration of this group's plan (timed once, then read from the cache) */
+        qgt_plan_options_t t;
+        int rc = qgt_plan_autotune(c, &o, bo->tune_cache, 3, &t, NULL);
+        if (rc) return rc;
+        o.tile_bits = t.tile_bits;
+        o.pass_kernels = t.pass_kernels;
+    }
     return qgt_plan_create(c, &o, out);
 }
 

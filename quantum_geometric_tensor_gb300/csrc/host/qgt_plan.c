@@ -437,6 +437,8 @@ static int choose_tile(qgt_plan_t* p)
 {
     p->wide = 0;
     if (p->fp64 || p->n < QGT_TILE_WIDE_F32) return 0;
+    if (p->opt.tile_bits == QGT_TILE_MAX_F32) return 0;
+    if (p->opt.tile_bits == QGT_TILE_WIDE_F32) { p->wide = 1; return 0; }
     int64_t vp[2];
     for (int w = 1; w >= 0; w--) {
         p->wide = w;
@@ -1263,6 +1265,8 @@ static int jit_wanted(const qgt_plan_t* p)
     if (p->fp64 || p->opt.precision != QGT_PRECISION_MIXED) return 0;
     if (env && env[0] == '0') return 0;
     if (env && env[0] == '1') return 1;
+    if (p->opt.pass_kernels == QGT_PASS_INTERPRET) return 0;
+    if (p->opt.pass_kernels == QGT_PASS_COMPILED) return 1;
     return p->n >= 16;
 }
 
@@ -1401,6 +1405,12 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
         return qgt_set_error(E_INVAL, "qgt_plan_create: unknown precision %d", bad);
     }
     if (!(p->opt.lambda >= 0) || !isfinite(p->opt.lambda)) { free(p); return qgt_set_error(E_INVAL, "lambda must be >= 0"); }
+    if ((p->opt.tile_bits != 0 && p->opt.tile_bits != QGT_TILE_MAX_F32 && p->opt.tile_bits != QGT_TILE_WIDE_F32) ||
+        p->opt.pass_kernels < QGT_PASS_AUTO || p->opt.pass_kernels > QGT_PASS_COMPILED) {
+        int tb = p->opt.tile_bits, pk = p->opt.pass_kernels;
+        free(p);
+        return qgt_set_error(E_INVAL, "qgt_plan_create: tile_bits %d (0, 13, 14) / pass_kernels %d (0 .. 2)", tb, pk);
+    }
     if (p->opt.hamiltonian < QGT_HAMILTONIAN_NONE || p->opt.hamiltonian > QGT_HAMILTONIAN_PAULI) {
         int bad = (int)p->opt.hamiltonian;
         free(p);
