@@ -5,7 +5,7 @@ QGT_PASS_JIT=1 compiles the passes of every complex64 plan on 13- or 14-qubit
 register tiles, QGT_PASS_JIT=0 keeps them on the interpreter.  The compiled
 kernels apply real gates as m0 x + m2 y (the interpreter uses the one-multiply
 tangent forms), so the two agree to FP32 rounding, not bit for bit:
-tolerance 1e-6 relative on Q and gradient, 1e-7 absolute on the energy, 5e-5 on
+tolerance 1e-6 relative on Q and gradient, 1e-6 absolute on the energy, 5e-5 on
 the natural-gradient step (the solve amplifies differences by the condition
 number of Re Q + 1e-3 I); against FP64 the mixed-precision tolerances (metric
 1e-6, Q and gradient 2e-6)."""
@@ -49,7 +49,7 @@ def test_compiled_passes_match_interpreter(Q, monkeypatch, n, L, ent):
     for k in ("Q", "grad"):
         assert rel(out[k], ref[k]) < 1e-6, k
     assert rel(out["natgrad"], ref["natgrad"]) < 5e-5
-    assert abs(out["energy"] - ref["energy"]) < 1e-7
+    assert abs(out["energy"] - ref["energy"]) < 1e-6
     monkeypatch.setenv("QGT_PASS_JIT", "0")
     with Q.Plan(n, gates, P, precision=Q.FP64) as p64:
         r64 = p64.run(theta)
