@@ -298,11 +298,16 @@ def run_gb300(args, ws, rank, local):
     if os.path.exists(tp):
         try:
             tj = json.load(open(tp))
-            traffic = tj.get(dom) if tj.get("workload") == workload else None   # measured for this workload only
+            # measured for this workload and this build of the pass kernels only
+            kinds = "compiled" if info.jit_passes > 0 else "interpreted"
+            if tj.get("workload") == workload and (dom != "passes" or tj.get("passes_kernels") == kinds):
+                traffic = tj.get(dom)
         except Exception:
             traffic = None
     if dom == "passes":
-        roof = {"bound": "hbm", "kernel": "pass2_kernel (all register-tile passes of a step)", "achieved": gate_gbs,
+        kname = ("qgt_passK_run / qgt_passK_ckpt (compiled pass kernels)" if info.jit_passes > 0
+                 else "pass2_kernel (interpreted pass programs)")
+        roof = {"bound": "hbm", "kernel": kname + ": all register-tile passes of a step", "achieved": gate_gbs,
                 "peak": hbm, "unit": "GB/s", "frac": gate_gbs / hbm, "traffic": traffic,
                 "peak_source": peak_src, "algorithmic_bytes": info.gate_bytes, "ms": prof.passes_ms}
     else:
@@ -392,9 +397,19 @@ def run_ragged(args):
     ns, Ls = rng.integers(12, 19, 1024), rng.integers(2, 7, 1024)
     spec = [(int(n), Q.ansatz_gates(int(n), int(L), "cnot"), 2 * int(n) * int(L)) for n, L in zip(ns, Ls)]
     thetas = [O.splitmix64_params(5000 + c, s_[2]) for c, s_ in enumerate(spec)]
+    tune = args.tune_cache or None
+    tuned_before = 0
+    if tune and os.path.exists(tune):
+        tuned_before = sum(1 for x in open(tune) if x.strip() and not x.startswith("#"))
     t0 = time.perf_counter()
-    b = Q.Batch(spec, [(0, s_[0]) for s_ in spec], precision=Q.MIXED, grid=32)
+    b = Q.Batch(spec, [(0, s_[0]) for s_ in spec], precision=Q.MIXED, grid=32, tune_cache=tune)
     t_create = time.perf_counter() - t0
+    tuning = None
+    if tune:
+        lines = [x.split() for x in open(tune) if x.strip() and not x.startswith("#")]
+        tuning = {"cache": tune, "entries_before": tuned_before, "entries": len(lines),
+                  "choices": sorted({f"tile{x[1]}/{'compiled' if x[2] == '2' else 'interpreted' if x[2] == '1' else 'default'}"
+                                     for x in lines if len(x) >= 3})}
     info = b.info()
     for _ in range(args.warmup):
         Qs, maps = b.run(thetas)
@@ -413,13 +428,14 @@ def run_ragged(args):
     _line("QGTs/sec (ragged batch of 1024 circuits, 12-18 qubits, each with a 32x32 Berry map)", 1024000.0 / ms,
           "QGTs/sec", args.steps, args.warmup, ms,
           {"workload": "ragged1024_q12-18_L2-6_cnot_berry32", "circuits": 1024, "groups": info.num_groups,
-           "berry_plans": info.num_berry_plans, "precision": "mixed"},
+           "berry_plans": info.num_berry_plans, "precision": "mixed",
+           "plan_configuration": "measured per group (tune cache)" if tune else "defaults"},
           {"dtype": "c64/fp16-digits/f64", "e2e": {"value": 1024000.0 / ms, "unit": "QGTs/sec",
                                                     "h2d_bytes_per_step": int(sum(len(t) for t in thetas) * 8),
                                                     "d2h_bytes_per_step": int(sum(s_[2] ** 2 * 16 for s_ in spec)
                                                                               + 1024 * 32 * 32 * 8)},
            "graph_kernels": info.graph_kernels, "device_gb": info.device_bytes / 1e9, "create_s": t_create,
-           "metric_rel_err_vs_fp64": errs, "clocks": clk.summary()})
+           "metric_rel_err_vs_fp64": errs, "tuning": tuning, "clocks": clk.summary()})
 
 
 def run_hea26(args):
@@ -506,6 +522,14 @@ def run_learned(args):
     for v in vqe.values():
         v.pop("E")
     ratio = float(np.mean(its["cg"]) / np.mean(its["learned"]))
+    # what any diag + rank-16 preconditioner of this form can gain at these points, and whether the
+    # training set pins down the part that gains (exact metrics of the held-out points, their
+    # nearest training points, random points and perturbed points)
+    from quantum_geometric_tensor_gb300 import precond_limits as PL
+    t0 = time.perf_counter()
+    limits = PL.analyse(lambda t_: Q.metric_dataset(n, g, t_, precision=Q.MIXED), th, th_h, lam=1e-3, r=16,
+                        learned=(d, U))
+    limits["seconds"] = time.perf_counter() - t0
     pc.close()
     _line("PCG iteration reduction, learned vs unpreconditioned (16q, P=192, held-out points)", ratio, "x",
           1, 0, 0.0,
@@ -513,7 +537,7 @@ def run_learned(args):
           {"dtype": "bf16-weights/f32-acc; f64 PCG",
            "heldout_pcg_iters_mean": {k: float(np.mean(v)) for k, v in its.items()},
            "train_s": t_train, "loss_first": float(hist[0]), "loss_last": float(hist[-1]),
-           "vqe_500": vqe, "vqe_max_abs_dE_learned_vs_cholesky": dE})
+           "vqe_500": vqe, "vqe_max_abs_dE_learned_vs_cholesky": dE, "limits": limits})
 
 
 def C_byref(x):
@@ -534,6 +558,9 @@ def main():
     ap.add_argument("--workload", default="hea20", choices=["hea20", "ragged1024", "hea26", "learned16"],
                     help="hea20: the headline step; the others reproduce the batch, 26-qubit and "
                          "learned-preconditioner measurements")
+    ap.add_argument("--tune-cache", default="",
+                    help="ragged1024: measure each structural group's plan configuration and keep the "
+                         "choices in this text file (qgt_batch_options_t.tune_cache)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":

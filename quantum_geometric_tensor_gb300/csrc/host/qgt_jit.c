@@ -143,19 +143,64 @@ static void emit_spawn(sbuf_t* b, const qgt_dev_op2_t* o)
     }
 }
 
-/* a single-qubit gate: real matrices (RY, H, X) as m0 x + m2 y / m4 x + m6 y, complex ones in full */
-static void emit_u(sbuf_t* b, const qgt_dev_op2_t* o)
+/* a derivative spawned at a rotation: the spawned vector applies (-i/2) G R in place of R (G
+ * commutes with R), so the generator is folded into the gate's coefficients by the one entry whose
+ * spawn op this is, a uniform branch on scalars; the other vectors apply R.  Real gates fold only
+ * Y (the product stays real); the caller applies other generators after the gate. */
+static int folds_spawn(const qgt_dev_op2_t* o)
+{
+    if (o->gen == QGEN_NONE || o->coef < 0) return 0;
+    if (o->kind == Q2_UR) return o->gen == QGEN_Y;
+    return o->kind == Q2_U;
+}
+
+static void emit_fold(sbuf_t* b, const qgt_dev_op2_t* o, int pc)
+{
+    /* m = [m00, m01, m10, m11] complex as (re, im) pairs; rows of (-i/2) G times M */
+    if (o->gen == QGEN_Y)   /* [[0, -1/2], [1/2, 0]] M */
+        sb_printf(b, "\n      if (spawn == %d) { R t_[8]; for (int i = 0; i < 4; i++) { t_[i] = -0.5f * m[4 + i]; "
+                     "t_[4 + i] = 0.5f * m[i]; } for (int i = 0; i < 8; i++) m[i] = t_[i]; }", pc);
+    else if (o->gen == QGEN_X)   /* [[0, -i/2], [-i/2, 0]] M: -i/2 (a + ib) = b/2 - i a/2 */
+        sb_printf(b, "\n      if (spawn == %d) { R t_[8]; for (int i = 0; i < 2; i++) { "
+                     "t_[2 * i] = 0.5f * m[5 + 2 * i]; t_[2 * i + 1] = -0.5f * m[4 + 2 * i]; "
+                     "t_[4 + 2 * i] = 0.5f * m[1 + 2 * i]; t_[5 + 2 * i] = -0.5f * m[2 * i]; } "
+                     "for (int i = 0; i < 8; i++) m[i] = t_[i]; }", pc);
+    else   /* Z: diag(-i/2, i/2) M */
+        sb_printf(b, "\n      if (spawn == %d) { R t_[8]; for (int i = 0; i < 2; i++) { "
+                     "t_[2 * i] = 0.5f * m[1 + 2 * i]; t_[2 * i + 1] = -0.5f * m[2 * i]; "
+                     "t_[4 + 2 * i] = -0.5f * m[5 + 2 * i]; t_[5 + 2 * i] = 0.5f * m[4 + 2 * i]; } "
+                     "for (int i = 0; i < 8; i++) m[i] = t_[i]; }", pc);
+}
+
+/* a single-qubit gate.  Real matrices (RY, H, X): RY's coefficients are stored in tangent form
+ * [[1, -t], [t, 1]] or cotangent form [[k, -g], [g, k]] (g = +-1), which one depends on the angle
+ * and is the same for every thread, so a register-bit gate branches (uniformly) to a path of one
+ * multiply-add per component for either form and a lane-bit gate to one for the tangent form;
+ * other real matrices (and the entry that carries the pass renormalisation) take m0 x + m2 y /
+ * m4 x + m6 y.  Complex matrices in full.  pc: the op's program index (its spawn number). */
+static void emit_u(sbuf_t* b, const qgt_dev_op2_t* o, int pc)
 {
     if (o->coef < 0) return;   /* identity */
     const int real = o->kind == Q2_UR;
     sb_printf(b, "    { ");
     load_coef(b, o->coef);
-    if (o->ra >= RL_REG_) {
-        sb_printf(b, " u_reg<%d, NR, %s, T, R>(v, m); }\n", o->ra - RL_REG_, real ? "true" : "false");
+    if (folds_spawn(o)) emit_fold(b, o, pc);
+    if (o->ra >= RL_REG_ && real) {
+        const int ri = o->ra - RL_REG_;
+        sb_printf(b, "\n      if (m[0] == 1.f && m[6] == 1.f) tan_reg<%d, NR, T, R>(v, m[2], m[4]);\n"
+                     "      else if (m[4] == 1.f && m[2] == -1.f) cot_reg<%d, NR, 1, T, R>(v, m[0], m[6]);\n"
+                     "      else if (m[4] == -1.f && m[2] == 1.f) cot_reg<%d, NR, -1, T, R>(v, m[0], m[6]);\n"
+                     "      else u_reg<%d, NR, true, T, R>(v, m); }\n", ri, ri, ri, ri);
+    } else if (o->ra >= RL_REG_) {
+        sb_printf(b, " u_reg<%d, NR, false, T, R>(v, m); }\n", o->ra - RL_REG_);
     } else if (real) {
-        sb_printf(b, " const int hi = (lane >> %d) & 1; const R cs0 = hi ? m[6] : m[0], cp0 = hi ? m[4] : m[2];\n"
-                     "#pragma unroll\n      for (int j = 0; j < NR; j++) { const T w = shfl_x<T>(v[j], %d); "
-                     "v[j] = rmad2<T, R>(cs0, v[j], cp0, w); } }\n", o->ra, 1 << o->ra);
+        sb_printf(b, " const int hi = (lane >> %d) & 1;\n"
+                     "      if (m[0] == 1.f && m[6] == 1.f) { const R cp0 = hi ? m[4] : m[2];\n"
+                     "#pragma unroll\n        for (int j = 0; j < NR; j++) { const T w = shfl_x<T>(v[j], %d); "
+                     "v[j] = fma_s<T, R>(cp0, w, v[j]); }\n"
+                     "      } else { const R cs0 = hi ? m[6] : m[0], cp0 = hi ? m[4] : m[2];\n"
+                     "#pragma unroll\n        for (int j = 0; j < NR; j++) { const T w = shfl_x<T>(v[j], %d); "
+                     "v[j] = rmad2<T, R>(cs0, v[j], cp0, w); } } }\n", o->ra, 1 << o->ra, 1 << o->ra);
     } else {
         sb_printf(b, " const int hi = (lane >> %d) & 1; const R mm[4] = {hi ? m[6] : m[0], hi ? m[7] : m[1], "
                      "hi ? m[4] : m[2], hi ? m[5] : m[3]};\n#pragma unroll\n      for (int j = 0; j < NR; j++) { "
@@ -309,21 +354,22 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
             const int cnt = o->seg, nl = o->ra;
             const unsigned rmask = o->rb;
             sb_printf(b, "    // op %d: block of %d commuting gates\n", pc, cnt);
-            for (int u = pc + 1; u <= pc + nl; u++) emit_u(b, &d->prog[u]);
+            for (int u = pc + 1; u <= pc + nl; u++) emit_u(b, &d->prog[u], u);
             int at = pc + 1 + nl;
             for (int i = 0; i < RB; i++)
                 if ((rmask >> i) & 1u) {
                     qgt_dev_op2_t x = d->prog[at];
                     x.ra = (uint8_t)(RL_REG_ + i);   /* the block's i-th register op acts on register bit i */
-                    emit_u(b, &x);
+                    emit_u(b, &x, at);
                     at++;
                 }
+            /* generators not folded into a gate: applied after the block (they commute with it) */
             int ng = 0;
-            for (int u = pc + 1; u <= pc + cnt; u++) ng += d->prog[u].gen != 0;
+            for (int u = pc + 1; u <= pc + cnt; u++) ng += d->prog[u].gen != 0 && !folds_spawn(&d->prog[u]);
             if (ng) {
                 sb_printf(b, "    switch (spawn) {\n");
                 for (int u = pc + 1; u <= pc + cnt; u++)
-                    if (d->prog[u].gen != 0) {
+                    if (d->prog[u].gen != 0 && !folds_spawn(&d->prog[u])) {
                         sb_printf(b, "    case %d: ", u);
                         emit_spawn(b, &d->prog[u]);
                         sb_printf(b, " break;\n");
@@ -336,7 +382,7 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
         switch (o->kind) {
         case Q2_U:
         case Q2_UR:
-            emit_u(b, o);
+            emit_u(b, o, pc);
             break;
         case Q2_PHASE:
             if (o->coef < 0) break;
@@ -372,7 +418,7 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
             qgt_set_error(-1, "jit: op kind %d at %d not expected outside a block", (int)o->kind, pc);
             return NULL;
         }
-        if (o->gen != 0 && (o->kind == Q2_U || o->kind == Q2_UR || o->kind == Q2_PHASE)) {
+        if (o->gen != 0 && (o->kind == Q2_U || o->kind == Q2_UR || o->kind == Q2_PHASE) && !folds_spawn(o)) {
             sb_printf(b, "    if (spawn == %d) { ", pc);
             emit_spawn(b, o);
             sb_printf(b, " }\n");

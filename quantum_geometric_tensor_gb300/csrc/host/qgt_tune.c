@@ -80,7 +80,7 @@ static void cache_store(const char* path, uint64_t key, int tile, int kern, doub
     if (!path) return;
     FILE* f = fopen(path, "a");
     if (!f) return;
-    fprintf(f, "%016llx %d %d %.6f\n", (unsigned long long)key, tile, kern, ms);
+    fprintf(f, "%016llx %d %d %.9g\n", (unsigned long long)key, tile, kern, ms);
     fclose(f);
 }
 

@@ -34,7 +34,7 @@ def test_autotune_picks_and_caches(Q, tmp_path):
     assert tile in (13, 14) and kern in (Q.PASS_INTERPRET, Q.PASS_COMPILED) and ms > 0
     lines = [x for x in cache.read_text().splitlines() if x and not x.startswith("#")]
     assert len(lines) == 1
-    assert Q.autotune(n, gates, P, cache=cache, steps=3) == (tile, kern, pytest.approx(ms))
+    assert Q.autotune(n, gates, P, cache=cache, steps=3) == (tile, kern, pytest.approx(ms, rel=1e-6, abs=1e-6))
     assert len([x for x in cache.read_text().splitlines() if x]) == 1   # read back, not timed again
     theta = O.splitmix64_params(81, P)
     with Q.Plan(n, gates, P, precision=Q.FP64) as p64:

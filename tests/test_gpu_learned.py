@@ -165,6 +165,31 @@ def test_training_cuts_pcg_iterations(Q):
     L.qgt_precond_destroy(h)
 
 
+def test_limits_of_the_diag_rank_r_form(Q):
+    """What diag + rank-r preconditioners of the metric gain on held-out points of a 10-qubit,
+    3-layer circuit (P = 60, r = 8), with exact GPU metrics: the deflation form built from the
+    point's own smallest eigenvectors cuts CG iterations by at least 1.5x, but the same form
+    built from the nearest of 3000 training points gains nothing (its eigenspace overlaps the
+    held-out one no more than a random point's does), while a point 0.1 rad away still gives
+    nearly the same subspace: the map from theta to the useful subspace changes on a scale far
+    below the spacing of any training set in 60 dimensions."""
+    from quantum_geometric_tensor_gb300 import precond_limits as PL
+    n, layers, r = 10, 3, 8
+    P = 2 * n * layers
+    gates = Q.ansatz_gates(n, layers, "cnot")
+    rng = np.random.default_rng(4)
+    tr = rng.uniform(0, 2 * np.pi, (3000, P))
+    ho = rng.uniform(0, 2 * np.pi, (12, P))
+    res = PL.analyse(lambda t: Q.metric_dataset(n, gates, t, precision=Q.FP64), tr, ho, r=r, rhos=(0.1, 1.0))
+    red, ov = res["reduction_vs_cg"], res["overlap"]
+    print(res["iterations"], ov, res["distance"])
+    assert red["deflation"] >= 1.5
+    assert red["deflation_nn"] <= 1.1
+    assert ov["nn"] <= ov["random"] + 0.1
+    assert ov["at_0.1"] >= 0.9 and red["deflation_at_0.1"] >= 0.9 * red["deflation"]
+    assert res["distance"]["nearest_train"] >= 0.7 * res["distance"]["random_point"]
+
+
 def oracle_vqe(orc, n, gates, th0, steps, eta, lam):
     th = th0.copy()
     E = []
