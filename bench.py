@@ -519,6 +519,8 @@ def run_learned(args):
         vqe[name] = {"E_first": float(E[0]), "E_last": float(E[-1]), "s": time.perf_counter() - t0,
                      "pcg_iters_mean": float(it.mean()), "E": E}
     dE = float(np.abs(vqe["learned"]["E"] - vqe["cholesky"]["E"]).max())
+    dE_cg = float(np.abs(vqe["cg"]["E"] - vqe["cholesky"]["E"]).max())
+    dE_final = {k: float(abs(vqe[k]["E"][-1] - vqe["cholesky"]["E"][-1])) for k in ("cg", "learned")}
     for v in vqe.values():
         v.pop("E")
     ratio = float(np.mean(its["cg"]) / np.mean(its["learned"]))
@@ -537,7 +539,8 @@ def run_learned(args):
           {"dtype": "bf16-weights/f32-acc; f64 PCG",
            "heldout_pcg_iters_mean": {k: float(np.mean(v)) for k, v in its.items()},
            "train_s": t_train, "loss_first": float(hist[0]), "loss_last": float(hist[-1]),
-           "vqe_500": vqe, "vqe_max_abs_dE_learned_vs_cholesky": dE, "limits": limits})
+           "vqe_500": vqe, "vqe_max_abs_dE_learned_vs_cholesky": dE, "vqe_max_abs_dE_cg_vs_cholesky": dE_cg,
+           "vqe_final_abs_dE_vs_cholesky": dE_final, "limits": limits})
 
 
 def C_byref(x):
