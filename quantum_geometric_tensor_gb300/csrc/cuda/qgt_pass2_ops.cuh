@@ -277,6 +277,31 @@ __device__ __forceinline__ void gate_lane(T* v, const R* m, bool real, int b, in
     }
 }
 
+// m (2x2 complex, row-major (re, im) pairs) <- (-i/2) G m for the generator G of a rotation: the
+// coefficients of a gate whose derivative vector is spawned there (G commutes with the rotation)
+__device__ __forceinline__ void fold_gen(float* m, int gen)
+{
+    float t[8];
+    if (gen == QGEN_Y) {   // (-i/2) Y = [[0, -1/2], [1/2, 0]]
+        for (int i = 0; i < 4; i++) { t[i] = -0.5f * m[4 + i]; t[4 + i] = 0.5f * m[i]; }
+    } else if (gen == QGEN_X) {   // (-i/2) X = [[0, -i/2], [-i/2, 0]]; -i/2 (a + ib) = b/2 - i a/2
+        for (int i = 0; i < 2; i++) {
+            t[2 * i] = 0.5f * m[5 + 2 * i];
+            t[2 * i + 1] = -0.5f * m[4 + 2 * i];
+            t[4 + 2 * i] = 0.5f * m[1 + 2 * i];
+            t[5 + 2 * i] = -0.5f * m[2 * i];
+        }
+    } else {   // (-i/2) Z = diag(-i/2, i/2)
+        for (int i = 0; i < 2; i++) {
+            t[2 * i] = 0.5f * m[1 + 2 * i];
+            t[2 * i + 1] = -0.5f * m[2 * i];
+            t[4 + 2 * i] = -0.5f * m[5 + 2 * i];
+            t[5 + 2 * i] = 0.5f * m[4 + 2 * i];
+        }
+    }
+    for (int i = 0; i < 8; i++) m[i] = t[i];
+}
+
 // bit value of a non-register role for this thread
 __device__ __forceinline__ int role_bit(int role, int q, int lane, int warp, uint64_t base)
 {

@@ -64,11 +64,42 @@ static void role_bit_expr(sbuf_t* b, int role, int q)
     else sb_printf(b, "(int)((base >> %d) & 1ull)", q);
 }
 
-/* coefficient entry c into R m[8] (identity for c < 0) */
-static void load_coef(sbuf_t* b, int c)
+/* The coefficient entries a pass reads, one shared-memory slot per op that reads one: the kernel
+ * copies them from the point's coefficient table into shared memory once per CTA (coalesced), and
+ * the ops read their 8 floats from there (a broadcast load) instead of from global memory just
+ * before use.  A slot may carry a spawn fold (see folds_spawn). */
+typedef struct {
+    int n, cap;
+    int* coef;      /* global coefficient index of the slot */
+    int* pc;        /* program index of the op (its spawn number) */
+    int8_t* gen;    /* generator folded into the slot for the entry spawned at pc (QGEN_NONE: none) */
+    int err;
+} slots_t;
+
+static int add_slot(slots_t* t, int coef, int pc, int gen)
+{
+    if (t->n == t->cap) {
+        int nc = t->cap ? 2 * t->cap : 64;
+        int* c = (int*)realloc(t->coef, sizeof(int) * nc);
+        if (c) t->coef = c;
+        int* q = (int*)realloc(t->pc, sizeof(int) * nc);
+        if (q) t->pc = q;
+        int8_t* g = (int8_t*)realloc(t->gen, (size_t)nc);
+        if (g) t->gen = g;
+        if (!c || !q || !g) { t->err = 1; return 0; }
+        t->cap = nc;
+    }
+    t->coef[t->n] = coef;
+    t->pc[t->n] = pc;
+    t->gen[t->n] = (int8_t)gen;
+    return t->n++;
+}
+
+/* coefficient entry c into R m[8] (identity for c < 0); fold_gen: spawn fold of this op */
+static void load_coef(sbuf_t* b, slots_t* t, int c, int pc, int fold_gen)
 {
     if (c < 0) sb_printf(b, "R m[8] = {1.f, 0.f, 0.f, 0.f, 0.f, 0.f, 1.f, 0.f};");
-    else sb_printf(b, "R m[8]; LD8(m, %d);", c);
+    else sb_printf(b, "R m[8]; LDS8(m, %d);", add_slot(t, c, pc, fold_gen));
 }
 
 /* layout of program layout index seg: lthr / pthr and the constant per-register offsets */
@@ -144,32 +175,15 @@ static void emit_spawn(sbuf_t* b, const qgt_dev_op2_t* o)
 }
 
 /* a derivative spawned at a rotation: the spawned vector applies (-i/2) G R in place of R (G
- * commutes with R), so the generator is folded into the gate's coefficients by the one entry whose
- * spawn op this is, a uniform branch on scalars; the other vectors apply R.  Real gates fold only
- * Y (the product stays real); the caller applies other generators after the gate. */
+ * commutes with R), so the generator is folded into the gate's coefficients in the shared-memory
+ * copy of the one CTA whose entry spawns there (fold_gen of qgt_pass2_ops.cuh, at staging); the
+ * other CTAs apply R.  Real gates fold only Y (the product stays real); the caller applies other
+ * generators after the gate. */
 static int folds_spawn(const qgt_dev_op2_t* o)
 {
     if (o->gen == QGEN_NONE || o->coef < 0) return 0;
     if (o->kind == Q2_UR) return o->gen == QGEN_Y;
     return o->kind == Q2_U;
-}
-
-static void emit_fold(sbuf_t* b, const qgt_dev_op2_t* o, int pc)
-{
-    /* m = [m00, m01, m10, m11] complex as (re, im) pairs; rows of (-i/2) G times M */
-    if (o->gen == QGEN_Y)   /* [[0, -1/2], [1/2, 0]] M */
-        sb_printf(b, "\n      if (spawn == %d) { R t_[8]; for (int i = 0; i < 4; i++) { t_[i] = -0.5f * m[4 + i]; "
-                     "t_[4 + i] = 0.5f * m[i]; } for (int i = 0; i < 8; i++) m[i] = t_[i]; }", pc);
-    else if (o->gen == QGEN_X)   /* [[0, -i/2], [-i/2, 0]] M: -i/2 (a + ib) = b/2 - i a/2 */
-        sb_printf(b, "\n      if (spawn == %d) { R t_[8]; for (int i = 0; i < 2; i++) { "
-                     "t_[2 * i] = 0.5f * m[5 + 2 * i]; t_[2 * i + 1] = -0.5f * m[4 + 2 * i]; "
-                     "t_[4 + 2 * i] = 0.5f * m[1 + 2 * i]; t_[5 + 2 * i] = -0.5f * m[2 * i]; } "
-                     "for (int i = 0; i < 8; i++) m[i] = t_[i]; }", pc);
-    else   /* Z: diag(-i/2, i/2) M */
-        sb_printf(b, "\n      if (spawn == %d) { R t_[8]; for (int i = 0; i < 2; i++) { "
-                     "t_[2 * i] = 0.5f * m[1 + 2 * i]; t_[2 * i + 1] = -0.5f * m[2 * i]; "
-                     "t_[4 + 2 * i] = -0.5f * m[5 + 2 * i]; t_[5 + 2 * i] = 0.5f * m[4 + 2 * i]; } "
-                     "for (int i = 0; i < 8; i++) m[i] = t_[i]; }", pc);
 }
 
 /* a single-qubit gate.  Real matrices (RY, H, X): RY's coefficients are stored in tangent form
@@ -178,13 +192,12 @@ static void emit_fold(sbuf_t* b, const qgt_dev_op2_t* o, int pc)
  * multiply-add per component for either form and a lane-bit gate to one for the tangent form;
  * other real matrices (and the entry that carries the pass renormalisation) take m0 x + m2 y /
  * m4 x + m6 y.  Complex matrices in full.  pc: the op's program index (its spawn number). */
-static void emit_u(sbuf_t* b, const qgt_dev_op2_t* o, int pc)
+static void emit_u(sbuf_t* b, slots_t* t, const qgt_dev_op2_t* o, int pc)
 {
     if (o->coef < 0) return;   /* identity */
     const int real = o->kind == Q2_UR;
     sb_printf(b, "    { ");
-    load_coef(b, o->coef);
-    if (folds_spawn(o)) emit_fold(b, o, pc);
+    load_coef(b, t, o->coef, pc, folds_spawn(o) ? o->gen : QGEN_NONE);
     if (o->ra >= RL_REG_ && real) {
         const int ri = o->ra - RL_REG_;
         sb_printf(b, "\n      if (m[0] == 1.f && m[6] == 1.f) tan_reg<%d, NR, T, R>(v, m[2], m[4]);\n"
@@ -215,18 +228,28 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
         qgt_set_error(-1, "jit: unsupported program (RB %d, WB %d)", RB, WB);
         return NULL;
     }
-    sbuf_t sb = {NULL, 0, 0, 0};
-    sbuf_t* b = &sb;
-    sb.cap = 1 << 16;
-    sb.s = (char*)malloc(sb.cap);
-    if (!sb.s) return NULL;
-    sb.s[0] = 0;
+    /* three parts: the kernel's head (hb), its body (bb: entry points, program, store), and, once the
+     * body has registered its coefficient slots, the slot table and the staging code between them */
+    sbuf_t hsb = {NULL, 0, 0, 0}, bsb = {NULL, 0, 0, 0}, osb = {NULL, 0, 0, 0};
+    slots_t slots = {0, 0, NULL, NULL, NULL, 0};
+    slots_t* t = &slots;
+    hsb.cap = 1 << 14;
+    bsb.cap = 1 << 16;
+    osb.cap = 1 << 16;
+    hsb.s = (char*)malloc(hsb.cap);
+    bsb.s = (char*)malloc(bsb.cap);
+    osb.s = (char*)malloc(osb.cap);
+    if (!hsb.s || !bsb.s || !osb.s) {
+        free(hsb.s);
+        free(bsb.s);
+        free(osb.s);
+        return NULL;
+    }
+    hsb.s[0] = bsb.s[0] = osb.s[0] = 0;
+    sbuf_t* b = &hsb;
     const int nthreads = 32 << WB;
     const int minb = WB >= 4 ? 1 : (RB == 4 ? 3 : 2);
     const int es = (int)(sizeof(qgt_dev_entry_t) / 4);
-    sb_printf(b, "#define LD8(m, c) { const float4 a_ = __ldg(reinterpret_cast<const float4*>(ct + 8 * (c))); "
-                 "const float4 b_ = __ldg(reinterpret_cast<const float4*>(ct + 8 * (c) + 4)); "
-                 "m[0] = a_.x; m[1] = a_.y; m[2] = a_.z; m[3] = a_.w; m[4] = b_.x; m[5] = b_.y; m[6] = b_.z; m[7] = b_.w; }\n");
     sb_printf(b, "extern \"C\" __global__ void __launch_bounds__(%d, %d) %s(float2* __restrict__ V, long long N, "
                  "const int* __restrict__ ents, const float* __restrict__ coef32, unsigned* __restrict__ rowmax, "
                  "int coef_stride, long long point_stride, int rowmax_stride)\n{\n",
@@ -257,6 +280,7 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
             sb_printf(b, " if ((threadIdx.x >> %d) & 1) o |= %uu;", lb - 5, 1u << d->l2p[lb]);
         sb_printf(b, " supper[threadIdx.x] = o; }\n    __syncthreads();\n");
     }
+    b = &bsb;
     /* entry points */
     sb_printf(b, "    switch (start) {\n");
     for (int i = 0; i < d->nstarts; i++) sb_printf(b, "    case %d: goto S_%d;\n", d->starts[i], d->starts[i]);
@@ -309,7 +333,7 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
                 const qgt_dev_op2_t* so = &d->prog[u];
                 if (so->coef < 0) continue;
                 sb_printf(b, "      { ");
-                load_coef(b, so->coef);
+                load_coef(b, t, so->coef, u, QGEN_NONE);
                 sb_printf(b, " const int bit = ");
                 role_bit_expr(b, so->ra, so->q);
                 sb_printf(b, "; const R pr = bit ? m[6] : m[0], pi = bit ? m[7] : m[1]; const R t = cr * pr - ci * pi; "
@@ -326,7 +350,7 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
             for (int i = 0; i < RB; i++) {
                 const qgt_dev_op2_t* so = &d->prog[r0 + i];
                 sb_printf(b, "      { ");
-                load_coef(b, so->coef);
+                load_coef(b, t, so->coef, r0 + i, QGEN_NONE);
                 if (so->slot != 0)
                     sb_printf(b, " const R sg = (__popc(pthr & %uu) & 1) ? (R)-1 : (R)1;", (unsigned)so->slot);
                 else
@@ -354,13 +378,13 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
             const int cnt = o->seg, nl = o->ra;
             const unsigned rmask = o->rb;
             sb_printf(b, "    // op %d: block of %d commuting gates\n", pc, cnt);
-            for (int u = pc + 1; u <= pc + nl; u++) emit_u(b, &d->prog[u], u);
+            for (int u = pc + 1; u <= pc + nl; u++) emit_u(b, t, &d->prog[u], u);
             int at = pc + 1 + nl;
             for (int i = 0; i < RB; i++)
                 if ((rmask >> i) & 1u) {
                     qgt_dev_op2_t x = d->prog[at];
                     x.ra = (uint8_t)(RL_REG_ + i);   /* the block's i-th register op acts on register bit i */
-                    emit_u(b, &x, at);
+                    emit_u(b, t, &x, at);
                     at++;
                 }
             /* generators not folded into a gate: applied after the block (they commute with it) */
@@ -382,17 +406,17 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
         switch (o->kind) {
         case Q2_U:
         case Q2_UR:
-            emit_u(b, o, pc);
+            emit_u(b, t, o, pc);
             break;
         case Q2_PHASE:
             if (o->coef < 0) break;
             if (o->ra >= RL_REG_ && o->ra < RL_WARP_) {
                 sb_printf(b, "    { ");
-                load_coef(b, o->coef);
+                load_coef(b, t, o->coef, pc, QGEN_NONE);
                 sb_printf(b, " phase_reg<%d, NR, T, R>(v, m); }\n", o->ra - RL_REG_);
             } else {
                 sb_printf(b, "    { ");
-                load_coef(b, o->coef);
+                load_coef(b, t, o->coef, pc, QGEN_NONE);
                 sb_printf(b, " const int bit = ");
                 role_bit_expr(b, o->ra, o->q);
                 sb_printf(b, "; const R pr = bit ? m[6] : m[0], pi = bit ? m[7] : m[1];\n"
@@ -414,7 +438,12 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
                              "if ((cmask >> j) & 1u) v[j] = w; } }\n", (int)o->ra);
             break;
         default:
-            free(sb.s);
+            free(hsb.s);
+            free(bsb.s);
+            free(osb.s);
+            free(t->coef);
+            free(t->pc);
+            free(t->gen);
             qgt_set_error(-1, "jit: op kind %d at %d not expected outside a block", (int)o->kind, pc);
             return NULL;
         }
@@ -438,10 +467,46 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
                  "          atomicMax(rowmax + (long long)blockIdx.z * rowmax_stride + e[%d], __float_as_uint(mx));\n"
                  "        }\n      }\n    }\n}\n",
               QENT_ROWMAX, 1 << WB, 1 << WB, (int)(offsetof(qgt_dev_entry_t, dst_row) / 4));
-    if (sb.err) {
-        free(sb.s);
+    /* assemble: slot table, head, staging of the slots (with the spawn folds), body */
+    b = &osb;
+    const int ns = t->n;
+    sb_printf(b, "#define LDS8(m, s) { const float4 a_ = *reinterpret_cast<const float4*>(csm + 8 * (s)); "
+                 "const float4 b_ = *reinterpret_cast<const float4*>(csm + 8 * (s) + 4); "
+                 "m[0] = a_.x; m[1] = a_.y; m[2] = a_.z; m[3] = a_.w; m[4] = b_.x; m[5] = b_.y; m[6] = b_.z; m[7] = b_.w; }\n");
+    if (ns > 0) {
+        sb_printf(b, "static __device__ const int qslot_%s[%d] = {", d->kname, ns);
+        for (int i = 0; i < ns; i++) sb_printf(b, "%s%d", i ? ", " : "", t->coef[i]);
+        sb_printf(b, "};\n");
+    }
+    sb_printf(b, "%s", hsb.s ? hsb.s : "");
+    if (ns > 0) {
+        sb_printf(b, "    __shared__ __align__(16) float csm[%d];\n", 8 * ns);
+        sb_printf(b, "    for (int i = threadIdx.x; i < %d; i += %d) csm[i] = __ldg(ct + 8 * qslot_%s[i >> 3] + (i & 7));\n",
+                  8 * ns, nthreads, d->kname);
+        sb_printf(b, "    __syncthreads();\n");
+        int nf = 0;
+        for (int i = 0; i < ns; i++) nf += t->gen[i] != QGEN_NONE;
+        if (nf) {
+            sb_printf(b, "    if (threadIdx.x == 0) {\n      switch (spawn) {\n");
+            for (int i = 0; i < ns; i++)
+                if (t->gen[i] != QGEN_NONE)
+                    sb_printf(b, "      case %d: fold_gen(csm + %d, %d); break;\n", t->pc[i], 8 * i, (int)t->gen[i]);
+            sb_printf(b, "      default: break;\n      }\n    }\n    __syncthreads();\n");
+        }
+    } else {
+        sb_printf(b, "    const float* csm = ct;\n    (void)csm;\n");
+    }
+    sb_printf(b, "%s", bsb.s ? bsb.s : "");
+    const int err = hsb.err || bsb.err || osb.err || t->err;
+    free(hsb.s);
+    free(bsb.s);
+    free(t->coef);
+    free(t->pc);
+    free(t->gen);
+    if (err) {
+        free(osb.s);
         qgt_set_error(-2, "jit: out of memory while writing the pass source");
         return NULL;
     }
-    return sb.s;
+    return osb.s;
 }
