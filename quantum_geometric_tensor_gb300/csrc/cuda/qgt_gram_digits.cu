@@ -33,7 +33,8 @@
 //             rest Re | rest Im] (two regions of 256 columns)
 //   epilogue (the converter warps): TMEM -> FP32 (hh + rest) -> partials
 // The raw ring (3 stages) and the plane ring (2 stages) are decoupled, so a
-// raw buffer is refilled as soon as it has been converted.
+// raw buffer is refilled as soon as it has been converted; the converters load
+// a k-step's raw values into registers before they wait for a free plane stage.
 // A second kernel sums the partials in FP64 and applies u_i u_j.
 //
 // Every mbarrier wait is bounded (globaltimer); on expiry the CTA records an
@@ -362,33 +363,57 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
             const int rs = kt % DG_RAW_STAGES, ps = kt % DG_PL_STAGES;
             bool ok = bar_wait(stall ? smem_u32(&never_bar) : smem_u32(&raw_full[rs]), (kt / DG_RAW_STAGES) & 1,
                                deadline);
+            const uint8_t* rawst = raw_base + rs * 2 * DG_RAW_BYTES;
+            uint8_t* plst = pl_base + ps * DG_PL_STAGE;
+            constexpr int NIT = 128 / (4 * DG_CONV_WARPS);
+            // all of the k-step's raw values first (independent shared loads, issued while the plane
+            // stage may still be in use by the MMAs), then the digit planes
+            float4 q[2][NIT];
+            float iuv[2][NIT];
+            if (ok) {
+#pragma unroll
+                for (int b = 0; b < 2; b++) {
+                    const float* raw = reinterpret_cast<const float*>(rawst + b * DG_RAW_BYTES);
+                    const int rlim = (diag || b == 1) ? rbB : 128;
+#pragma unroll
+                    for (int it = 0; it < NIT; it++) {
+                        const int r = 4 * cw + 4 * DG_CONV_WARPS * it + sub;
+                        if (b < nblk && 4 * cw + 4 * DG_CONV_WARPS * it < rlim) {
+                            q[b][it] = *reinterpret_cast<const float4*>(raw + r * 32 + 2 * kp);
+                            iuv[b][it] = inv_u[b][r];
+                        } else {
+                            q[b][it] = make_float4(0.f, 0.f, 0.f, 0.f);
+                            iuv[b][it] = 0.f;
+                        }
+                    }
+                }
+            }
             if (ok && kt >= DG_PL_STAGES) ok = bar_wait(smem_u32(&pl_empty[ps]), ((kt / DG_PL_STAGES) & 1) ^ 1, deadline);
             if (!ok) {
                 atomicExch(err, DG_ERR_TIMEOUT);
                 abort_sh = 1;
             }
             if (abort_sh) break;
-            const uint8_t* rawst = raw_base + rs * 2 * DG_RAW_BYTES;
-            uint8_t* plst = pl_base + ps * DG_PL_STAGE;
-            for (int b = 0; b < nblk; b++) {
-                const float* raw = reinterpret_cast<const float*>(rawst + b * DG_RAW_BYTES);
+#pragma unroll
+            for (int b = 0; b < 2; b++) {
+                if (b >= nblk) break;
                 // the B layout (9 planes) for the B block and for a diagonal pair's only block
                 const bool blay = diag || b == 1;
                 uint8_t* planes = plst + (diag ? 0 : b * DG_PL_A * DG_PLANE_BYTES);
                 const uint32_t ps_ = blay ? pbB : (uint32_t)DG_PLANE_BYTES;   // plane stride
                 const int rlim = blay ? rbB : 128;
 #pragma unroll
-                for (int it = 0; it < 128 / (4 * DG_CONV_WARPS); it++) {
+                for (int it = 0; it < NIT; it++) {
                     const int rr = 4 * cw + 4 * DG_CONV_WARPS * it;
                     if (rr >= rlim) break;   // warp-uniform (rr depends on the warp only)
                     const int r = rr + sub;
-                    const float4 q = *reinterpret_cast<const float4*>(raw + r * 32 + 2 * kp);
-                    const float iu = inv_u[b][r];
+                    const float4 qq = q[b][it];
+                    const float iu = iuv[b][it];
                     // SWIZZLE_32B: 16-byte chunk (k / 8) xor bit 2 of the row; kp, kp + 1 share a chunk
                     const int off = r * 32 + ((((kp >> 3) ^ (r >> 2)) & 1) << 4) + (kp & 7) * 2;
 #pragma unroll
                     for (int c = 0; c < 2; c++) {   // 0: real parts, 1: imaginary parts
-                        const float x0 = (c ? q.y : q.x) * iu, x1 = (c ? q.w : q.z) * iu;
+                        const float x0 = (c ? qq.y : qq.x) * iu, x1 = (c ? qq.w : qq.z) * iu;
                         const float d0 = rintf(x0), d1 = rintf(x1);
                         const float l0 = x0 - d0, l1 = x1 - d1;
                         const __half2 h1 = __floats2half2_rn(l0, l1);
