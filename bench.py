@@ -300,7 +300,9 @@ def run_gb300(args, ws, rank, local):
             tj = json.load(open(tp))
             # measured for this workload and this build of the pass kernels only
             kinds = "compiled" if info.jit_passes > 0 else "interpreted"
-            if tj.get("workload") == workload and (dom != "passes" or tj.get("passes_kernels") == kinds):
+            same = (tj.get("passes_kernels") == kinds and tj.get("tile_bits") == info.tile_bits and
+                    tj.get("thread_amps", 32) == info.thread_amps)
+            if tj.get("workload") == workload and (dom != "passes" or same):
                 traffic = tj.get(dom)
         except Exception:
             traffic = None
@@ -367,6 +369,7 @@ def run_gb300(args, ws, rank, local):
             "gate_hbm_gbs": gate_gbs,
             "gram_tflops_algorithmic": gram_tf,
             "plan": {"passes": info.num_passes, "vector_passes": info.vector_passes, "tile_bits": info.tile_bits,
+                     "thread_amps": info.thread_amps,
                      "device_gb": info.device_bytes / 1e9, "compiled_passes": info.jit_passes,
                      "create_s": t_create},
             "fp64_gpu": fp64,

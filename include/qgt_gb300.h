@@ -121,6 +121,11 @@ typedef struct {
      * interpreter below), QGT_PASS_INTERPRET, QGT_PASS_COMPILED; the environment variable
      * QGT_PASS_JIT=0 / 1 overrides it */
     int32_t pass_kernels;
+    /* amplitudes each thread holds in registers on 13- / 14-qubit complex64 (MIXED) tiles: 0 or
+     * 32, or 16 (twice the threads per tile and twice the warps per SM, about a quarter more
+     * re-layouts; faster for some circuits, slower for others: qgt_plan_autotune measures it).
+     * 16 needs compiled pass kernels. */
+    int32_t thread_amps;
 } qgt_plan_options_t;
 enum { QGT_TRANSPORT_AUTO = 0, QGT_TRANSPORT_FORWARD = 1, QGT_TRANSPORT_MEET = 2 };
 enum { QGT_PASS_AUTO = 0, QGT_PASS_INTERPRET = 1, QGT_PASS_COMPILED = 2 };
@@ -138,6 +143,7 @@ typedef struct {
     int32_t batch, num_deriv_params;                       /* points per step; output width Pd */
     int32_t meet_in_middle, cut_gate;                      /* transport used; first gate of the backward half */
     int32_t jit_passes;                                    /* passes running as compiled straight-line kernels */
+    int32_t thread_amps;                                   /* amplitudes per thread of the register tiles */
 } qgt_plan_info_t;
 
 /* Default options: MIXED, TFIM J = h = 1, lambda = 1e-3, device 0, graph on. */
@@ -397,11 +403,12 @@ int qgt_plan_test_gram_stall(qgt_plan_t* plan, int stall, int64_t timeout_ns);
 
 /* ---- autotuning --------------------------------------------------------
  * Times the candidate configurations of a circuit's plan on the GPU (the
- * register tile, 13 or 14 qubits; interpreted or compiled pass kernels) for
- * the given base options (precision, batch, derivative parameters,
- * Hamiltonian), each over `steps` graph launches after two warm-up steps,
- * and returns the fastest as *tuned (base with tile_bits and pass_kernels
- * set) and its time per step.  Results are kept in the text file cache_path
+ * register tile, 13 or 14 qubits; interpreted or compiled pass kernels; 32
+ * or 16 amplitudes per thread with compiled kernels) for the given base options
+ * (precision, batch, derivative parameters, Hamiltonian), each over `steps`
+ * graph launches after two warm-up steps, and returns the fastest as *tuned
+ * (base with tile_bits, pass_kernels and thread_amps set) and its time per
+ * step.  Results are kept in the text file cache_path
  * (one line per circuit structure and base options; NULL: no file): a circuit
  * already in the file is not timed again.  No reference counterpart. */
 int qgt_plan_autotune(const qgt_circuit_desc_t* circuit, const qgt_plan_options_t* base, const char* cache_path,

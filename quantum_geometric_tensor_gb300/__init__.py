@@ -37,7 +37,7 @@ class PlanOptions(C.Structure):
                 ("lambda_", C.c_double), ("device", C.c_int32), ("use_graph", C.c_int32), ("batch", C.c_int32),
                 ("num_deriv_params", C.c_int32), ("num_pauli_terms", C.c_int32), ("pauli_strings", C.c_char_p),
                 ("pauli_coeffs", C.c_void_p), ("transport", C.c_int32), ("tile_bits", C.c_int32),
-                ("pass_kernels", C.c_int32)]
+                ("pass_kernels", C.c_int32), ("thread_amps", C.c_int32)]
 
 
 class PlanInfo(C.Structure):
@@ -46,7 +46,7 @@ class PlanInfo(C.Structure):
                 ("tile_bits", C.c_int32), ("vector_passes", C.c_int64), ("gate_bytes", C.c_int64),
                 ("gram_flops", C.c_int64), ("device_bytes", C.c_int64), ("batch", C.c_int32),
                 ("num_deriv_params", C.c_int32), ("meet_in_middle", C.c_int32), ("cut_gate", C.c_int32),
-                ("jit_passes", C.c_int32)]
+                ("jit_passes", C.c_int32), ("thread_amps", C.c_int32)]
 
 
 class BatchOptions(C.Structure):
@@ -201,7 +201,7 @@ class Plan:
 
     def __init__(self, n, gates, num_params=None, precision=MIXED, hamiltonian=HAM_TFIM, J=1.0, h=1.0,
                  lam=1e-3, device=0, use_graph=True, batch=1, deriv_params=0, pauli=None, transport=0,
-                 tile_bits=0, pass_kernels=0):
+                 tile_bits=0, pass_kernels=0, thread_amps=0):
         """pauli: [(coeff, "XZIY..."), ...] selects the Pauli-sum Hamiltonian (character n-1-q acts on qubit q)."""
         L = lib()
         self.desc = circuit_desc(n, gates, num_params)
@@ -218,7 +218,7 @@ class Plan:
             o.pauli_coeffs = self._pauli[1].ctypes.data
         o.lambda_, o.device, o.use_graph = lam, device, int(use_graph)
         o.batch, o.num_deriv_params, o.transport = int(batch), int(deriv_params), int(transport)
-        o.tile_bits, o.pass_kernels = int(tile_bits), int(pass_kernels)
+        o.tile_bits, o.pass_kernels, o.thread_amps = int(tile_bits), int(pass_kernels), int(thread_amps)
         self.opt = o
         h_ = C.c_void_p()
         _check(L.qgt_plan_create(C.byref(self.desc), C.byref(o), C.byref(h_)), "qgt_plan_create")
@@ -551,7 +551,7 @@ def berry_phase(states):
 
 def autotune(n, gates, num_params=None, precision=MIXED, hamiltonian=HAM_TFIM, batch=1, deriv_params=0, lam=1e-3,
              device=0, cache=None, steps=5):
-    """qgt_plan_autotune -> (tile_bits, pass_kernels, ms per step) of the fastest configuration."""
+    """qgt_plan_autotune -> (tile_bits, pass_kernels, thread_amps, ms per step) of the fastest configuration."""
     L = lib()
     L.qgt_plan_autotune.argtypes = [C.POINTER(CircuitDesc), C.POINTER(PlanOptions), C.c_char_p, C.c_int32,
                                     C.POINTER(PlanOptions), C.POINTER(C.c_double)]
@@ -564,4 +564,4 @@ def autotune(n, gates, num_params=None, precision=MIXED, hamiltonian=HAM_TFIM, b
     ms = C.c_double()
     _check(L.qgt_plan_autotune(C.byref(d), C.byref(o), None if cache is None else str(cache).encode(), int(steps),
                                C.byref(t), C.byref(ms)), "qgt_plan_autotune")
-    return int(t.tile_bits), int(t.pass_kernels), float(ms.value)
+    return int(t.tile_bits), int(t.pass_kernels), int(t.thread_amps), float(ms.value)

@@ -42,6 +42,7 @@ struct qgt_jit_kernel {
     cudaLibrary_t lib;
     cudaKernel_t kern;
     int32_t smem;
+    int32_t nthreads;        // block size: 32 << warp bits of the tile
     int32_t attr_dev_mask;   // devices (bit per ordinal < 32) whose shared-memory limit is raised
     struct qgt_jit_kernel* next;
 };
@@ -182,10 +183,12 @@ static int set_smem(struct qgt_jit_kernel* k, int device)
     return 0;
 }
 
-extern "C" int qgt_dev_jit_compile(const char* body, const char* kname, int32_t smem, int32_t device,
+extern "C" int qgt_dev_jit_compile(const char* body, const char* kname, int32_t smem, int32_t nthreads, int32_t device,
                                    qgt_jit_kernel_t** out)
 {
     *out = NULL;
+    if (nthreads != 256 && nthreads != 512 && nthreads != 1024)
+        return qgt_set_error(-1, "jit: block of %d threads", nthreads);
     if (cudaSetDevice(device) != cudaSuccess) return qgt_set_error(-6, "jit: device %d", device);
     char* src = full_source(body);
     if (!src) return qgt_set_error(-2, "jit: out of host memory");
@@ -234,6 +237,7 @@ extern "C" int qgt_dev_jit_compile(const char* body, const char* kname, int32_t 
     if (!k) { free(cubin); return qgt_set_error(-2, "jit: out of host memory"); }
     k->key = key;
     k->smem = smem;
+    k->nthreads = nthreads;
     cudaError_t e = cudaLibraryLoadData(&k->lib, cubin, NULL, NULL, 0, NULL, NULL, 0);
     free(cubin);
     if (e == cudaSuccess) e = cudaLibraryGetKernel(&k->kern, k->lib, kname);
@@ -269,7 +273,6 @@ extern "C" int qgt_dev_jit_compile(const char* body, const char* kname, int32_t 
 extern "C" int qgt_dev_jit_launch(const qgt_jit_kernel_t* k, const qgt_dev_pass2_args_t* a, void* stream)
 {
     if (a->nentries <= 0) return 0;
-    const int WB = a->tile_bits - 5 - 5;   // complex64 tiles of 13 / 14 bits: 5 register bits
     const int64_t ntiles = (int64_t)1 << (a->n - a->tile_bits);
     const int np = a->npoints > 0 ? a->npoints : 1;
     if (a->tile_bits < 13 || a->tile_bits > 14 || a->nentries > 65535 || ntiles > 0x7fffffff || np > 65535)
@@ -284,7 +287,7 @@ extern "C" int qgt_dev_jit_launch(const qgt_jit_kernel_t* k, const qgt_dev_pass2
     int rowmax_stride = a->rowmax_stride;
     void* args[] = {&V, &N, &ents, &coef32, &rowmax, &coef_stride, &point_stride, &rowmax_stride};
     dim3 grid((unsigned)ntiles, (unsigned)a->nentries, (unsigned)np);
-    cudaError_t e = cudaLaunchKernel((const void*)k->kern, grid, dim3(32u << WB), args, (size_t)k->smem,
+    cudaError_t e = cudaLaunchKernel((const void*)k->kern, grid, dim3((unsigned)k->nthreads), args, (size_t)k->smem,
                                      (cudaStream_t)stream);
     if (e != cudaSuccess) return qgt_set_error(-6, "jit: launch: %s", cudaGetErrorString(e));
     return 0;

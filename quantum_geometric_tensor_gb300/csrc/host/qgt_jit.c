@@ -224,7 +224,7 @@ static void emit_u(sbuf_t* b, slots_t* t, const qgt_dev_op2_t* o, int pc)
 char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
 {
     const int RB = d->RB, WB = d->WB, NR = 1 << RB;
-    if (RB < 4 || RB > 5 || WB < 3 || WB > 4 || d->nops < 1 || d->prog[0].kind != Q2_SEG) {
+    if (RB < 4 || RB > 5 || WB < 3 || WB > 5 || d->nops < 1 || d->prog[0].kind != Q2_SEG) {
         qgt_set_error(-1, "jit: unsupported program (RB %d, WB %d)", RB, WB);
         return NULL;
     }
@@ -248,7 +248,10 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
     hsb.s[0] = bsb.s[0] = osb.s[0] = 0;
     sbuf_t* b = &hsb;
     const int nthreads = 32 << WB;
-    const int minb = WB >= 4 ? 1 : (RB == 4 ? 3 : 2);
+    /* CTAs per SM the registers must allow: 512-thread 14-qubit tiles 1, 1024-thread 14-qubit tiles 1
+     * (64 registers), 512-thread 13-qubit tiles of 16 amplitudes 2 (64 registers), 256-thread tiles
+     * 2 (32 amplitudes) or 3 (16) */
+    const int minb = WB == 5 ? 1 : (WB == 4 ? (RB == 4 ? 2 : 1) : (RB == 4 ? 3 : 2));
     const int es = (int)(sizeof(qgt_dev_entry_t) / 4);
     sb_printf(b, "extern \"C\" __global__ void __launch_bounds__(%d, %d) %s(float2* __restrict__ V, long long N, "
                  "const int* __restrict__ ents, const float* __restrict__ coef32, unsigned* __restrict__ rowmax, "

@@ -303,9 +303,20 @@ static int full_tile_bits(const qgt_plan_t* p)
     return p->wide ? QGT_TILE_WIDE_F32 : QGT_TILE_MAX_F32;
 }
 
-/* register bits of the plan's register-resident tiles: 4 for complex128 and for 12-bit complex64
- * tiles, 5 otherwise */
-static int reg_bits(const qgt_plan_t* p) { return (p->fp64 || full_tile_bits(p) == QGT_TILE_MAX_F64) ? 4 : 5; }
+/* register bits of the plan's register-resident tiles: 4 for complex128, for 12-bit complex64
+ * tiles and for 13- / 14-bit tiles with thread_amps = 16 (compiled kernels only), 5 otherwise */
+static int amps16(const qgt_plan_t* p)
+{
+    const int tb = full_tile_bits(p);
+    return p->opt.precision == QGT_PRECISION_MIXED && p->opt.thread_amps == 16 &&
+           (tb == QGT_TILE_MAX_F32 || tb == QGT_TILE_WIDE_F32);
+}
+
+static int reg_bits(const qgt_plan_t* p)
+{
+    if (amps16(p)) return 4;   /* 512 threads on 13-qubit tiles, 1024 on 14 */
+    return (p->fp64 || full_tile_bits(p) == QGT_TILE_MAX_F64) ? 4 : 5;
+}
 
 static int compile_schedule(qgt_plan_t* p)
 {
@@ -431,8 +442,13 @@ static void free_schedule(qgt_plan_t* p)
 }
 
 /* complex64 plans of 14 or more qubits: 14-bit tiles (512-thread CTAs, one per SM) when their
- * schedule needs at least 8 % fewer vector passes than 13-bit tiles (two 256-thread CTAs per
- * SM), the cost of a vector pass being about 8 % higher with the wide tile */
+ * schedule needs sufficiently fewer vector passes than 13-bit tiles (two 256-thread CTAs per SM).
+ * A vector pass costs about 8 % more on the wide tile with the program interpreter and about
+ * 55 % more with compiled kernels (20 qubits, 8 layers: 486 wide vector passes took 4.9 ms, 649
+ * narrow ones 4.1 ms: two CTAs per SM overlap one tile's loads with the other's gates), so the wide
+ * tile needs 8 % fewer vector passes with the interpreter and 36 % fewer with compiled kernels. */
+static int jit_wanted(const qgt_plan_t* p);
+
 static int choose_tile(qgt_plan_t* p)
 {
     p->wide = 0;
@@ -448,7 +464,7 @@ static int choose_tile(qgt_plan_t* p)
         free_schedule(p);
         if (rc) return rc;
     }
-    p->wide = 100 * vp[1] <= 92 * vp[0];
+    p->wide = 100 * vp[1] <= (jit_wanted(p) ? 64 : 92) * vp[0];
     return 0;
 }
 
@@ -1254,7 +1270,7 @@ typedef struct {
 static void* jit_worker(void* arg)
 {
     jit_job_t* j = (jit_job_t*)arg;
-    j->rc = qgt_dev_jit_compile(j->src, j->d.kname, j->smem, j->device, &j->out);
+    j->rc = qgt_dev_jit_compile(j->src, j->d.kname, j->smem, 32 << j->d.WB, j->device, &j->out);
     if (j->rc) snprintf(j->err, sizeof j->err, "%s", qgt_last_error());
     return NULL;
 }
@@ -1266,7 +1282,7 @@ static int jit_wanted(const qgt_plan_t* p)
     if (env && env[0] == '0') return 0;
     if (env && env[0] == '1') return 1;
     if (p->opt.pass_kernels == QGT_PASS_INTERPRET) return 0;
-    if (p->opt.pass_kernels == QGT_PASS_COMPILED) return 1;
+    if (p->opt.pass_kernels == QGT_PASS_COMPILED || p->opt.thread_amps == 16) return 1;
     return p->n >= 16;
 }
 
@@ -1374,6 +1390,12 @@ static int build_jit(qgt_plan_t* p)
         }
     }
     jit_set_free(&js);
+    /* the interpreter has no 16-amplitude 13- / 14-qubit tile: every such pass must have its kernels */
+    for (int k = 0; !rc && k < p->npasses; k++) {
+        const spass_t* ps = &p->passes[k];
+        if (ps->prog_count > 0 && amps16(p) && (!ps->jit[0] || (ps->ckpt_writer && !ps->jit[1])))
+            rc = qgt_set_error(E_STATE, "jit: pass %d of a 16-amplitude tile has no compiled kernel", k);
+    }
     if (rc) { for (int k = 0; k < p->npasses; k++) p->passes[k].jit[0] = p->passes[k].jit[1] = NULL; p->njit = 0; }
     return rc;
 }
@@ -1411,6 +1433,11 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
         free(p);
         return qgt_set_error(E_INVAL, "qgt_plan_create: tile_bits %d (0, 13, 14) / pass_kernels %d (0 .. 2)", tb, pk);
     }
+    if (p->opt.thread_amps != 0 && p->opt.thread_amps != 16 && p->opt.thread_amps != 32) {
+        int bad = p->opt.thread_amps;
+        free(p);
+        return qgt_set_error(E_INVAL, "qgt_plan_create: thread_amps %d (0, 16 or 32)", bad);
+    }
     if (p->opt.hamiltonian < QGT_HAMILTONIAN_NONE || p->opt.hamiltonian > QGT_HAMILTONIAN_PAULI) {
         int bad = (int)p->opt.hamiltonian;
         free(p);
@@ -1418,6 +1445,10 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
     }
     p->n = c->num_qubits;
     p->N = (int64_t)1 << p->n;
+    if (p->opt.thread_amps == 16 && p->opt.precision == QGT_PRECISION_MIXED && !jit_wanted(p)) {
+        free(p);
+        return qgt_set_error(E_INVAL, "qgt_plan_create: thread_amps 16 needs compiled pass kernels (pass_kernels, QGT_PASS_JIT)");
+    }
     p->P = c->num_params;
     p->B = p->opt.batch > 0 ? p->opt.batch : 1;
     p->Pd = p->opt.num_deriv_params > 0 ? p->opt.num_deriv_params : p->P;
@@ -1741,6 +1772,7 @@ int qgt_plan_get_info(const qgt_plan_t* p, qgt_plan_info_t* info)
     info->meet_in_middle = p->mitm;
     info->cut_gate = p->mitm ? p->cut : -1;
     info->jit_passes = p->njit;
+    info->thread_amps = p->nprog > 0 ? 1 << reg_bits(p) : 0;
     info->device_bytes = p->device_bytes;
     return 0;
 }

@@ -1,15 +1,16 @@
 /*
  * qgt_tune.c -- measured choice of a plan's configuration.
  *
- * Which register tile (13 or 14 qubits) and which pass kernels (the program
- * interpreter or compiled straight-line kernels) run a circuit fastest
+ * Which register tile (13 or 14 qubits), which pass kernels (the program
+ * interpreter or compiled straight-line kernels) and how many amplitudes per
+ * thread (32, or 16 with compiled kernels) run a circuit fastest
  * depends on its shape: how many gates a pass packs, how many vectors cross
  * it, how far the derivative states travel.  qgt_plan_autotune builds each
  * candidate plan, times its step graph on the GPU with CUDA events and keeps
  * the fastest.  Results go to a text cache, one line per circuit structure
  * and base options:
  *
- *     <key (16 hex digits)> <tile_bits> <pass_kernels> <ms per step>
+ *     <key (16 hex digits)> <tile_bits> <pass_kernels> <thread_amps> <ms per step>
  *
  * so a structure is timed once; ragged batches consult the cache for every
  * structural group (qgt_batch_options_t.tune_cache).
@@ -47,12 +48,12 @@ static uint64_t tune_key(const qgt_circuit_desc_t* c, const qgt_plan_options_t* 
         h = fnv(h, &d->param, sizeof d->param);
         if (d->param < 0) h = fnv(h, &d->angle, sizeof d->angle);
     }
-    const int32_t f[6] = {(int32_t)o->precision, (int32_t)o->hamiltonian, o->batch, o->num_deriv_params, o->transport,
-                          o->num_pauli_terms};
+    const int32_t f[7] = {(int32_t)o->precision, (int32_t)o->hamiltonian, o->batch, o->num_deriv_params, o->transport,
+                          o->num_pauli_terms, 3 /* candidate set: tile x kernels x amplitudes per thread */};
     return fnv(h, f, sizeof f);
 }
 
-static int cache_lookup(const char* path, uint64_t key, int* tile, int* kern, double* ms)
+static int cache_lookup(const char* path, uint64_t key, int* tile, int* kern, int* amps, double* ms)
 {
     if (!path) return 0;
     FILE* f = fopen(path, "r");
@@ -61,12 +62,13 @@ static int cache_lookup(const char* path, uint64_t key, int* tile, int* kern, do
     int found = 0;
     while (fgets(line, sizeof line, f)) {
         unsigned long long k;
-        int t, kk;
+        int t, kk, a;
         double m;
         if (line[0] == '#') continue;
-        if (sscanf(line, "%llx %d %d %lf", &k, &t, &kk, &m) == 4 && k == key) {
+        if (sscanf(line, "%llx %d %d %d %lf", &k, &t, &kk, &a, &m) == 5 && k == key) {
             *tile = t;
             *kern = kk;
+            *amps = a;
             *ms = m;
             found = 1;   /* the last line for a key wins */
         }
@@ -75,12 +77,12 @@ static int cache_lookup(const char* path, uint64_t key, int* tile, int* kern, do
     return found;
 }
 
-static void cache_store(const char* path, uint64_t key, int tile, int kern, double ms)
+static void cache_store(const char* path, uint64_t key, int tile, int kern, int amps, double ms)
 {
     if (!path) return;
     FILE* f = fopen(path, "a");
     if (!f) return;
-    fprintf(f, "%016llx %d %d %.9g\n", (unsigned long long)key, tile, kern, ms);
+    fprintf(f, "%016llx %d %d %d %.9g\n", (unsigned long long)key, tile, kern, amps, ms);
     fclose(f);
 }
 
@@ -120,11 +122,12 @@ int qgt_plan_autotune(const qgt_circuit_desc_t* c, const qgt_plan_options_t* bas
     *tuned = o;
     if (best_ms) *best_ms = -1.0;
     const uint64_t key = tune_key(c, &o);
-    int tile = 0, kern = 0;
+    int tile = 0, kern = 0, amps = 0;
     double ms = -1.0;
-    if (cache_lookup(cache_path, key, &tile, &kern, &ms)) {
+    if (cache_lookup(cache_path, key, &tile, &kern, &amps, &ms)) {
         tuned->tile_bits = tile;
         tuned->pass_kernels = kern;
+        tuned->thread_amps = amps;
         if (best_ms) *best_ms = ms;
         return 0;
     }
@@ -147,23 +150,30 @@ int qgt_plan_autotune(const qgt_circuit_desc_t* c, const qgt_plan_options_t* bas
     }
     double best = -1.0;
     for (int a = 0; a < nt; a++)
-        for (int b = 0; b < nk; b++) {
-            qgt_plan_options_t x = o;
-            x.use_graph = 1;
-            x.tile_bits = tiles[a];
-            x.pass_kernels = kerns[b];
-            const double t = time_config(c, &x, steps, theta);
-            if (t > 0 && (best < 0 || t < best)) {
-                best = t;
-                tile = tiles[a];
-                kern = kerns[b];
+        for (int b = 0; b < nk; b++)
+            for (int m = 0; m < 2; m++) {
+                /* 16 amplitudes per thread: 13- / 14-qubit tiles with compiled kernels only */
+                const int am = m ? 16 : 0;
+                if (m && !(mixed && n >= 13 && kerns[b] != QGT_PASS_INTERPRET)) continue;
+                qgt_plan_options_t x = o;
+                x.use_graph = 1;
+                x.tile_bits = tiles[a];
+                x.pass_kernels = m ? QGT_PASS_COMPILED : kerns[b];
+                x.thread_amps = am;
+                const double t = time_config(c, &x, steps, theta);
+                if (t > 0 && (best < 0 || t < best)) {
+                    best = t;
+                    tile = x.tile_bits;
+                    kern = x.pass_kernels;
+                    amps = am;
+                }
             }
-        }
     free(theta);
     if (best < 0) return qgt_set_error(-6, "qgt_plan_autotune: no configuration of the circuit could be built");
     tuned->tile_bits = tile;
     tuned->pass_kernels = kern;
+    tuned->thread_amps = amps;
     if (best_ms) *best_ms = best;
-    cache_store(cache_path, key, tile, kern, best);
+    cache_store(cache_path, key, tile, kern, amps, best);
     return 0;
 }

@@ -180,8 +180,10 @@ typedef struct {
 /* CUDA source of one pass program (malloc'd; NULL and an error message on failure) */
 char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d);
 typedef struct qgt_jit_kernel qgt_jit_kernel_t;
-/* compile (or take from the process / disk cache) and load for `device`; smem = dynamic shared bytes */
-int qgt_dev_jit_compile(const char* body, const char* kname, int32_t smem, int32_t device, qgt_jit_kernel_t** out);
+/* compile (or take from the process / disk cache) and load for `device`; smem = dynamic shared bytes,
+ * nthreads = the kernel's block size (its __launch_bounds__) */
+int qgt_dev_jit_compile(const char* body, const char* kname, int32_t smem, int32_t nthreads, int32_t device,
+                        qgt_jit_kernel_t** out);
 /* launch over the entries of a, as qgt_dev_pass2 (complex64 register tiles only) */
 int qgt_dev_jit_launch(const qgt_jit_kernel_t* k, const qgt_dev_pass2_args_t* a, void* stream);
 /* seconds spent in the compiler by this process (cache hits cost nothing) */

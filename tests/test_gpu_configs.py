@@ -59,7 +59,7 @@ def test_headline_mixed_against_fp64(Q):
         info = pm.info()
         out = pm.run(theta)
         assert pm.status()[0] == 0
-    assert info.tile_bits == 14 and info.meet_in_middle == 1
+    assert info.tile_bits in (13, 14) and info.meet_in_middle == 1 and info.jit_passes > 0
     e = {"metric": rel(out["Q"].real, ref["Q"].real), "berry": rel(out["Q"].imag, ref["Q"].imag),
          "Q": rel(out["Q"], ref["Q"]), "grad": rel(out["grad"], ref["grad"]),
          "step": rel(out["natgrad"], ref["natgrad"]), "energy": abs(out["energy"] - ref["energy"])}

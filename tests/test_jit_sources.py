@@ -16,11 +16,13 @@ def Q():
     return Q
 
 
-def check(Q, n, gates, P, tmp_path, compile=1):
+def check(Q, n, gates, P, tmp_path, compile=1, **opts):
     d = Q.circuit_desc(n, gates, P)
     o = Q.PlanOptions()
     Q.lib().qgt_plan_default_options(C.byref(o))
     o.precision = Q.MIXED
+    for k_, v_ in opts.items():
+        setattr(o, k_, v_)
     sec = C.c_double()
     rc = Q.lib().qgt_plan_jit_check(C.cast(C.pointer(d), C.c_void_p), C.cast(C.pointer(o), C.c_void_p),
                                     str(tmp_path).encode(), compile, C.byref(sec))
@@ -60,3 +62,13 @@ def test_twenty_qubit_sources(Q, tmp_path):
     n, L = 20, 8
     k, _ = check(Q, n, Q.ansatz_gates(n, L, "cz"), 2 * n * L, tmp_path, compile=0)
     assert k >= 6
+
+
+@pytest.mark.parametrize("tile,bounds", [(14, "__launch_bounds__(1024, 1)"), (13, "__launch_bounds__(512, 2)")])
+def test_sixteen_amplitude_tile_sources(Q, tmp_path, tile, bounds):
+    """16 amplitudes per thread (thread_amps = 16): 1024-thread 14-qubit tiles and 512-thread
+    13-qubit tiles (two per SM) generate and compile."""
+    n, L = 16, 2
+    k, s = check(Q, n, Q.ansatz_gates(n, L, "cz"), 2 * n * L, tmp_path, tile_bits=tile, thread_amps=16)
+    srcs = [p.read_text() for p in tmp_path.iterdir()]
+    assert k == len(srcs) and all(bounds in x for x in srcs)
