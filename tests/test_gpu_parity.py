@@ -125,21 +125,24 @@ def test_reused_output_buffers(Q):
 
 
 def test_wide_tiles_against_fp64(Q):
-    """19 qubits, 8 layers: the scheduler takes 14-qubit register tiles (512-thread CTAs; 6 passes
-    instead of 9), with 32 tiles per vector and segment checkpoints; single and batched complex64
-    plans against the FP64 plan (12-qubit tiles)."""
+    """19 qubits, 8 layers on 14-qubit register tiles (512-thread CTAs; 6 passes instead of 9),
+    with 32 tiles per vector and segment checkpoints, interpreted and compiled; single and
+    batched complex64 plans against the FP64 plan (12-qubit tiles)."""
     n, L = 19, 8
     gates = Q.ansatz_gates(n, L, "cz")
     P = 2 * n * L
     th = np.stack([O.splitmix64_params(90, P), O.splitmix64_params(91, P)])
     with Q.Plan(n, gates, P, precision=Q.FP64) as p64:
         ref = p64.run(th[0])
-    with Q.Plan(n, gates, P, precision=Q.MIXED) as pm:
+    with Q.Plan(n, gates, P, precision=Q.MIXED, tile_bits=14) as pm:
         assert pm.info().tile_bits == 14
         out = pm.run(th[0])
-    with Q.Plan(n, gates, P, precision=Q.MIXED, batch=2) as pb:
+    with Q.Plan(n, gates, P, precision=Q.MIXED, tile_bits=14, pass_kernels=Q.PASS_INTERPRET) as pi:
+        assert pi.info().tile_bits == 14 and pi.info().jit_passes == 0
+        outi = pi.run(th[0])
+    with Q.Plan(n, gates, P, precision=Q.MIXED, batch=2, tile_bits=14) as pb:
         outb = pb.run(th)
-    for o in (out, {k: (v[0] if v is not None else None) for k, v in outb.items()}):
+    for o in (out, outi, {k: (v[0] if v is not None else None) for k, v in outb.items()}):
         assert rel(o["Q"].real, ref["Q"].real) < 1e-6
         assert rel(o["Q"], ref["Q"]) < 2e-6
         assert rel(o["grad"], ref["grad"]) < 2e-6
