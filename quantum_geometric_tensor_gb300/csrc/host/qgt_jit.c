@@ -186,34 +186,23 @@ static int folds_spawn(const qgt_dev_op2_t* o)
     return o->kind == Q2_U;
 }
 
-/* a single-qubit gate.  Real matrices (RY, H, X): RY's coefficients are stored in tangent form
- * [[1, -t], [t, 1]] or cotangent form [[k, -g], [g, k]] (g = +-1), which one depends on the angle
- * and is the same for every thread, so a register-bit gate branches (uniformly) to a path of one
- * multiply-add per component for either form and a lane-bit gate to one for the tangent form;
- * other real matrices (and the entry that carries the pass renormalisation) take m0 x + m2 y /
- * m4 x + m6 y.  Complex matrices in full.  pc: the op's program index (its spawn number). */
+/* a single-qubit gate: real matrices (RY, H, X) as m0 x + m2 y / m4 x + m6 y (two packed FP32x2
+ * instructions per amplitude), complex ones in full.  Uniform branches to one-multiply-add paths
+ * for RY's tangent and cotangent forms were measured slower (passes 4.24 -> 4.49 ms at 20 qubits):
+ * the code they add per gate costs more in instruction fetch than the multiply they save.
+ * pc: the op's program index (its spawn number). */
 static void emit_u(sbuf_t* b, slots_t* t, const qgt_dev_op2_t* o, int pc)
 {
     if (o->coef < 0) return;   /* identity */
     const int real = o->kind == Q2_UR;
     sb_printf(b, "    { ");
     load_coef(b, t, o->coef, pc, folds_spawn(o) ? o->gen : QGEN_NONE);
-    if (o->ra >= RL_REG_ && real) {
-        const int ri = o->ra - RL_REG_;
-        sb_printf(b, "\n      if (m[0] == 1.f && m[6] == 1.f) tan_reg<%d, NR, T, R>(v, m[2], m[4]);\n"
-                     "      else if (m[4] == 1.f && m[2] == -1.f) cot_reg<%d, NR, 1, T, R>(v, m[0], m[6]);\n"
-                     "      else if (m[4] == -1.f && m[2] == 1.f) cot_reg<%d, NR, -1, T, R>(v, m[0], m[6]);\n"
-                     "      else u_reg<%d, NR, true, T, R>(v, m); }\n", ri, ri, ri, ri);
-    } else if (o->ra >= RL_REG_) {
-        sb_printf(b, " u_reg<%d, NR, false, T, R>(v, m); }\n", o->ra - RL_REG_);
+    if (o->ra >= RL_REG_) {
+        sb_printf(b, " u_reg<%d, NR, %s, T, R>(v, m); }\n", o->ra - RL_REG_, real ? "true" : "false");
     } else if (real) {
-        sb_printf(b, " const int hi = (lane >> %d) & 1;\n"
-                     "      if (m[0] == 1.f && m[6] == 1.f) { const R cp0 = hi ? m[4] : m[2];\n"
-                     "#pragma unroll\n        for (int j = 0; j < NR; j++) { const T w = shfl_x<T>(v[j], %d); "
-                     "v[j] = fma_s<T, R>(cp0, w, v[j]); }\n"
-                     "      } else { const R cs0 = hi ? m[6] : m[0], cp0 = hi ? m[4] : m[2];\n"
-                     "#pragma unroll\n        for (int j = 0; j < NR; j++) { const T w = shfl_x<T>(v[j], %d); "
-                     "v[j] = rmad2<T, R>(cs0, v[j], cp0, w); } } }\n", o->ra, 1 << o->ra, 1 << o->ra);
+        sb_printf(b, " const int hi = (lane >> %d) & 1; const R cs0 = hi ? m[6] : m[0], cp0 = hi ? m[4] : m[2];\n"
+                     "#pragma unroll\n      for (int j = 0; j < NR; j++) { const T w = shfl_x<T>(v[j], %d); "
+                     "v[j] = rmad2<T, R>(cs0, v[j], cp0, w); } }\n", o->ra, 1 << o->ra);
     } else {
         sb_printf(b, " const int hi = (lane >> %d) & 1; const R mm[4] = {hi ? m[6] : m[0], hi ? m[7] : m[1], "
                      "hi ? m[4] : m[2], hi ? m[5] : m[3]};\n#pragma unroll\n      for (int j = 0; j < NR; j++) { "
