@@ -117,7 +117,7 @@ typedef struct {
      * least 8 % of the vector passes, else 13), 13 or 14 */
     int32_t tile_bits;
     /* pass kernels of complex64 plans on 13- / 14-qubit tiles: QGT_PASS_AUTO (each pass program
-     * compiled into its own straight-line kernel at plan creation from 16 qubits, the program
+     * compiled into its own straight-line kernel at plan creation from 13 qubits, the program
      * interpreter below), QGT_PASS_INTERPRET, QGT_PASS_COMPILED; the environment variable
      * QGT_PASS_JIT=0 / 1 overrides it */
     int32_t pass_kernels;

@@ -1255,7 +1255,7 @@ static int fold_diagonal_runs(qgt_plan_t* p)
 static int run_step(qgt_plan_t* p);
 
 /* Straight-line pass kernels (qgt_jit.c): complex64 plans of MIXED precision
- * whose passes run on 13- or 14-qubit register tiles, from 16 qubits on (or
+ * whose passes run on 13- or 14-qubit register tiles, from 13 qubits on (or
  * for every such plan with QGT_PASS_JIT=1; QGT_PASS_JIT=0 keeps the
  * interpreter).  The kernels of one plan compile in parallel. */
 typedef struct {
@@ -1283,7 +1283,7 @@ static int jit_wanted(const qgt_plan_t* p)
     if (env && env[0] == '1') return 1;
     if (p->opt.pass_kernels == QGT_PASS_INTERPRET) return 0;
     if (p->opt.pass_kernels == QGT_PASS_COMPILED || p->opt.thread_amps == 16) return 1;
-    return p->n >= 16;
+    return p->n >= 13;   /* every register-tile plan of 13 or more qubits */
 }
 
 /* the sources of every compiled pass kernel of the plan (host only) */
