@@ -603,6 +603,7 @@ int qgt_dev_event_create(void** ev)
 }
 int qgt_dev_event_destroy(void* ev) { if (ev) CK(cudaEventDestroy((cudaEvent_t)ev), "cudaEventDestroy"); return QGT_OK; }
 int qgt_dev_event_record(void* ev, void* s) { CK(cudaEventRecord((cudaEvent_t)ev, (cudaStream_t)s), "cudaEventRecord"); return QGT_OK; }
+int qgt_dev_event_sync(void* ev) { CK(cudaEventSynchronize((cudaEvent_t)ev), "cudaEventSynchronize"); return QGT_OK; }
 int qgt_dev_stream_wait_event(void* s, void* ev)
 {
     CK(cudaStreamWaitEvent((cudaStream_t)s, (cudaEvent_t)ev, 0), "cudaStreamWaitEvent");

@@ -120,12 +120,19 @@ struct qgt_plan {
     int32_t *slot_param_h, *param_ptr_h, *param_slots_h;
     /* device */
     void* stream;
-    void* graph;
+    void* graph;                  /* the step up to Q, grad and energy (run_head) */
+    void* graph_solve;            /* its natural-gradient solve (run_solve); NULL when there is none */
     /* passes with a checkpoint writer fork onto aux_stream (the writer, then the spawns that start
      * from its checkpoints) while the other entries run on stream; joined at the pass end */
     void* aux_stream;
     void* ev_fork;
     void* ev_join;
+    /* host outputs: Q, grad and energy are final after the post kernels, before the solve;
+     * qgt_plan_execute_host records ev_post between the two graphs and copies them on copy_stream
+     * and into the caller's buffers while the solve still runs */
+    void* copy_stream;
+    void* ev_post;
+    void* ev_copied;
     void* V;
     void* split;
     qgt_dev_op_t* ops_d;
@@ -1253,6 +1260,8 @@ static int fold_diagonal_runs(qgt_plan_t* p)
     } while (0)
 
 static int run_step(qgt_plan_t* p);
+static int run_head(qgt_plan_t* p, int* nl);
+static int run_solve(qgt_plan_t* p, int* nl);
 
 /* Straight-line pass kernels (qgt_jit.c): complex64 plans of MIXED precision
  * whose passes run on 13- or 14-qubit register tiles, from 13 qubits on (or
@@ -1548,6 +1557,9 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
     if (host_only) { *out = p; return 0; }
     if ((rc = qgt_dev_set_device(p->opt.device)) != 0) goto fail;
     if ((rc = qgt_dev_stream_create(&p->stream)) != 0) goto fail;
+    if ((rc = qgt_dev_stream_create(&p->copy_stream)) != 0) goto fail;
+    if ((rc = qgt_dev_event_create(&p->ev_post)) != 0) goto fail;
+    if ((rc = qgt_dev_event_create(&p->ev_copied)) != 0) goto fail;
     for (int k = 0; k < p->npasses; k++)
         if (p->passes[k].ckpt_writer && !p->aux_stream) {
             if ((rc = qgt_dev_stream_create(&p->aux_stream)) != 0) goto fail;
@@ -1691,13 +1703,20 @@ static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* op
     if ((rc = run_step(p)) != 0) goto fail;
     if ((rc = qgt_dev_stream_sync(p->stream)) != 0) goto fail;
     if (p->opt.use_graph) {
-        if ((rc = qgt_dev_graph_begin(p->stream)) != 0) goto fail;
-        int rs = run_step(p);
-        void* exec = NULL;
-        int re = qgt_dev_graph_end(p->stream, &exec);
-        if (rs) { rc = rs; goto fail; }
-        if (re) { rc = re; goto fail; }
-        p->graph = exec;
+        /* two graphs: the step up to Q / grad / energy, then the solve (so that host outputs can
+         * leave while the solve runs) */
+        int nl = 0;
+        for (int part = 0; part < 2; part++) {
+            if (part == 1 && !(p->Pd > 0 && p->opt.hamiltonian != QGT_HAMILTONIAN_NONE)) break;
+            if ((rc = qgt_dev_graph_begin(p->stream)) != 0) goto fail;
+            int rs = part == 0 ? run_head(p, &nl) : run_solve(p, &nl);
+            void* exec = NULL;
+            int re = qgt_dev_graph_end(p->stream, &exec);
+            if (rs) { qgt_dev_graph_destroy(exec); rc = rs; goto fail; }
+            if (re) { rc = re; goto fail; }
+            if (part == 0) p->graph = exec;
+            else p->graph_solve = exec;
+        }
     }
     *out = p;
     return 0;
@@ -1722,12 +1741,19 @@ void qgt_plan_destroy(qgt_plan_t* p)
     }
     if (p->stream) qgt_dev_stream_sync(p->stream);
     qgt_dev_graph_destroy(p->graph);
+    qgt_dev_graph_destroy(p->graph_solve);
     if (p->aux_stream) {
         qgt_dev_stream_sync(p->aux_stream);
         qgt_dev_stream_destroy(p->aux_stream);
     }
     qgt_dev_event_destroy(p->ev_fork);
     qgt_dev_event_destroy(p->ev_join);
+    if (p->copy_stream) {
+        qgt_dev_stream_sync(p->copy_stream);
+        qgt_dev_stream_destroy(p->copy_stream);
+    }
+    qgt_dev_event_destroy(p->ev_post);
+    qgt_dev_event_destroy(p->ev_copied);
     qgt_dev_tc_gram_destroy(p->tc);
     qgt_dev_dg_gram_destroy(p->dg);
     qgt_dev_free(p->rowmax_d);
@@ -1816,7 +1842,7 @@ static int pass2_launch(const spass_t* ps, const qgt_dev_pass2_args_t* b, int fp
     return qgt_dev_pass2(b, fp64, stream);
 }
 
-static int run_step(qgt_plan_t* p)
+static int run_head(qgt_plan_t* p, int* nl)
 {
     int rc;
     int launches = 0;
@@ -1993,7 +2019,19 @@ static int run_step(qgt_plan_t* p)
         pa.ngroups = p->nscale_groups;
         if ((rc = qgt_dev_post(&pa, p->stream)) != 0) return rc;
         launches += 1 + has_h;
-        MARK(5);
+    }
+    MARK(5);
+    *nl += launches;
+    return 0;
+}
+
+/* the natural-gradient solve of a step (after run_head) */
+static int run_solve(qgt_plan_t* p, int* nl)
+{
+    int rc;
+    int launches = 0;
+    const int has_h = p->opt.hamiltonian != QGT_HAMILTONIAN_NONE;
+    if (p->Pd > 0) {
         if (has_h) {
             if (p->B > 1) {
                 /* one CTA per point, lambda x10 retries inside */
@@ -2019,10 +2057,18 @@ static int run_step(qgt_plan_t* p)
             }
         }
     }
-    if (p->Pd <= 0) MARK(5);
     MARK(6);
-    p->launches = launches;
+    *nl += launches;
     return 0;
+}
+
+static int run_step(qgt_plan_t* p)
+{
+    int launches = 0;
+    int rc = run_head(p, &launches);
+    if (!rc) rc = run_solve(p, &launches);
+    if (!rc) p->launches = launches;
+    return rc;
 }
 
 int qgt_plan_profile_step(qgt_plan_t* p, qgt_step_profile_t* pr)
@@ -2046,14 +2092,22 @@ int qgt_plan_profile_step(qgt_plan_t* p, qgt_step_profile_t* pr)
     return 0;
 }
 
-static int launch_step(qgt_plan_t* p)
+/* one step; post_event: recorded on the stream once Q, grad and energy are final (NULL: none) */
+static int launch_step_ev(qgt_plan_t* p, void* post_event)
 {
-    int rc;
+    int rc, nl = 0;
     if (p->graph) rc = qgt_dev_graph_launch(p->graph, p->stream);
-    else rc = run_step(p);
+    else rc = run_head(p, &nl);
+    if (!rc && post_event) rc = qgt_dev_event_record(post_event, p->stream);
+    if (!rc) {
+        if (p->graph) rc = p->graph_solve ? qgt_dev_graph_launch(p->graph_solve, p->stream) : 0;
+        else rc = run_solve(p, &nl);
+    }
     p->has_run = 1;
     return rc;
 }
+
+static int launch_step(qgt_plan_t* p) { return launch_step_ev(p, NULL); }
 
 int qgt_plan_execute_device(qgt_plan_t* p, const double* theta_dev, double* Q_dev, double* grad_dev,
                             double* energy_dev, double* natgrad_dev)
@@ -2089,20 +2143,32 @@ int qgt_plan_execute_host(qgt_plan_t* p, const double* theta, double* Q, double*
         memcpy(p->theta_pin, theta, sizeof(double) * nth);
         if ((rc = qgt_dev_memcpy_h2d(p->theta_d, p->theta_pin, sizeof(double) * nth, p->stream)) != 0) return rc;
     }
-    if ((rc = launch_step(p)) != 0) return rc;
-    /* every output copy is queued behind the step: one synchronisation in the common case */
+    const int early = p->Pd > 0;
+    if ((rc = launch_step_ev(p, early ? p->ev_post : NULL)) != 0) return rc;
     const int need_status = has_h && p->Pd > 0;
     const int* gerr = p->tc ? qgt_dev_tc_gram_err(p->tc) : (p->dg ? qgt_dev_dg_gram_err(p->dg) : NULL);
+    /* Q, grad, energy and the Gram's status are final when the post kernels end (ev_post): they
+     * travel on copy_stream and into the caller's buffers while the solve runs; the solve's
+     * status and natgrad follow on the step's stream (one more synchronisation) */
+    void* cs = early ? p->copy_stream : p->stream;
+    if (early && (rc = qgt_dev_stream_wait_event(cs, p->ev_post)) != 0) return rc;
+    if (gerr && (rc = qgt_dev_memcpy_d2h(p->gerr_pin, gerr, sizeof(int), cs)) != 0) return rc;
+    if (Q && (rc = qgt_dev_memcpy_d2h(p->Q_pin, p->Q_d, sizeof(double) * 2 * B * Pd * Pd, cs)) != 0) return rc;
+    if (grad && (rc = qgt_dev_memcpy_d2h(p->grad_pin, p->grad_d, sizeof(double) * B * Pd, cs)) != 0) return rc;
+    if (energy && (rc = qgt_dev_memcpy_d2h(p->energy_pin, p->energy_d, sizeof(double) * B, cs)) != 0) return rc;
+    if (early && (rc = qgt_dev_event_record(p->ev_copied, cs)) != 0) return rc;
     if (need_status && (rc = qgt_dev_memcpy_d2h(p->status_pin, p->status_d, sizeof(double) * 2 * B, p->stream)) != 0) return rc;
-    if (gerr && (rc = qgt_dev_memcpy_d2h(p->gerr_pin, gerr, sizeof(int), p->stream)) != 0) return rc;
-    if (Q && (rc = qgt_dev_memcpy_d2h(p->Q_pin, p->Q_d, sizeof(double) * 2 * B * Pd * Pd, p->stream)) != 0) return rc;
-    if (grad && (rc = qgt_dev_memcpy_d2h(p->grad_pin, p->grad_d, sizeof(double) * B * Pd, p->stream)) != 0) return rc;
-    if (energy && (rc = qgt_dev_memcpy_d2h(p->energy_pin, p->energy_d, sizeof(double) * B, p->stream)) != 0) return rc;
     if (natgrad && (rc = qgt_dev_memcpy_d2h(p->natgrad_pin, p->natgrad_d, sizeof(double) * B * Pd, p->stream)) != 0) return rc;
-    if ((rc = qgt_dev_stream_sync(p->stream)) != 0) return rc;
+    if (early && (rc = qgt_dev_event_sync(p->ev_copied)) != 0) return rc;
     /* a failed Gram invalidates everything after it: report it first */
-    if (gerr && p->gerr_pin[0])
+    if (gerr && p->gerr_pin[0]) {
+        qgt_dev_stream_sync(p->stream);
         return qgt_set_error(p->gerr_pin[0], "tensor-core Gram reported device status %d", p->gerr_pin[0]);
+    }
+    if (Q) memcpy(Q, p->Q_pin, sizeof(double) * 2 * B * Pd * Pd);
+    if (grad) memcpy(grad, p->grad_pin, sizeof(double) * B * Pd);
+    if (energy) memcpy(energy, p->energy_pin, sizeof(double) * B);
+    if ((rc = qgt_dev_stream_sync(p->stream)) != 0) return rc;
     if (need_status) {
         if (B == 1) {
             /* the graph's blocked solve has no retries: on a non-positive pivot
@@ -2132,9 +2198,6 @@ int qgt_plan_execute_host(qgt_plan_t* p, const double* theta, double* Q, double*
                     return qgt_set_error((int)p->status_pin[2 * b], "cholesky: point %zu not positive definite after lambda retries", b);
         }
     }
-    if (Q) memcpy(Q, p->Q_pin, sizeof(double) * 2 * B * Pd * Pd);
-    if (grad) memcpy(grad, p->grad_pin, sizeof(double) * B * Pd);
-    if (energy) memcpy(energy, p->energy_pin, sizeof(double) * B);
     if (natgrad) memcpy(natgrad, p->natgrad_pin, sizeof(double) * B * Pd);
     return 0;
 }

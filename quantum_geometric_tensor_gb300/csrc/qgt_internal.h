@@ -243,6 +243,7 @@ const char* qgt_dev_error_string(void);
 int qgt_dev_event_create(void** ev);
 int qgt_dev_event_destroy(void* ev);
 int qgt_dev_event_record(void* ev, void* stream);
+int qgt_dev_event_sync(void* ev);
 int qgt_dev_stream_wait_event(void* stream, void* ev);
 int qgt_dev_event_elapsed(void* start, void* end, float* ms);
 
