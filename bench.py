@@ -215,7 +215,6 @@ def run_reference(args, ws, rank):
 def run_gb300(args, ws, rank, local):
     import torch
     import quantum_geometric_tensor_gb300 as Q
-    from oracle import oracle as O
 
     dist = init_dist(ws, local)
     dev = local if ws > 1 else 0
@@ -224,7 +223,7 @@ def run_gb300(args, ws, rank, local):
     workload = WORKLOAD if (nq, nl) == (N_QUBITS, LAYERS) else f"hea{nq}_L{nl}_czring_P{2 * nq * nl}_tfim_natgrad"
     gates = Q.ansatz_gates(nq, nl, ENT)
     P = 2 * nq * nl
-    theta = O.splitmix64_params(SEED + rank, P)
+    theta = Q.seeded_params(SEED + rank, P)
     t0 = time.perf_counter()
     plan = Q.Plan(nq, gates, P, precision=Q.MIXED, lam=LAMBDA, device=dev)
     t_create = time.perf_counter() - t0
@@ -394,12 +393,12 @@ def _line(metric, value, unit, steps, warmup, ms, cfg, extra):
 def run_ragged(args):
     """1024 circuits (qubits U{12..18}, layers U{2..6}, RY/RZ + CNOT ladder), full QGT of each plus a
     32 x 32 Berry map over (first RY, first RZ of qubit 0), one graph launch per batch."""
+    import torch
     import quantum_geometric_tensor_gb300 as Q
-    from oracle import oracle as O
     rng = np.random.default_rng(SEED)
     ns, Ls = rng.integers(12, 19, 1024), rng.integers(2, 7, 1024)
     spec = [(int(n), Q.ansatz_gates(int(n), int(L), "cnot"), 2 * int(n) * int(L)) for n, L in zip(ns, Ls)]
-    thetas = [O.splitmix64_params(5000 + c, s_[2]) for c, s_ in enumerate(spec)]
+    thetas = [Q.seeded_params(5000 + c, s_[2]) for c, s_ in enumerate(spec)]
     tune = args.tune_cache or None
     tuned_before = 0
     if tune and os.path.exists(tune):
@@ -416,11 +415,25 @@ def run_ragged(args):
     info = b.info()
     for _ in range(args.warmup):
         Qs, maps = b.run(thetas)
+        b.run_device()
+    # value: the batch graph on device-resident thetas (CUDA events on the batch's stream);
+    # e2e: the public call with host thetas in and host Q matrices and maps out
+    stream = torch.cuda.ExternalStream(b.stream(), device="cuda:0")
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(0) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            b.run_device()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / args.steps
+        bufs = b.output_buffers()   # host outputs reused across batches, as a training loop would
+        Qs, maps = b.run(thetas, out=bufs)
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            Qs, maps = b.run(thetas)
-        ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+            Qs, maps = b.run(thetas, out=bufs)
+        e2e_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
     errs = []
     for c in (0, 511, 1023):
         n, g, P = spec[c]
@@ -433,7 +446,7 @@ def run_ragged(args):
           {"workload": "ragged1024_q12-18_L2-6_cnot_berry32", "circuits": 1024, "groups": info.num_groups,
            "berry_plans": info.num_berry_plans, "precision": "mixed",
            "plan_configuration": "measured per group (tune cache)" if tune else "defaults"},
-          {"dtype": "c64/fp16-digits/f64", "e2e": {"value": 1024000.0 / ms, "unit": "QGTs/sec",
+          {"dtype": "c64/fp16-digits/f64", "e2e": {"value": 1024000.0 / e2e_ms, "unit": "QGTs/sec", "ms_per_step": e2e_ms,
                                                     "h2d_bytes_per_step": int(sum(len(t) for t in thetas) * 8),
                                                     "d2h_bytes_per_step": int(sum(s_[2] ** 2 * 16 for s_ in spec)
                                                                               + 1024 * 32 * 32 * 8)},
@@ -444,11 +457,10 @@ def run_ragged(args):
 def run_hea26(args):
     """26 qubits, 2 layers RY/RZ + CNOT ladder (P = 104), mixed step against the FP64 GPU step."""
     import quantum_geometric_tensor_gb300 as Q
-    from oracle import oracle as O
     n, L = 26, 2
     g = Q.ansatz_gates(n, L, "cnot")
     P = 2 * n * L
-    th = O.splitmix64_params(26, P)
+    th = Q.seeded_params(26, P)
     with Q.Plan(n, g, P, precision=Q.MIXED) as pm:
         info = pm.info()
         for _ in range(args.warmup):
@@ -491,7 +503,6 @@ def run_learned(args):
     (width 512, rank 16) on 20000 exact metrics generated on the GPU, then PCG iterations on held-out
     points and a 500-step natural-gradient VQE (TFIM ring) against the Cholesky step."""
     import quantum_geometric_tensor_gb300 as Q
-    from oracle import oracle as O
     n, L = 16, 6
     g = Q.ansatz_gates(n, L, "cnot")
     P = 2 * n * L
@@ -512,7 +523,7 @@ def run_learned(args):
         its["cg"].append(Q.pcg_solve(met[k], b, 1e-3, tol=1e-8, max_iter=5000)[1])
         its["jacobi"].append(Q.pcg_solve(met[k], b, 1e-3, d=np.diag(met[k]) + 1e-3, tol=1e-8, max_iter=5000)[1])
         its["learned"].append(Q.pcg_solve(met[k], b, 1e-3, d=d[k], U=U[k], tol=1e-8, max_iter=5000)[1])
-    th0 = O.splitmix64_params(500, P)
+    th0 = Q.seeded_params(500, P)
     vqe = {}
     for name, solver, p_ in (("cholesky", Q.VQE_CHOLESKY, None), ("cg", Q.VQE_CG, None),
                              ("learned", Q.VQE_PCG_LEARNED, pc)):

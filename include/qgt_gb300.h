@@ -242,6 +242,11 @@ int qgt_batch_create(const qgt_circuit_desc_t* circuits, int32_t count, const in
  * Q: their P x P complex QGTs back to back (NULL allowed); berry: count x G x G
  * doubles, map[i][j] at (theta_a, theta_b) = (2 pi i / G, 2 pi j / G) (NULL allowed). */
 int qgt_batch_execute_host(qgt_batch_t* batch, const double* theta, double* Q, double* berry);
+/* the batch's work on the inputs already on the device (the thetas of the last
+ * qgt_batch_execute_host), results left on the device: one graph launch on
+ * qgt_batch_stream(batch), asynchronous (measurement of the device-resident batch) */
+int qgt_batch_execute_device(qgt_batch_t* batch);
+void* qgt_batch_stream(const qgt_batch_t* batch);
 int qgt_batch_get_info(const qgt_batch_t* batch, qgt_batch_info_t* info);
 void qgt_batch_destroy(qgt_batch_t* batch);
 

@@ -119,6 +119,9 @@ def lib() -> C.CDLL:
         L.qgt_batch_create.argtypes = [vp, C.c_int32, vp, C.POINTER(BatchOptions), C.POINTER(vp)]
         L.qgt_batch_execute_host.argtypes = [vp, vp, vp, vp]
         L.qgt_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
+        L.qgt_batch_execute_device.argtypes = [vp]
+        L.qgt_batch_stream.argtypes = [vp]
+        L.qgt_batch_stream.restype = vp
         L.qgt_batch_destroy.argtypes = [vp]
         L.qgt_flux_default_options.argtypes = [C.POINTER(FluxOptions)]
         L.qgt_berry_flux_grid.argtypes = [C.POINTER(CircuitDesc), vp, C.POINTER(FluxOptions), vp, vp]
@@ -178,6 +181,18 @@ def circuit_desc(n: int, gates, num_params: int | None = None):
     d = CircuitDesc(n, len(gates), C.cast(arr, C.POINTER(GateDesc)), P)
     d._keep = arr
     return d
+
+
+def seeded_params(seed: int, count: int) -> np.ndarray:
+    """`count` angles uniform in [0, 2 pi) from a splitmix64 stream started at `seed`: state
+    s_i = seed + i * 0x9E3779B97F4A7C15 (mod 2^64), the splitmix64 finaliser of s_i, its top 53
+    bits as a fraction of 2 pi.  The workloads' seeded parameter vectors."""
+    with np.errstate(over="ignore"):
+        s = np.uint64(seed & ((1 << 64) - 1)) + np.arange(1, count + 1, dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15)
+        z = (s ^ (s >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z ^= z >> np.uint64(31)
+    return 2.0 * np.pi * ((z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0))
 
 
 def ansatz_gates(n: int, layers: int, entangler: str = "cnot"):
@@ -334,17 +349,35 @@ class Batch:
         _check(lib().qgt_batch_get_info(self.h, C.byref(i)), "qgt_batch_get_info")
         return i
 
-    def run(self, thetas):
-        """thetas: one parameter vector per circuit -> (list of P x P complex Q, count x G x G maps or None)."""
+    def output_buffers(self):
+        """Host arrays for run(..., out=): the QGTs back to back (complex128) and the maps (or None)."""
+        return (np.zeros(sum(P * P for P in self.P), dtype=np.complex128),
+                np.zeros((len(self.P), self.G, self.G)) if self.G > 0 else None)
+
+    def run(self, thetas, out=None):
+        """thetas: one parameter vector per circuit -> (list of P x P complex Q, count x G x G maps or None).
+        out: buffers from output_buffers(), reused (the returned matrices are views of them)."""
         th = np.ascontiguousarray(np.concatenate([np.asarray(t, dtype=np.float64).reshape(-1) for t in thetas]))
-        Qflat = np.zeros(sum(P * P for P in self.P), dtype=np.complex128)
-        maps = np.zeros((len(self.P), self.G, self.G)) if self.G > 0 else None
+        Qflat, maps = out if out is not None else self.output_buffers()
+        if Qflat.dtype != np.complex128 or Qflat.size != sum(P * P for P in self.P) or not Qflat.flags.c_contiguous:
+            raise ValueError("out: QGT buffer of the wrong size or type")
+        if self.G > 0 and (maps is None or maps.shape != (len(self.P), self.G, self.G) or maps.dtype != np.float64
+                           or not maps.flags.c_contiguous):
+            raise ValueError("out: map buffer of the wrong shape or type")
         _check(lib().qgt_batch_execute_host(self.h, _ptr(th), _ptr(Qflat), _ptr(maps)), "qgt_batch_execute_host")
         out, at = [], 0
         for P in self.P:
             out.append(Qflat[at:at + P * P].reshape(P, P))
             at += P * P
         return out, maps
+
+    def run_device(self):
+        """The batch on the thetas of the last run(), results left on the device: one asynchronous
+        graph launch on stream() (qgt_batch_execute_device)."""
+        _check(lib().qgt_batch_execute_device(self.h), "qgt_batch_execute_device")
+
+    def stream(self) -> int:
+        return lib().qgt_batch_stream(self.h) or 0
 
     def close(self):
         if getattr(self, "h", None):

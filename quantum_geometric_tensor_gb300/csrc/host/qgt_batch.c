@@ -29,6 +29,7 @@
  * points as separate 2 x 2 QGTs.
  */
 #include <math.h>
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -72,7 +73,8 @@ struct qgt_batch {
     int nstreams;
     void* s[MAX_STREAMS];
     void* ev[MAX_STREAMS + 1];
-    void* graph;
+    void* graph;            /* with the theta uploads and result downloads */
+    void* graph_dev;        /* the same work without them */
     int nodes;
     int64_t device_bytes;
 };
@@ -140,6 +142,7 @@ void qgt_batch_destroy(qgt_batch_t* b)
     if (!b) return;
     if (b->nstreams > 0 && b->s[0]) qgt_dev_stream_sync(b->s[0]);
     qgt_dev_graph_destroy(b->graph);
+    qgt_dev_graph_destroy(b->graph_dev);
     for (int i = 0; i < b->nbp; i++) {
         qgt_plan_destroy(b->bp[i].plan);
         free(b->bp[i].mem);
@@ -154,6 +157,53 @@ void qgt_batch_destroy(qgt_batch_t* b)
     qgt_dev_host_free(b->out_pin);
     free(b->bp); free(b->P); free(b->th_at); free(b->q_at);
     free(b);
+}
+
+/* one graph: fork over the streams, per plan [upload theta ->] step [-> download Q or the map], join */
+static int capture(qgt_batch_t* b, const qgt_circuit_desc_t* circuits, int copies, void** graph)
+{
+    const int K = b->nstreams;
+    int cr = qgt_dev_graph_begin(b->s[0]);
+    if (!cr) cr = qgt_dev_event_record(b->ev[K], b->s[0]);
+    for (int k = 1; k < K && !cr; k++) cr = qgt_dev_stream_wait_event(b->s[k], b->ev[K]);
+    int nodes = 0;
+    for (int i = 0; i < b->nbp && !cr; i++) {
+        bplan_t* bp = &b->bp[i];
+        void* st = b->s[i % K];
+        const size_t pts = (size_t)bp->nmem * bp->per;
+        if (bp->P > 0 && copies)
+            cr = qgt_dev_memcpy_h2d(qgt_plan_dev_theta(bp->plan), b->th_pin + bp->th_off,
+                                    sizeof(double) * pts * (size_t)bp->P, st);
+        if (!cr) cr = qgt_plan_enqueue_step(bp->plan, st);
+        if (!cr && bp->berry && bp->compact) {
+            int64_t pstride = 0;
+            int32_t f64 = 0;
+            const void* V = qgt_plan_dev_V(bp->plan, &pstride, &f64);
+            const int npair = 10 * bp->nmem;
+            const int64_t N = (int64_t)1 << circuits[bp->mem[0]].num_qubits;
+            cr = qgt_dev_overlaps(V, f64, N, bp->off_d, bp->off_d + npair, npair, bp->nchunk, bp->part_d, st);
+            if (!cr) cr = qgt_dev_berry_closed(bp->part_d, bp->nchunk, bp->nmem, b->G, bp->maps_d, st);
+            if (!cr && copies)
+                cr = qgt_dev_memcpy_d2h(b->out_pin + bp->out_off, bp->maps_d,
+                                        sizeof(double) * (size_t)bp->nmem * b->G * b->G, st);
+            nodes += 2;
+        } else if (!cr && bp->Pd > 0 && copies) {
+            cr = qgt_dev_memcpy_d2h(b->out_pin + bp->out_off, qgt_plan_dev_Q(bp->plan),
+                                    sizeof(double) * pts * 2 * (size_t)bp->Pd * bp->Pd, st);
+        }
+        nodes += qgt_plan_launches(bp->plan) + (copies ? 2 : 0);
+    }
+    for (int k = 1; k < K && !cr; k++) {
+        cr = qgt_dev_event_record(b->ev[k], b->s[k]);
+        if (!cr) cr = qgt_dev_stream_wait_event(b->s[0], b->ev[k]);
+    }
+    void* exec = NULL;
+    int re = qgt_dev_graph_end(b->s[0], &exec);
+    if (cr) { qgt_dev_graph_destroy(exec); return cr; }
+    if (re) return re;
+    *graph = exec;
+    if (copies) b->nodes = nodes;
+    return 0;
 }
 
 int qgt_batch_create(const qgt_circuit_desc_t* circuits, int32_t count, const int32_t* berry_params,
@@ -335,53 +385,67 @@ int qgt_batch_create(const qgt_circuit_desc_t* circuits, int32_t count, const in
         if ((rc = qgt_dev_stream_create(&b->s[k])) != 0) goto fail;
     for (int k = 0; k <= b->nstreams; k++)
         if ((rc = qgt_dev_event_create(&b->ev[k])) != 0) goto fail;
-    /* one graph: fork over the streams, per plan upload theta -> step -> download Q, join */
-    {
-        const int K = b->nstreams;
-        int cr = qgt_dev_graph_begin(b->s[0]);
-        if (!cr) cr = qgt_dev_event_record(b->ev[K], b->s[0]);
-        for (int k = 1; k < K && !cr; k++) cr = qgt_dev_stream_wait_event(b->s[k], b->ev[K]);
-        for (int i = 0; i < b->nbp && !cr; i++) {
-            bplan_t* bp = &b->bp[i];
-            void* st = b->s[i % K];
-            const size_t pts = (size_t)bp->nmem * bp->per;
-            if (bp->P > 0)
-                cr = qgt_dev_memcpy_h2d(qgt_plan_dev_theta(bp->plan), b->th_pin + bp->th_off,
-                                        sizeof(double) * pts * (size_t)bp->P, st);
-            if (!cr) cr = qgt_plan_enqueue_step(bp->plan, st);
-            if (!cr && bp->berry && bp->compact) {
-                int64_t pstride = 0;
-                int32_t f64 = 0;
-                const void* V = qgt_plan_dev_V(bp->plan, &pstride, &f64);
-                const int npair = 10 * bp->nmem;
-                const int64_t N = (int64_t)1 << circuits[bp->mem[0]].num_qubits;
-                cr = qgt_dev_overlaps(V, f64, N, bp->off_d, bp->off_d + npair, npair, bp->nchunk, bp->part_d, st);
-                if (!cr) cr = qgt_dev_berry_closed(bp->part_d, bp->nchunk, bp->nmem, b->G, bp->maps_d, st);
-                if (!cr)
-                    cr = qgt_dev_memcpy_d2h(b->out_pin + bp->out_off, bp->maps_d,
-                                            sizeof(double) * (size_t)bp->nmem * b->G * b->G, st);
-                b->nodes += 2;
-            } else if (!cr && bp->Pd > 0) {
-                cr = qgt_dev_memcpy_d2h(b->out_pin + bp->out_off, qgt_plan_dev_Q(bp->plan),
-                                        sizeof(double) * pts * 2 * (size_t)bp->Pd * bp->Pd, st);
-            }
-            b->nodes += qgt_plan_launches(bp->plan) + 2;
-        }
-        for (int k = 1; k < K && !cr; k++) {
-            cr = qgt_dev_event_record(b->ev[k], b->s[k]);
-            if (!cr) cr = qgt_dev_stream_wait_event(b->s[0], b->ev[k]);
-        }
-        void* exec = NULL;
-        int re = qgt_dev_graph_end(b->s[0], &exec);
-        if (cr) { qgt_dev_graph_destroy(exec); rc = cr; goto fail; }
-        if (re) { rc = re; goto fail; }
-        b->graph = exec;
-    }
+    /* two graphs: the batch with its copies (execute_host) and the same work on the device-resident
+     * inputs and outputs alone (execute_device) */
+    if ((rc = capture(b, circuits, 1, &b->graph)) != 0) goto fail;
+    if ((rc = capture(b, circuits, 0, &b->graph_dev)) != 0) goto fail;
     *out = b;
     return 0;
 fail:
     qgt_batch_destroy(b);
     return rc ? rc : qgt_set_error(E_INVAL, "qgt_batch_create failed");
+}
+
+/* host copies of a batch's results, cut into chunks that a few threads take in turn */
+typedef struct {
+    void* dst;
+    const void* src;
+    size_t n;
+} ucopy_t;
+typedef struct {
+    ucopy_t* t;
+    int n, cap;
+    int next;   /* next chunk to take (atomic) */
+} unpack_t;
+
+#define UNPACK_CHUNK ((size_t)4 << 20)
+#define UNPACK_THREADS 8
+
+static int unpack_add(unpack_t* u, void* dst, const void* src, size_t n)
+{
+    for (size_t at = 0; at < n; at += UNPACK_CHUNK) {
+        if (u->n == u->cap) {
+            const int nc = u->cap ? 2 * u->cap : 1024;
+            ucopy_t* t = (ucopy_t*)realloc(u->t, sizeof(ucopy_t) * (size_t)nc);
+            if (!t) return qgt_set_error(E_NOMEM, "qgt_batch_execute_host: out of host memory");
+            u->t = t;
+            u->cap = nc;
+        }
+        const size_t k = n - at < UNPACK_CHUNK ? n - at : UNPACK_CHUNK;
+        u->t[u->n++] = (ucopy_t){(char*)dst + at, (const char*)src + at, k};
+    }
+    return 0;
+}
+
+static void* unpack_worker(void* arg)
+{
+    unpack_t* u = (unpack_t*)arg;
+    for (;;) {
+        const int i = __atomic_fetch_add(&u->next, 1, __ATOMIC_RELAXED);
+        if (i >= u->n) return NULL;
+        memcpy(u->t[i].dst, u->t[i].src, u->t[i].n);
+    }
+}
+
+static void unpack_run(unpack_t* u)
+{
+    pthread_t th[UNPACK_THREADS - 1];
+    int started[UNPACK_THREADS - 1] = {0};
+    const int nt = u->n < UNPACK_THREADS ? u->n : UNPACK_THREADS;
+    for (int k = 0; k + 1 < nt; k++) started[k] = pthread_create(&th[k], NULL, unpack_worker, u) == 0;
+    unpack_worker(u);   /* the calling thread takes chunks too, so every chunk is copied */
+    for (int k = 0; k + 1 < nt; k++)
+        if (started[k]) pthread_join(th[k], NULL);
 }
 
 int qgt_batch_execute_host(qgt_batch_t* b, const double* theta, double* Q, double* berry)
@@ -418,21 +482,26 @@ int qgt_batch_execute_host(qgt_batch_t* b, const double* theta, double* Q, doubl
         int st = qgt_plan_device_status(b->bp[i].plan, NULL);
         if (st) return qgt_set_error(st, "qgt_batch_execute_host: plan %d reported device status %d", i, st);
     }
+    /* results from the pinned staging buffer into the caller's arrays: contiguous blocks are copied
+     * in chunks by a few host threads (one thread copies ~10-20 GB/s, the batch returns ~300 MB);
+     * the per-point Berry maps of non-compact plans are gathered by the calling thread */
     const size_t G = (size_t)b->G;
-    for (int i = 0; i < b->nbp; i++) {
+    unpack_t u = {NULL, 0, 0, 0};
+    int rc2 = 0;
+    for (int i = 0; i < b->nbp && !rc2; i++) {
         const bplan_t* bp = &b->bp[i];
         const size_t blk = 2 * (size_t)bp->Pd * bp->Pd;
-        for (int m = 0; m < bp->nmem; m++) {
+        for (int m = 0; m < bp->nmem && !rc2; m++) {
             const int c = bp->mem[m];
             const double* src = b->out_pin + bp->out_off + (size_t)m * bp->per * blk;
             if (!bp->berry) {
-                if (Q) memcpy(Q + b->q_at[c], src, sizeof(double) * blk);
+                if (Q) rc2 = unpack_add(&u, Q + b->q_at[c], src, sizeof(double) * blk);
                 continue;
             }
             if (!berry) continue;
             double* map = berry + (size_t)c * G * G;
             if (bp->compact) {   /* maps formed on the device from the closed form */
-                memcpy(map, b->out_pin + bp->out_off + (size_t)m * G * G, sizeof(double) * G * G);
+                rc2 = unpack_add(&u, map, b->out_pin + bp->out_off + (size_t)m * G * G, sizeof(double) * G * G);
                 continue;
             }
             /* Omega_ab = Im Q_01 of the 2 x 2 block (imaginary part at double index 3) */
@@ -440,7 +509,20 @@ int qgt_batch_execute_host(qgt_batch_t* b, const double* theta, double* Q, doubl
                 for (size_t y = 0; y < G; y++) map[x * G + y] = src[(x * G + y) * blk + 3];
         }
     }
-    return 0;
+    if (!rc2) unpack_run(&u);
+    free(u.t);
+    return rc2;
+}
+
+int qgt_batch_execute_device(qgt_batch_t* b)
+{
+    if (!b) return qgt_set_error(E_INVAL, "qgt_batch_execute_device: NULL batch");
+    return qgt_dev_graph_launch(b->graph_dev, b->s[0]);
+}
+
+void* qgt_batch_stream(const qgt_batch_t* b)
+{
+    return b ? b->s[0] : NULL;
 }
 
 int qgt_batch_get_info(const qgt_batch_t* b, qgt_batch_info_t* info)

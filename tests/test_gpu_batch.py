@@ -93,6 +93,24 @@ def test_ragged_batch_qgt_and_berry_maps(Q, orc, prec):
         assert np.abs(maps[c] - ref.reshape(G, G)).max() < tm, (c, n, L, pairs[c])
 
 
+def test_device_resident_batch_launch(Q):
+    """qgt_batch_execute_device repeats the batch on the thetas of the last execute_host without the
+    copies; the next execute_host returns the same results (same inputs, deterministic kernels)."""
+    import torch
+    circs, thetas, pairs = ragged(7, 14, 4, 9, 3)
+    spec = [(n, Q.ansatz_gates(n, L, "cnot"), 2 * n * L) for (n, L) in circs]
+    with Q.Batch(spec, pairs, precision=Q.MIXED, grid=8) as b:
+        Q1, m1 = b.run(thetas)
+        assert b.stream() != 0
+        for _ in range(3):
+            b.run_device()
+        torch.cuda.synchronize()
+        Q2, m2 = b.run(thetas, out=b.output_buffers())
+    for a, c in zip(Q1, Q2):
+        assert np.array_equal(a, c)
+    assert np.array_equal(m1, m2)
+
+
 def test_berry_map_shared_parameter_full_lattice(Q, orc):
     """A parameter driving two gates: every lattice point is evaluated."""
     n = 5
