@@ -329,10 +329,10 @@ __global__ void __launch_bounds__(CB* CB) chol32_solve_kernel(const float* __res
             for (int k = r0 + CB + wp; k < P; k += CB) s += L[(int64_t)k * P + r0 + lane] * y[k];
         part[wp][lane] = s;
         __syncthreads();
-        if (wp == 0) {
-            float u = 0.f;
-            for (int q = 0; q < CB; q++) u += part[q][lane];
-            t[lane] = (r0 + lane < P) ? y[r0 + lane] - u : 0.f;
+        {   // u[c] = sum over warps q of part[q][c]: warp wp sums column c = wp (a shuffle tree)
+            float u = part[lane][wp];
+            for (int o = 16; o > 0; o >>= 1) u += __shfl_xor_sync(0xffffffffu, u, o);
+            if (lane == 0) t[wp] = (r0 + wp < P) ? y[r0 + wp] - u : 0.f;
         }
         __syncthreads();
         // d_blk[c] = sum_r W[r][c] t[r] (W^T t): warp wp computes column c = wp
@@ -428,13 +428,11 @@ extern "C" int qgt_dev_cholesky_refined(const double* A, int cplx, const double*
         }
         rc = qgt_dev_last_error();
     }
-    if (!rc) {
-        chol32_solve_kernel<<<1, CB * CB, 0, s>>>(L, W, b, x, P, 0, status, conv);
-        rc = qgt_dev_last_error();
-    }
-    for (int it = 0; it < CHOL_REFINE_STEPS && !rc; it++) {
-        chol_residual_kernel<<<(unsigned)((P + 7) / 8), 256, 0, s>>>(A64, b, x, r, P, conv);
-        chol32_solve_kernel<<<1, CB * CB, 0, s>>>(L, W, r, x, P, it == CHOL_REFINE_STEPS - 1 ? 2 : 1, status, conv);
+    for (int it = -1; it < CHOL_REFINE_STEPS && !rc; it++) {
+        const int mode = it < 0 ? 0 : (it == CHOL_REFINE_STEPS - 1 ? 2 : 1);
+        const double* rhs = it < 0 ? b : r;
+        if (it >= 0) chol_residual_kernel<<<(unsigned)((P + 7) / 8), 256, 0, s>>>(A64, b, x, r, P, conv);
+        chol32_solve_kernel<<<1, CB * CB, 0, s>>>(L, W, rhs, x, P, mode, status, conv);
         rc = qgt_dev_last_error();
     }
     return rc;

@@ -32,9 +32,11 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-@pytest.mark.parametrize("n,L,ent", [(14, 2, "cz"), (16, 3, "cnot"), (13, 3, "cz"), (14, 19, "cnot")])
+@pytest.mark.parametrize("n,L,ent", [(14, 2, "cz"), (16, 3, "cnot"), (13, 3, "cz"), (14, 19, "cnot"),
+                                     (10, 16, "cz"), (10, 15, "cnot")])
 def test_refined_step_is_fp64_accurate(Q, n, L, ent):
-    """P = 56, 96, 78 (a partial last block of the 32-wide blocked factor) and 532 (17 blocks)."""
+    """P = 56, 96, 78 (a partial last block of the 32-wide blocked factor), 532 (17 blocks), 320
+    (the headline's size) and 300 (10 blocks, the last partial)."""
     gates = Q.ansatz_gates(n, L, ent)
     P = 2 * n * L
     th = O.splitmix64_params(300 + n, P)
