@@ -217,24 +217,34 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
         qgt_set_error(-1, "jit: unsupported program (RB %d, WB %d)", RB, WB);
         return NULL;
     }
-    /* three parts: the kernel's head (hb), its body (bb: entry points, program, store), and, once the
-     * body has registered its coefficient slots, the slot table and the staging code between them */
-    sbuf_t hsb = {NULL, 0, 0, 0}, bsb = {NULL, 0, 0, 0}, osb = {NULL, 0, 0, 0};
+    /* four parts: the kernel's head (hsb), its entry points (lsb: each loads its tile), its program
+     * and store (bsb), and, once the program has registered its coefficient slots, the slot table
+     * and the staging code.  The staging runs after the tile loads are issued, so that the loads'
+     * latency overlaps the staging's own global reads and barriers. */
+    sbuf_t hsb = {NULL, 0, 0, 0}, lsb = {NULL, 0, 0, 0}, bsb = {NULL, 0, 0, 0}, osb = {NULL, 0, 0, 0};
+    sbuf_t tsb = {NULL, 0, 0, 0};   /* file-scope constant tables of the program (generator lookups) */
+    sbuf_t* tb_ = &tsb;
     slots_t slots = {0, 0, NULL, NULL, NULL, 0};
     slots_t* t = &slots;
     hsb.cap = 1 << 14;
+    lsb.cap = 1 << 14;
     bsb.cap = 1 << 16;
     osb.cap = 1 << 16;
+    tsb.cap = 1 << 12;
     hsb.s = (char*)malloc(hsb.cap);
+    lsb.s = (char*)malloc(lsb.cap);
     bsb.s = (char*)malloc(bsb.cap);
     osb.s = (char*)malloc(osb.cap);
-    if (!hsb.s || !bsb.s || !osb.s) {
+    tsb.s = (char*)malloc(tsb.cap);
+    if (!hsb.s || !lsb.s || !bsb.s || !osb.s || !tsb.s) {
         free(hsb.s);
+        free(lsb.s);
         free(bsb.s);
         free(osb.s);
+        free(tsb.s);
         return NULL;
     }
-    hsb.s[0] = bsb.s[0] = osb.s[0] = 0;
+    hsb.s[0] = lsb.s[0] = bsb.s[0] = osb.s[0] = tsb.s[0] = 0;
     sbuf_t* b = &hsb;
     const int nthreads = 32 << WB;
     /* CTAs per SM the registers must allow: 512-thread 14-qubit tiles 1, 1024-thread 14-qubit tiles 1
@@ -272,8 +282,8 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
             sb_printf(b, " if ((threadIdx.x >> %d) & 1) o |= %uu;", lb - 5, 1u << d->l2p[lb]);
         sb_printf(b, " supper[threadIdx.x] = o; }\n    __syncthreads();\n");
     }
-    b = &bsb;
-    /* entry points */
+    b = &lsb;
+    /* entry points: the tile loads of each start, then the coefficient staging (STG_) */
     sb_printf(b, "    switch (start) {\n");
     for (int i = 0; i < d->nstarts; i++) sb_printf(b, "    case %d: goto S_%d;\n", d->starts[i], d->starts[i]);
     sb_printf(b, "    default: return;\n    }\n");
@@ -287,13 +297,14 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
             sb_printf(b, "    if (flags & %d) {\n", QENT_SRC_ZERO);
             for (int j = 0; j < NR; j++)
                 sb_printf(b, "        v[%d] = make_float2((pthr + %uu) == 0u ? 1.f : 0.f, 0.f);\n", j, pconst(d, &L, j));
-            sb_printf(b, "        goto B_%d;\n    }\n", a);
+            sb_printf(b, "        goto STG_;\n    }\n");
         }
         sb_printf(b, "    {\n        const T* src = Vp + (long long)e[%d] * N;\n",
                   (int)(offsetof(qgt_dev_entry_t, src_row) / 4));
         for (int j = 0; j < NR; j++) sb_printf(b, "        v[%d] = src[pthr + %uu];\n", j, pconst(d, &L, j));
-        sb_printf(b, "    }\n    goto B_%d;\n", a);
+        sb_printf(b, "    }\n    goto STG_;\n");
     }
+    b = &bsb;
     /* the program */
     lay_t cur;
     layout_of(d, d->prog[0].seg, &cur);
@@ -350,17 +361,24 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
                 sb_printf(b, " f0r[%d] = m[0]; f0i[%d] = m[1]; f1r[%d] = sg * m[6]; f1i[%d] = sg * m[7]; }\n", i, i, i, i);
             }
             sb_printf(b, "      diag_run_apply<NR, RB, T, R>(v, cr, ci, f0r, f0i, f1r, f1i, %uu);\n", (unsigned)o->slot);
-            int nzg = 0;
-            for (int u = z0 + nz; u <= pc + cnt; u++) nzg += d->prog[u].kind == Q2_ZGEN;
-            if (nzg) {
-                sb_printf(b, "      switch (spawn) {\n");
-                for (int u = z0 + nz; u <= pc + cnt; u++) {
+            /* (-i/2) Z of a rotation spawned inside the run, after it: the spawning entry looks up the
+             * rotation's role and qubit in a constant table over the run's op range (one code path
+             * per run instead of one per rotation) */
+            int zlo = -1, zhi = -1;
+            for (int u = z0 + nz; u <= pc + cnt; u++)
+                if (d->prog[u].kind == Q2_ZGEN) { if (zlo < 0) zlo = u; zhi = u; }
+            if (zlo >= 0) {
+                sb_printf(tb_, "static __constant__ int zg_%s_%d[%d] = {", d->kname, pc, 2 * (zhi - zlo + 1));
+                for (int u = zlo; u <= zhi; u++) {
                     const qgt_dev_op2_t* so = &d->prog[u];
-                    if (so->kind != Q2_ZGEN) continue;
-                    sb_printf(b, "      case %d: zgen_apply<NR, T, R>(v, role_mask<NR>(%d, %d, lane, warp, base)); break;\n",
-                              u, (int)so->ra, (int)so->q);
+                    if (so->kind == Q2_ZGEN) sb_printf(tb_, "%s%d, %d", u > zlo ? ", " : "", (int)so->ra, (int)so->q);
+                    else sb_printf(tb_, "%s-1, 0", u > zlo ? ", " : "");
                 }
-                sb_printf(b, "      default: break;\n      }\n");
+                sb_printf(tb_, "};\n");
+                sb_printf(b, "      if ((unsigned)(spawn - %d) <= %uu) { const int zr = zg_%s_%d[2 * (spawn - %d)], "
+                             "zq = zg_%s_%d[2 * (spawn - %d) + 1];\n"
+                             "        if (zr >= 0) zgen_apply<NR, T, R>(v, role_mask<NR>(zr, zq, lane, warp, base)); }\n",
+                          zlo, (unsigned)(zhi - zlo), d->kname, pc, zlo, d->kname, pc, zlo);
             }
             sb_printf(b, "    }\n");
             pc += cnt;
@@ -431,8 +449,10 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
             break;
         default:
             free(hsb.s);
+            free(lsb.s);
             free(bsb.s);
             free(osb.s);
+            free(tsb.s);
             free(t->coef);
             free(t->pc);
             free(t->gen);
@@ -449,49 +469,64 @@ char* qgt_jit_pass_source(const qgt_jit_pass_desc_t* d)
     sb_printf(b, "    {\n      T* dst = Vp + (long long)e[%d] * N;\n", (int)(offsetof(qgt_dev_entry_t, dst_row) / 4));
     sb_printf(b, "      if (flags & %d) {\n", QENT_STORE_V);
     for (int j = 0; j < NR; j++) sb_printf(b, "        dst[pthr + %uu] = v[%d];\n", pconst(d, &cur, j), j);
+    /* row maximum of |v|: the largest squared magnitude, one square root per thread (sqrtf is
+     * correctly rounded, hence monotonic: the same value as the largest of the roots) */
     sb_printf(b, "      }\n      if (flags & %d) {\n        float vmax = 0.f;\n#pragma unroll\n"
-                 "        for (int j = 0; j < NR; j++) vmax = fmaxf(vmax, sqrtf((float)(v[j].x * v[j].x + v[j].y * v[j].y)));\n"
-                 "        __shared__ float red[%d];\n"
+                 "        for (int j = 0; j < NR; j++) vmax = fmaxf(vmax, (float)(v[j].x * v[j].x + v[j].y * v[j].y));\n"
+                 "        vmax = sqrtf(vmax);\n"
                  "        for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));\n"
-                 "        if (lane == 0) red[warp] = vmax;\n        __syncthreads();\n"
-                 "        if (threadIdx.x == 0) {\n          float mx = 0.f;\n"
-                 "          for (int w = 0; w < %d; w++) mx = fmaxf(mx, red[w]);\n"
-                 "          atomicMax(rowmax + (long long)blockIdx.z * rowmax_stride + e[%d], __float_as_uint(mx));\n"
-                 "        }\n      }\n    }\n}\n",
-              QENT_ROWMAX, 1 << WB, 1 << WB, (int)(offsetof(qgt_dev_entry_t, dst_row) / 4));
-    /* assemble: slot table, head, staging of the slots (with the spawn folds), body */
+                 "        if (lane == 0) atomicMax(rowmax + (long long)blockIdx.z * rowmax_stride + e[%d], __float_as_uint(vmax));\n"
+                 "      }\n    }\n}\n",
+              QENT_ROWMAX, (int)(offsetof(qgt_dev_entry_t, dst_row) / 4));
+    /* assemble: slot table and program tables, head, entry points (tile loads), staging of the
+     * slots (with the spawn folds), dispatch to the start, program */
     b = &osb;
     const int ns = t->n;
     sb_printf(b, "#define LDS8(m, s) { const float4 a_ = *reinterpret_cast<const float4*>(csm + 8 * (s)); "
                  "const float4 b_ = *reinterpret_cast<const float4*>(csm + 8 * (s) + 4); "
                  "m[0] = a_.x; m[1] = a_.y; m[2] = a_.z; m[3] = a_.w; m[4] = b_.x; m[5] = b_.y; m[6] = b_.z; m[7] = b_.w; }\n");
     if (ns > 0) {
-        sb_printf(b, "static __device__ const int qslot_%s[%d] = {", d->kname, ns);
+        sb_printf(b, "static __constant__ int qslot_%s[%d] = {", d->kname, ns);
         for (int i = 0; i < ns; i++) sb_printf(b, "%s%d", i ? ", " : "", t->coef[i]);
         sb_printf(b, "};\n");
     }
+    sb_printf(b, "%s", tsb.s ? tsb.s : "");
     sb_printf(b, "%s", hsb.s ? hsb.s : "");
+    if (ns > 0) sb_printf(b, "    __shared__ __align__(16) float csm[%d];\n", 8 * ns);
+    else sb_printf(b, "    const float* csm = ct;\n    (void)csm;\n");
+    sb_printf(b, "%s", lsb.s ? lsb.s : "");
+    sb_printf(b, "STG_:\n");
     if (ns > 0) {
-        sb_printf(b, "    __shared__ __align__(16) float csm[%d];\n", 8 * ns);
-        sb_printf(b, "    for (int i = threadIdx.x; i < %d; i += %d) csm[i] = __ldg(ct + 8 * qslot_%s[i >> 3] + (i & 7));\n",
-                  8 * ns, nthreads, d->kname);
-        sb_printf(b, "    __syncthreads();\n");
+        /* the slot whose gate this entry's derivative spawns at (fs, generator fg) is written by
+         * thread 0 with the generator folded in; every other slot is copied as is; one barrier */
         int nf = 0;
         for (int i = 0; i < ns; i++) nf += t->gen[i] != QGEN_NONE;
         if (nf) {
-            sb_printf(b, "    if (threadIdx.x == 0) {\n      switch (spawn) {\n");
+            sb_printf(b, "    int fs = -1, fg = 0;\n    switch (spawn) {\n");
             for (int i = 0; i < ns; i++)
-                if (t->gen[i] != QGEN_NONE)
-                    sb_printf(b, "      case %d: fold_gen(csm + %d, %d); break;\n", t->pc[i], 8 * i, (int)t->gen[i]);
-            sb_printf(b, "      default: break;\n      }\n    }\n    __syncthreads();\n");
+                if (t->gen[i] != QGEN_NONE) sb_printf(b, "    case %d: fs = %d; fg = %d; break;\n", t->pc[i], i, (int)t->gen[i]);
+            sb_printf(b, "    default: break;\n    }\n");
+            sb_printf(b, "    for (int i = threadIdx.x; i < %d; i += %d) if ((i >> 3) != fs) csm[i] = __ldg(ct + 8 * qslot_%s[i >> 3] + (i & 7));\n",
+                      8 * ns, nthreads, d->kname);
+            sb_printf(b, "    if (fs >= 0 && threadIdx.x == 0) {\n      float fm[8];\n"
+                         "      for (int k = 0; k < 8; k++) fm[k] = __ldg(ct + 8 * qslot_%s[fs] + k);\n"
+                         "      fold_gen(fm, fg);\n      for (int k = 0; k < 8; k++) csm[8 * fs + k] = fm[k];\n    }\n",
+                      d->kname);
+        } else {
+            sb_printf(b, "    for (int i = threadIdx.x; i < %d; i += %d) csm[i] = __ldg(ct + 8 * qslot_%s[i >> 3] + (i & 7));\n",
+                      8 * ns, nthreads, d->kname);
         }
-    } else {
-        sb_printf(b, "    const float* csm = ct;\n    (void)csm;\n");
+        sb_printf(b, "    __syncthreads();\n");
     }
+    sb_printf(b, "    switch (start) {\n");
+    for (int i = 0; i < d->nstarts; i++) sb_printf(b, "    case %d: goto B_%d;\n", d->starts[i], d->starts[i]);
+    sb_printf(b, "    default: return;\n    }\n");
     sb_printf(b, "%s", bsb.s ? bsb.s : "");
-    const int err = hsb.err || bsb.err || osb.err || t->err;
+    const int err = hsb.err || lsb.err || bsb.err || osb.err || tsb.err || t->err;
     free(hsb.s);
+    free(lsb.s);
     free(bsb.s);
+    free(tsb.s);
     free(t->coef);
     free(t->pc);
     free(t->gen);
