@@ -72,3 +72,27 @@ def test_sixteen_amplitude_tile_sources(Q, tmp_path, tile, bounds):
     k, s = check(Q, n, Q.ansatz_gates(n, L, "cz"), 2 * n * L, tmp_path, tile_bits=tile, thread_amps=16)
     srcs = [p.read_text() for p in tmp_path.iterdir()]
     assert k == len(srcs) and all(bounds in x for x in srcs)
+
+
+def test_prologue_order_and_tables(Q, tmp_path):
+    """Generated kernels issue the tile loads of every entry point before the coefficient staging
+    (so the loads overlap the staging's reads and its barrier), stage behind one barrier, look up
+    the slot and generator tables in constant memory, and end without a CTA-wide barrier (the row
+    maximum is one atomicMax per warp)."""
+    n, L = 16, 3
+    check(Q, n, Q.ansatz_gates(n, L, "cz"), 2 * n * L, tmp_path, compile=0)
+    srcs = {p.name: p.read_text() for p in tmp_path.iterdir()}
+    assert srcs
+    for name, src in srcs.items():
+        body = src[src.index("__global__"):]
+        assert "static __device__ const int qslot_" not in src, name
+        assert "static __constant__ int qslot_" in src, name
+        stg = body.index("STG_:")
+        loads = [i for i in range(len(body)) if body.startswith("const T* src = Vp", i)]
+        assert loads and max(loads) < stg, name
+        dispatch = body.index("switch (start)", stg)
+        assert body[stg:dispatch].count("__syncthreads()") == 1, name
+        tail = body[body.rindex("if (flags & "):]
+        assert "__syncthreads" not in tail and "atomicMax" in tail, name
+        if "zgen_apply" in body:
+            assert "static __constant__ int zg_" in src, name
