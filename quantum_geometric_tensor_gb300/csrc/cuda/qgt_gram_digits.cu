@@ -136,6 +136,15 @@ static __device__ __forceinline__ void tma_3d(uint32_t dst, const CUtensorMap* m
         : "memory");
 }
 
+// two half2 (four consecutive k of one row) as one 8-byte shared store
+static __device__ __forceinline__ void st_h4(uint8_t* p, __half2 a, __half2 b)
+{
+    uint2 u;
+    u.x = *reinterpret_cast<const uint32_t*>(&a);
+    u.y = *reinterpret_cast<const uint32_t*>(&b);
+    *reinterpret_cast<uint2*>(p) = u;
+}
+
 // K-major SWIZZLE_32B operand: rows of 32 B (16 fp16), 8-row groups 256 B apart
 static __device__ __forceinline__ uint64_t desc_sw32(uint32_t saddr)
 {
@@ -356,19 +365,19 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
     } else if (warp >= 2) {
         // ---------- converters: complex64 -> {Re D, Re l1, Re l2, Im D, Im l1, Im l2} ----------
         const int cw = warp - 2;
-        // lane -> (row r = 4 cw + 32 i + lane / 8, amplitude pair kp, kp + 1): one 16-byte load of
-        // (re, im, re, im), then 32-bit stores of half2 pairs into the six planes
-        const int sub = lane >> 3, kp = (lane & 7) * 2;
+        // lane -> (row r = 8 cw + 64 i + lane / 4, amplitudes kq .. kq + 3): two 16-byte loads of
+        // (re, im, re, im), then one 8-byte store of two half2 pairs into each plane
+        const int sub = lane >> 2, kq = (lane & 3) * 4;
         for (int kt = 0; kt < nk; kt++) {
             const int rs = kt % DG_RAW_STAGES, ps = kt % DG_PL_STAGES;
             bool ok = bar_wait(stall ? smem_u32(&never_bar) : smem_u32(&raw_full[rs]), (kt / DG_RAW_STAGES) & 1,
                                deadline);
             const uint8_t* rawst = raw_base + rs * 2 * DG_RAW_BYTES;
             uint8_t* plst = pl_base + ps * DG_PL_STAGE;
-            constexpr int NIT = 128 / (4 * DG_CONV_WARPS);
+            constexpr int NIT = 128 / (8 * DG_CONV_WARPS);
             // all of the k-step's raw values first (independent shared loads, issued while the plane
             // stage may still be in use by the MMAs), then the digit planes
-            float4 q[2][NIT];
+            float4 q[2][NIT][2];
             float iuv[2][NIT];
             if (ok) {
 #pragma unroll
@@ -377,12 +386,14 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
                     const int rlim = (diag || b == 1) ? rbB : 128;
 #pragma unroll
                     for (int it = 0; it < NIT; it++) {
-                        const int r = 4 * cw + 4 * DG_CONV_WARPS * it + sub;
-                        if (b < nblk && 4 * cw + 4 * DG_CONV_WARPS * it < rlim) {
-                            q[b][it] = *reinterpret_cast<const float4*>(raw + r * 32 + 2 * kp);
+                        // rlim is a multiple of 16, so a group of 8 rows is all below it or all above
+                        const int rr = 8 * cw + 8 * DG_CONV_WARPS * it, r = rr + sub;
+                        if (b < nblk && rr < rlim) {
+                            q[b][it][0] = *reinterpret_cast<const float4*>(raw + r * 32 + 2 * kq);
+                            q[b][it][1] = *reinterpret_cast<const float4*>(raw + r * 32 + 2 * kq + 4);
                             iuv[b][it] = inv_u[b][r];
                         } else {
-                            q[b][it] = make_float4(0.f, 0.f, 0.f, 0.f);
+                            q[b][it][0] = q[b][it][1] = make_float4(0.f, 0.f, 0.f, 0.f);
                             iuv[b][it] = 0.f;
                         }
                     }
@@ -404,33 +415,37 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
                 const int rlim = blay ? rbB : 128;
 #pragma unroll
                 for (int it = 0; it < NIT; it++) {
-                    const int rr = 4 * cw + 4 * DG_CONV_WARPS * it;
+                    const int rr = 8 * cw + 8 * DG_CONV_WARPS * it;
                     if (rr >= rlim) break;   // warp-uniform (rr depends on the warp only)
                     const int r = rr + sub;
-                    const float4 qq = q[b][it];
                     const float iu = iuv[b][it];
-                    // SWIZZLE_32B: 16-byte chunk (k / 8) xor bit 2 of the row; kp, kp + 1 share a chunk
-                    const int off = r * 32 + ((((kp >> 3) ^ (r >> 2)) & 1) << 4) + (kp & 7) * 2;
+                    // SWIZZLE_32B: 16-byte chunk (k / 8) xor bit 2 of the row; kq .. kq + 3 share a chunk
+                    const int off = r * 32 + ((((kq >> 3) ^ (r >> 2)) & 1) << 4) + (kq & 7) * 2;
 #pragma unroll
                     for (int c = 0; c < 2; c++) {   // 0: real parts, 1: imaginary parts
-                        const float x0 = (c ? qq.y : qq.x) * iu, x1 = (c ? qq.w : qq.z) * iu;
-                        const float d0 = rintf(x0), d1 = rintf(x1);
-                        const float l0 = x0 - d0, l1 = x1 - d1;
-                        const __half2 h1 = __floats2half2_rn(l0, l1);
-                        const float2 f1 = __half22float2(h1);
-                        const __half2 h2 = __floats2half2_rn(l0 - f1.x, l1 - f1.y);
-                        const __half2 hd = __floats2half2_rn(d0, d1);
+                        __half2 hd[2], h1[2], h2[2];
+#pragma unroll
+                        for (int h = 0; h < 2; h++) {
+                            const float4 qq = q[b][it][h];
+                            const float x0 = (c ? qq.y : qq.x) * iu, x1 = (c ? qq.w : qq.z) * iu;
+                            const float d0 = rintf(x0), d1 = rintf(x1);
+                            const float l0 = x0 - d0, l1 = x1 - d1;
+                            h1[h] = __floats2half2_rn(l0, l1);
+                            const float2 f1 = __half22float2(h1[h]);
+                            h2[h] = __floats2half2_rn(l0 - f1.x, l1 - f1.y);
+                            hd[h] = __floats2half2_rn(d0, d1);
+                        }
                         // level l plane: A layout 2 l + c, B layout 3 l + c (+ the negated real part at 3 l + 2)
                         const int ls = blay ? 3 : 2;
                         uint8_t* pD = planes + c * ps_ + off;
-                        *reinterpret_cast<__half2*>(pD) = hd;
-                        *reinterpret_cast<__half2*>(pD + ls * ps_) = h1;
-                        *reinterpret_cast<__half2*>(pD + 2 * ls * ps_) = h2;
+                        st_h4(pD, hd[0], hd[1]);
+                        st_h4(pD + ls * ps_, h1[0], h1[1]);
+                        st_h4(pD + 2 * ls * ps_, h2[0], h2[1]);
                         if (blay && c == 0) {
                             uint8_t* pN = planes + 2 * ps_ + off;
-                            *reinterpret_cast<__half2*>(pN) = __hneg2(hd);
-                            *reinterpret_cast<__half2*>(pN + 3 * ps_) = __hneg2(h1);
-                            *reinterpret_cast<__half2*>(pN + 6 * ps_) = __hneg2(h2);
+                            st_h4(pN, __hneg2(hd[0]), __hneg2(hd[1]));
+                            st_h4(pN + 3 * ps_, __hneg2(h1[0]), __hneg2(h1[1]));
+                            st_h4(pN + 6 * ps_, __hneg2(h2[0]), __hneg2(h2[1]));
                         }
                     }
                 }
