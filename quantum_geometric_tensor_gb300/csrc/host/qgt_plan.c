@@ -2455,7 +2455,33 @@ int qgt_plan_schedule_dump(const void* circuit, const void* options, const char*
             const qgt_dev_entry_t* en = &p->ents_h[ps->ent_begin + e];
             fprintf(f, "%s[%d, %d, %d, %d]", e ? ", " : "", en->src_row, en->dst_row, en->spawn_op, en->flags);
         }
+        /* the register programs in full (kind, ra, rb, seg, slot, coef, q, q2, gen), the pass's tile
+         * (local bit -> physical qubit) and the start op of each entry */
+        fprintf(f, "], \"tile_bits\": %d, \"l2p\": [", ps->tile_bits);
+        for (int b = 0; b < 16; b++) fprintf(f, "%s%d", b ? ", " : "", (int)ps->l2p[b]);
+        fprintf(f, "], \"prog2\": [");
+        for (int j = 0; j < ps->prog_count; j++) {
+            const qgt_dev_op2_t* o = &p->prog_h[ps->prog_begin + j];
+            fprintf(f, "%s[%d, %d, %d, %d, %d, %d, %d, %d, %d]", j ? ", " : "", (int)o->kind, (int)o->ra, (int)o->rb,
+                    (int)o->seg, o->slot, o->coef, (int)o->q, (int)o->q2, (int)o->gen);
+        }
+        fprintf(f, "], \"starts\": [");
+        for (int e = 0; e < ps->ent_count; e++)
+            fprintf(f, "%s%d", e ? ", " : "", p->ents_h[ps->ent_begin + e].start_op);
         fprintf(f, "]}");
+    }
+    fprintf(f, "],\n\"reg_bits\": %d, \"ncoef\": %d, \"segs\": [", p->nprog ? reg_bits(p) : 0, p->ncoef);
+    for (int g = 0; g < p->nsegs; g++) {
+        fprintf(f, "%s[", g ? ", " : "");
+        for (int b = 0; b < 16; b++) fprintf(f, "%s%d", b ? ", " : "", (int)p->segs_h[16 * g + b]);
+        fprintf(f, "]");
+    }
+    fprintf(f, "], \"comb\": [");
+    for (int k = 0; k < p->ncomb; k++) {
+        fprintf(f, "%s[", k ? ", " : "");
+        for (int i = p->comb_ptr_h[k]; i < p->comb_ptr_h[k + 1]; i++)
+            fprintf(f, "%s%d", i > p->comb_ptr_h[k] ? ", " : "", p->comb_src_h[i]);
+        fprintf(f, "]");
     }
     fprintf(f, "]}\n");
     fclose(f);
