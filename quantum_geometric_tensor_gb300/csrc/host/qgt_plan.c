@@ -1417,7 +1417,8 @@ int qgt_plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, 
 }
 
 /* host_only: 0 a full plan; 1 the schedule without checkpoints (qgt_plan_schedule_dump); 2 the
- * schedule with checkpoints (qgt_plan_jit_check); 1 and 2 hold no device resources */
+ * schedule with checkpoints (qgt_plan_jit_check, qgt_plan_schedule_dump_ckpt); 1 and 2 hold no device
+ * resources */
 static int plan_create(const qgt_circuit_desc_t* c, const qgt_plan_options_t* opt, qgt_plan_t** out, int host_only)
 {
     int rc = 0;
@@ -2414,12 +2415,24 @@ int qgt_plan_combine_slots(qgt_plan_t* p, const double* c, double* out)
 /* The compiled schedule as JSON (no device needed): passes with their gate
  * ops and vector entries, coefficient sources and the row layout.  Used by
  * the CPU tests, which replay it against the FP64 oracle. */
+static int schedule_dump(const void* circuit, const void* options, const char* path, int host_only);
+
 int qgt_plan_schedule_dump(const void* circuit, const void* options, const char* path)
+{
+    return schedule_dump(circuit, options, path, 1);
+}
+
+int qgt_plan_schedule_dump_ckpt(const void* circuit, const void* options, const char* path)
+{
+    return schedule_dump(circuit, options, path, 2);
+}
+
+static int schedule_dump(const void* circuit, const void* options, const char* path, int host_only)
 {
     const qgt_circuit_desc_t* c = (const qgt_circuit_desc_t*)circuit;
     const qgt_plan_options_t* opt = (const qgt_plan_options_t*)options;
     qgt_plan_t* p = NULL;
-    int rc = plan_create(c, opt, &p, 1);
+    int rc = plan_create(c, opt, &p, host_only);
     if (rc) return rc;
     FILE* f = fopen(path, "w");
     if (!f) { qgt_plan_destroy(p); return qgt_set_error(E_INVAL, "qgt_plan_schedule_dump: cannot write %s", path); }
@@ -2457,7 +2470,7 @@ int qgt_plan_schedule_dump(const void* circuit, const void* options, const char*
         }
         /* the register programs in full (kind, ra, rb, seg, slot, coef, q, q2, gen), the pass's tile
          * (local bit -> physical qubit) and the start op of each entry */
-        fprintf(f, "], \"tile_bits\": %d, \"l2p\": [", ps->tile_bits);
+        fprintf(f, "], \"ckpt_writer\": %d, \"tile_bits\": %d, \"l2p\": [", ps->ckpt_writer, ps->tile_bits);
         for (int b = 0; b < 16; b++) fprintf(f, "%s%d", b ? ", " : "", (int)ps->l2p[b]);
         fprintf(f, "], \"prog2\": [");
         for (int j = 0; j < ps->prog_count; j++) {

@@ -215,6 +215,9 @@ int qgt_plan_launches(const struct qgt_plan* p);
 /* the host-side schedule of a circuit as JSON, without a device (circuit /
  * options: qgt_circuit_desc_t / qgt_plan_options_t of qgt_gb300.h) */
 int qgt_plan_schedule_dump(const void* circuit, const void* options, const char* path);
+/* the same with the segment checkpoints of the register-tile passes (a writer entry first; entries
+ * that start at a later segment read its checkpoint row) */
+int qgt_plan_schedule_dump_ckpt(const void* circuit, const void* options, const char* path);
 
 /* thread-local last error (host/qgt_error.c): stores the message and returns code */
 int qgt_set_error(int code, const char* fmt, ...);

@@ -22,6 +22,8 @@ import pytest
 from oracle import oracle as O
 from test_schedule_replay import INV, QENT_SRC_ZERO, apply_1q, apply_op, gate_matrix, generator
 
+QENT_STORE_V = 1
+
 RL_REG, RL_WARP, RL_OUT = 8, 16, 32
 Q2_SEG, Q2_U, Q2_UR, Q2_PHASE, Q2_CZ, Q2_CNOT, Q2_DIAG, Q2_CZT, Q2_ZGEN, Q2_UM = 1, 2, 3, 4, 5, 6, 7, 9, 10, 11
 GEN = {1: np.array([[0, 1], [1, 0]]), 2: np.array([[0, -1j], [1j, 0]]), 3: np.diag([1, -1])}
@@ -35,7 +37,7 @@ def Q():
     return Q
 
 
-def dump(Q, n, gates, P, precision, transport, tmp_path, **opts):
+def dump(Q, n, gates, P, precision, transport, tmp_path, ckpt=False, **opts):
     d = Q.circuit_desc(n, gates, P)
     o = Q.PlanOptions()
     Q.lib().qgt_plan_default_options(C.byref(o))
@@ -43,8 +45,9 @@ def dump(Q, n, gates, P, precision, transport, tmp_path, **opts):
     for k, v in opts.items():
         setattr(o, k, v)
     path = str(tmp_path / "sched.json")
-    rc = Q.lib().qgt_plan_schedule_dump(C.cast(C.pointer(d), C.c_void_p), C.cast(C.pointer(o), C.c_void_p),
-                                        path.encode())
+    fn = Q.lib().qgt_plan_schedule_dump_ckpt if ckpt else Q.lib().qgt_plan_schedule_dump
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_char_p]
+    rc = fn(C.cast(C.pointer(d), C.c_void_p), C.cast(C.pointer(o), C.c_void_p), path.encode())
     assert rc == 0, Q.lib().qgt_last_error()
     with open(path) as f:
         return json.load(f)
@@ -168,7 +171,9 @@ class Program:
             v = self.gen(v, g, q)
         return v, pc + cnt
 
-    def run(self, v, start, spawn):
+    def run(self, v, start, spawn, ckpt=None):
+        """The entry's vector from program op `start` (a layout switch) to the end; with `ckpt` (the
+        checkpoint writer) the state before every layout switch that carries a checkpoint row."""
         assert self.prog[start][0] == Q2_SEG
         lay = self.layout(self.prog[start][3])
         pc = start + 1
@@ -176,6 +181,8 @@ class Program:
             op = self.prog[pc]
             kind = op[0]
             if kind == Q2_SEG:
+                if ckpt is not None and op[4] >= 0:
+                    ckpt[op[4]] = v.copy()
                 lay = self.layout(op[3])
             elif kind == Q2_DIAG:
                 v, pc = self.diag(v, pc, lay, spawn)
@@ -212,6 +219,7 @@ def replay_programs(orc, plan, theta, n):
     zero[0] = 1
     h_done = False
     nprog = 0
+    stats = {"ckpt_starts": 0}
 
     def ham():
         src = plan["row_T"] if plan["mitm"] else 0
@@ -223,18 +231,27 @@ def replay_programs(orc, plan, theta, n):
             h_done = True
         snap = dict(rows)
         out = {}
+        ck = {}   # checkpoint rows of this pass: written by its first entry, read by later ones
         prog = Program(plan, ps, theta, n) if ps["prog2"] else None
         nprog += prog is not None
         for k, (src, dst, spawn, flags) in enumerate(ps["entries"]):
-            v = zero.copy() if flags & QENT_SRC_ZERO else snap[src].copy()
+            if flags & QENT_SRC_ZERO:
+                v = zero.copy()
+            else:
+                v = (ck[src] if src in ck else snap[src]).copy()
             if prog is not None:
-                v = prog.run(v, ps["starts"][k], spawn)
+                writer = k == 0 and ps.get("ckpt_writer", 0)
+                nck = len(ck)
+                v = prog.run(v, ps["starts"][k], spawn, ck if writer else None)
+                assert writer or len(ck) == nck
+                stats["ckpt_starts"] += ps["starts"][k] > 0
             else:
                 for op in ps["ops"]:
                     v = apply_op(v, op, plan["coefs"], theta)
                     if spawn >= 0 and op[4] == dst - 2:
                         v = generator(v, op)
-            out[dst] = v
+            if flags & QENT_STORE_V:
+                out[dst] = v
         rows.update(out)
     if not h_done:
         ham()
@@ -252,7 +269,7 @@ def replay_programs(orc, plan, theta, n):
     Qm = B / s - np.outer(v, v.conj()) / s ** 2
     E = HG[0, 1].real / s
     grad = 2 * (M @ HG[:, 1]).real / s - 2 * E * v.real / s
-    return Qm, grad, nprog
+    return Qm, grad, nprog, stats
 
 
 def rel(a, b):
@@ -267,7 +284,7 @@ def test_register_programs_match_oracle(Q, orc, tmp_path, precision, n, L, ent, 
     P = 2 * n * L
     th = O.splitmix64_params(700 + n, P)
     plan = dump(Q, n, gates, P, precision, transport, tmp_path)
-    Qm, grad, nprog = replay_programs(orc, plan, th, n)
+    Qm, grad, nprog, _ = replay_programs(orc, plan, th, n)
     assert nprog > 0   # the register-tile passes really went through their programs
     psi, D = orc.derivatives(n, O.gates_array(gates), th)
     assert rel(Qm, orc.qgt_from_states(psi, D)) < 1e-11
@@ -282,7 +299,7 @@ def test_register_programs_random_circuit(Q, orc, tmp_path):
     th = O.splitmix64_params(11, P)
     for transport in (1, 2):
         plan = dump(Q, n, gates, P, 1, transport, tmp_path)
-        Qm, grad, nprog = replay_programs(orc, plan, th, n)
+        Qm, grad, nprog, _ = replay_programs(orc, plan, th, n)
         assert nprog > 0
         psi, D = orc.derivatives(n, O.gates_array(gates), th, P)
         assert rel(Qm, orc.qgt_from_states(psi, D)) < 1e-11
@@ -299,8 +316,24 @@ def test_register_programs_other_tiles(Q, orc, tmp_path, opts):
     plan = dump(Q, n, gates, P, 1, 2, tmp_path, **opts)
     assert plan["passes"] and all(ps["tile_bits"] == opts.get("tile_bits", 13) for ps in plan["passes"] if ps["prog2"])
     assert plan["reg_bits"] == (4 if opts.get("thread_amps") == 16 else 5)
-    Qm, grad, nprog = replay_programs(orc, plan, th, n)
+    Qm, grad, nprog, _ = replay_programs(orc, plan, th, n)
     assert nprog > 0
+    psi, D = orc.derivatives(n, O.gates_array(gates), th)
+    assert rel(Qm, orc.qgt_from_states(psi, D)) < 1e-11
+    assert rel(grad, orc.energy_grad(D, orc.tfim_apply(n, psi))) < 1e-11
+
+
+@pytest.mark.parametrize("precision,n,L,ent,transport", [(1, 16, 4, "cz", 2), (1, 16, 4, "cnot", 1), (0, 13, 3, "cz", 2)])
+def test_register_programs_with_checkpoints(Q, orc, tmp_path, precision, n, L, ent, transport):
+    """Segment checkpoints: a pass's first entry stores its state before every segment that a
+    group of spawns starts in, and those spawns run from their segment on the stored state."""
+    gates = Q.ansatz_gates(n, L, ent)
+    P = 2 * n * L
+    th = O.splitmix64_params(900 + n, P)
+    plan = dump(Q, n, gates, P, precision, transport, tmp_path, ckpt=True)
+    assert any(ps.get("ckpt_writer") for ps in plan["passes"])
+    Qm, grad, nprog, stats = replay_programs(orc, plan, th, n)
+    assert nprog > 0 and stats["ckpt_starts"] > 0
     psi, D = orc.derivatives(n, O.gates_array(gates), th)
     assert rel(Qm, orc.qgt_from_states(psi, D)) < 1e-11
     assert rel(grad, orc.energy_grad(D, orc.tfim_apply(n, psi))) < 1e-11
