@@ -20,7 +20,7 @@
 // rounding is ~1e-8 relative to the sum.
 //
 // Data path per CTA (tile pair mb <= nb, K range of <= 1024 amplitudes):
-//   TMA: 128 rows x 16 amplitudes of complex64 per row block -> raw smem
+//   TMA: 128 rows x 16 amplitudes of complex64 per row block -> raw smem (128-byte swizzle)
 //   8 converter warps: raw -> FP16 planes in the SWIZZLE_32B K-major UMMA
 //                      layout: the A block as 6 planes {Re D, Im D, Re l1,
 //                      Im l1, Re l2, Im l2}, the B block as 9 planes
@@ -389,8 +389,11 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
                         // rlim is a multiple of 16, so a group of 8 rows is all below it or all above
                         const int rr = 8 * cw + 8 * DG_CONV_WARPS * it, r = rr + sub;
                         if (b < nblk && rr < rlim) {
-                            q[b][it][0] = *reinterpret_cast<const float4*>(raw + r * 32 + 2 * kq);
-                            q[b][it][1] = *reinterpret_cast<const float4*>(raw + r * 32 + 2 * kq + 4);
+                            // the raw rows arrive 128-byte swizzled (16-byte chunk c of row r at
+                            // c ^ (r & 7)), so the two rows of a quarter-warp read different banks
+                            const int sw = r & 7, c0 = kq >> 1;
+                            q[b][it][0] = *reinterpret_cast<const float4*>(raw + r * 32 + 4 * (c0 ^ sw));
+                            q[b][it][1] = *reinterpret_cast<const float4*>(raw + r * 32 + 4 * ((c0 + 1) ^ sw));
                             iuv[b][it] = inv_u[b][r];
                         } else {
                             q[b][it][0] = q[b][it][1] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -648,7 +651,7 @@ extern "C" int qgt_dev_dg_gram_create(const void* V, int64_t N, int32_t rows, co
     cuuint32_t box[3] = {2 * DG_BK, 128, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = enc(&g->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)V, dims, strides, box, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         free(g);
